@@ -1,0 +1,377 @@
+"""Benchmark: SSA velocity solves per second on one GB300 (UFEMISM ice-velocity solve).
+
+Workload: the 200k-vertex dome (2 km at the margin grading to 20 km, seeded jitter; about
+800k AaAc rows), Vialov dome H0 = 3600 m, R = 750 km, flat bed, A = 1e-16 Pa^-3 yr^-1, linear
+sliding beta^2 = 1e3 Pa yr/m, Picard tolerance 1e-3, SOR omega 1.3, SOR tolerance 1e-4 m/yr.
+One step = one full cold-start solve_SSA (every Picard iteration and SOR sweep until the
+reference's stopping rules fire).
+
+  value   mixed-precision solves/s, inputs resident in HBM (ufe_ssa_run)
+  e2e     the same through ufe_ssa_solve with host buffers (H2D + solve + D2H each step)
+  fp64    the plain FP64 path, same workload
+  roofline  the persistent SSA kernel: algorithmic bytes per launch / launch time vs HBM peak
+
+``--impl reference`` times the reference algorithm on the host cores: the CPU oracle (a C
+restatement of the Fortran routines; the Fortran reference cannot be built on this image),
+on a bounded sample of the same solve, extrapolated to solves/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SSA solves/s mixed vs FP64 on GB300 @ rel-L2<=1e-6; sweep HBM GB/s; adjoint ms"
+UNIT = "solves/s"
+WORKLOAD = "200k-vertex dome SSA cold-start solve"
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(size: str):
+    from ufemism_gb300 import api, workloads
+    from ufemism_gb300.meshgen import dome_mesh
+    base = dome_mesh(size)
+    mesh = api.build_aaac(base)
+    Hi, Hb, SL = workloads.dome_geometry(base)
+    ssa, sia = workloads.prepare_inputs(mesh, Hi, Hb, SL)
+    return base, mesh, ssa, sia
+
+
+def mesh_counts(mesh):
+    nV = mesh.base.nV
+    nA = mesh.nVAaAc
+    is_edge = np.concatenate([mesh.base.edge_index > 0, mesh.edge_index_Ac > 0])
+    nnz_all = int(mesh.nCAaAc.sum())
+    nnz_act = int(mesh.nCAaAc[~is_edge].sum())
+    n_act = int((~is_edge).sum())
+    n_edge = int(is_edge.sum())
+    # Neumann lists: edge rows' non-edge neighbours (+ corners' neighbours)
+    nb_bnd = 0
+    for ai in np.flatnonzero(is_edge):
+        nb = mesh.CAaAc[ai, : mesh.nCAaAc[ai]] - 1
+        nb_bnd += int((~is_edge[nb]).sum()) if ai >= 4 else len(nb)
+    return dict(nV=nV, nA=nA, nnz_all=nnz_all, nnz_act=nnz_act, n_act=n_act, n_edge=n_edge, nb_bnd=nb_bnd)
+
+
+def algorithmic_bytes(c, st, mixed: bool, refold: int = 32):
+    """Compulsory DRAM bytes of one persistent-kernel launch (each array touched once per
+    phase; neighbour gathers of U,V counted once through the row's own U,V)."""
+    if not mixed:
+        sweep = c["n_act"] * (16 + 16 + 16 + 16 + 8 + 1) + c["nnz_act"] * (4 + 16)
+    else:
+        sweep = c["n_act"] * (8 + 8 + 8 + 8 + 4 + 1) + c["nnz_act"] * (4 + 8)
+    bnd = c["n_edge"] * (16 + 4) + c["nb_bnd"] * 4 + (c["n_edge"] * (8 if mixed else 0))
+    sweep += bnd
+    # viscosity: U,V + home coefs + A + H + eta + N (w) + Nprev (r) + deg; entries col + (Nx,Ny)
+    visc = c["nA"] * (16 + 16 + 8 + 8 + 8 + 8 + 8 + 1) + c["nnz_all"] * (4 + (8 if mixed else 16))
+    # coefficients: U,V + tau/beta + eta + H + Hb + SL + hx + hy + home cuv -> S, rhs, euv (+euv32)
+    coef = c["nA"] * (16 + 8 + 8 + 8 + 8 + 8 + 8 + 8 + 16 + 8) + c["n_act"] * (16 + 16 + (8 if mixed else 0))
+    total = st["total_sweeps"] * sweep + st["picard_iterations"] * visc + st["linear_solves"] * coef
+    if mixed:
+        defect = c["n_act"] * (16 + 8 + 16 + 16 + 8 + 1) + c["nnz_act"] * (4 + 16)
+        fold = c["nA"] * (8 + 16 + 16 + 8)
+        n_refold = sum(max(0, (s - 1) // refold) for s in st["sweeps"]) if st.get("sweeps") else 0
+        total += (st["linear_solves"] + n_refold) * defect + (st["linear_solves"] + n_refold) * fold
+    return int(total), int(sweep)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        try:
+            rows = [l.strip().split(", ") for l in open(self.path) if l.strip()]
+        except Exception:
+            return out
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        out.update(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                   reasons=sorted(reasons), samples=len(rows))
+        try:
+            os.unlink(self.path)
+        except Exception:
+            pass
+        return out
+
+
+def timed_runs(dm, params, steps, warmup, stream_ptr):
+    """Device-resident solves: ufe_ssa_run on the uploaded inputs, timed with CUDA events
+    recorded on the handle's stream. Returns per-step ms and the stats of the last run."""
+    import torch
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    st = None
+    for _ in range(warmup):
+        rc, st = dm.ssa_run(params)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        rc, st = dm.ssa_run(params)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    return times, st
+
+
+def cpu_baseline(mesh, ssa, gpu_stats, sample_sweeps=120, threads=None):
+    """The oracle (C restatement of the reference's FP64 solve) on the host cores: one
+    viscosity update and ``sample_sweeps`` SOR sweeps of the same workload (replay mode),
+    extrapolated with the full solve's sweep and Picard counts."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    om = orc.build_aaac(mesh.base)
+    t_mesh = time.perf_counter() - t0
+    p1 = orc.default_params(n_threads=threads, replay_picard=1)
+    t0 = time.perf_counter()
+    orc.solve_ssa(om, ssa, p1)
+    t_visc = time.perf_counter() - t0
+    p2 = orc.default_params(n_threads=threads, replay_picard=2,
+                            replay_sweeps=np.array([sample_sweeps, 0], dtype=np.int32))
+    t0 = time.perf_counter()
+    orc.solve_ssa(om, ssa, p2)
+    t_two = time.perf_counter() - t0
+    t_sweep = max(t_two - 2 * t_visc, 1e-9) / sample_sweeps
+    full = gpu_stats["total_sweeps"] * t_sweep + gpu_stats["picard_iterations"] * t_visc
+    return dict(value=1.0 / full, unit=UNIT, cores=threads, kind="port",
+                sample="oracle FP64 solve on %d host threads: %d SOR sweeps + 2 viscosity updates of the "
+                       "200k-vertex dome (%.3f s/sweep, %.3f s/viscosity), extrapolated to the full solve's "
+                       "%d sweeps and %d Picard iterations" % (threads, sample_sweeps, t_sweep, t_visc,
+                                                              gpu_stats["total_sweeps"],
+                                                              gpu_stats["picard_iterations"]),
+                seconds_per_solve=full, mesh_build_s=t_mesh)
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    base, mesh, ssa, sia = make_workload(args.size)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    threads = os.cpu_count() or 1
+    om = orc.build_aaac(mesh.base)
+    # Full-solve iteration counts of this workload (from the oracle's own 8-thread run of the
+    # same seeded problem): 13558 SOR sweeps over 8 linear solves, 9 Picard iterations.
+    counts = dict(total_sweeps=13558, picard_iterations=9)
+    sample = args.ref_sample_sweeps
+    times = []
+    for i in range(args.warmup + args.steps):
+        p1 = orc.default_params(n_threads=threads, replay_picard=1)
+        t0 = time.perf_counter()
+        orc.solve_ssa(om, ssa, p1)
+        t_visc = time.perf_counter() - t0
+        p2 = orc.default_params(n_threads=threads, replay_picard=2,
+                                replay_sweeps=np.array([sample, 0], dtype=np.int32))
+        t0 = time.perf_counter()
+        orc.solve_ssa(om, ssa, p2)
+        t_two = time.perf_counter() - t0
+        t_sweep = max(t_two - 2 * t_visc, 1e-9) / sample
+        if i >= args.warmup:
+            times.append(counts["total_sweeps"] * t_sweep + counts["picard_iterations"] * t_visc)
+    sec = statistics.median(times)
+    value = 1.0 / sec
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dome geometry and mesh)",
+        "config": {"workload": WORKLOAD, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc), "precision": "fp64",
+                   "l2": "n/a (CPU)"},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "per step: 1 viscosity update + %d SOR sweeps of the 200k-vertex dome solve by the "
+                                   "oracle (C restatement of the Fortran routines) on %d host threads, extrapolated to "
+                                   "13558 sweeps / 9 Picard iterations" % (sample, threads)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", default="200k")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-sample-sweeps", type=int, default=40)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    rank, world, local = dist_info()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api
+    api.init(local)
+
+    base, mesh, ssa, sia = make_workload(args.size)
+    dm = api.DeviceMesh(mesh)
+    counts = mesh_counts(mesh)
+    p64 = api.default_params(precision=nat.UFE_FP64)
+    p32 = api.default_params(precision=nat.UFE_MIXED)
+
+    # accuracy of the mixed path against the FP64 path (which matches the oracle to 1e-10)
+    rc64, o64, s64 = dm.solve_ssa(ssa, p64)
+    rc32, o32, s32 = dm.solve_ssa(ssa, p32)
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    l2 = max(rel(o32[k], o64[k]) for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac"))
+
+    dm.ssa_upload(ssa, p64)
+    stream_ptr = dm.stream
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t64, st64 = timed_runs(dm, p64, args.steps, args.warmup, stream_ptr)
+        t32, st32 = timed_runs(dm, p32, args.steps, args.warmup, stream_ptr)
+    clocks = clk.summary()
+    torch.cuda.synchronize()
+    ms32 = float(np.mean(t32))
+    ms64 = float(np.mean(t64))
+    if world > 1:
+        tt = torch.tensor([ms32, ms64], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms32, ms64 = float(tt[0]), float(tt[1])
+    value = world * 1000.0 / ms32
+    fp64_value = world * 1000.0 / ms64
+
+    # e2e: host buffers through ufe_ssa_solve (H2D inputs, solve, D2H results) each step
+    h2d = sum(np.asarray(v).nbytes for k, v in ssa.items()
+              if k in ("Hi", "Hb", "SL", "dHs_dx_shelf", "dHs_dy_shelf", "A_flow_mean", "mask_sheet", "Hi_Ac",
+                       "Hb_Ac", "SL_Ac", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac", "A_flow_mean_Ac"))
+    h2d += 8 * (2 * base.nV + 2 * mesh.nAc + mesh.nVAaAc)   # warm start + Picard state
+    d2h = 8 * (2 * base.nV + 4 * mesh.nAc + 5 * mesh.nVAaAc)
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc, out, st = dm.solve_ssa(ssa, p32)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_value = world * 1000.0 / float(np.mean(e2e_ms))
+
+    peak, peak_kind = load_peaks()
+    bytes32, sweep32 = algorithmic_bytes(counts, st32, True)
+    bytes64, sweep64 = algorithmic_bytes(counts, st64, False)
+    ach32 = bytes32 / (ms32 * 1e-3) / 1e9
+    ach64 = bytes64 / (ms64 * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "ssa_persistent_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("dram_bytes_per_launch_scaled")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 sweeps / f64 defect", "data": "synthetic (seeded dome geometry and mesh)",
+        "config": {"workload": WORKLOAD, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc),
+                   "nnz": counts["nnz_all"], "precision": "mixed", "sliding": "linear beta^2=1e3",
+                   "picard_iterations": st32["picard_iterations"], "sor_sweeps": st32["total_sweeps"],
+                   "l2": "inputs and coefficient arrays (> 300 MB) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms64, "sor_sweeps": st64["total_sweeps"],
+                 "picard_iterations": st64["picard_iterations"],
+                 "vertex_sweeps_per_s": counts["nA"] * st64["total_sweeps"] / (ms64 * 1e-3),
+                 "achieved_gbs": ach64, "frac": ach64 / peak},
+        "mixed_vs_fp64_speedup": fp64_value and value / fp64_value,
+        "rel_l2_mixed_vs_fp64": l2,
+        "vertex_sweeps_per_s": counts["nA"] * st32["total_sweeps"] / (ms32 * 1e-3),
+        "roofline": {"bound": "hbm", "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "ssa_persistent<mixed>",
+                     "algorithmic_bytes_per_launch": bytes32, "bytes_per_sweep": sweep32},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        # k_gather + ssa_persistent + k_scatter per mixed solve in the timed region
+        "gpu_launches": 3 * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(mesh, ssa, st64)
+        line["cpu_baseline"].pop("mesh_build_s", None)
+        line["cpu_baseline"].pop("seconds_per_solve", None)
+    dm.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,217 @@
+/*
+ * ufemism_gb300 -- C-ABI of the GB300 (sm_103a) ice-velocity solver for UFEMISM.
+ *
+ * Drop-in boundary for the two Fortran call sites of the reference model:
+ *   CALL solve_SIA( region%mesh, region%ice)   UFEMISM_main_model.f90:124
+ *   CALL solve_SSA( region%mesh, region%ice)   UFEMISM_main_model.f90:132
+ * A Fortran wrapper with the same names and signatures (ice_dynamics_module.f90:240-249 and
+ * 408-417) passes raw pointers of the type_mesh / type_ice_model components
+ * (data_types_module.f90:15-345) to the functions below through ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Every array is in the reference's own layout: 2-D arrays column-major (Fortran order)
+ *    with their allocated leading dimension, index VALUES 1-based, unused neighbour slots 0.
+ *    Floating point is double (REAL(dp)), integers int32_t (default INTEGER).
+ *  - The library copies host arrays in and out during each call and keeps no host pointer
+ *    after it returns. Device buffers live in the opaque mesh handle; the handle must be
+ *    destroyed and re-created after a mesh update (run_model_update_mesh,
+ *    UFEMISM_main_model.f90:240-315).
+ *  - Calls on one handle are not re-entrant; each handle owns one CUDA stream and the host
+ *    thread blocks until results are back. The Fortran wrapper calls from the master rank
+ *    only, then CALL sync (all ranks see the results in the shared windows).
+ *  - Return value: 0 = UFE_OK, > 0 a warning, < 0 an error. ufe_last_error_string() gives a
+ *    thread-local message for the last non-zero status.
+ *  - There is no CPU fallback: without a usable sm_103a device every solve returns
+ *    UFE_NO_DEVICE.
+ */
+#ifndef UFEMISM_GB300_H
+#define UFEMISM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UFE_ABI_VERSION 1
+
+/* Status codes. The warnings and errors mirror the reference's failure handling:
+ *   UFE_NOT_CONVERGED  SOR hit SSA_max_inner_loops: WRITE(0,*) warning, ice_dynamics_module.f90:685-689
+ *   UFE_RESET_ONCE     velocities reset to zero once after max residual > 1e6, 676-684
+ *   UFE_DIVERGED       second reset: the reference calls MPI_ABORT, 532-540
+ *   UFE_BAD_MESH       make_combined_AaAc_mesh / check_solution aborts
+ *   UFE_COLOUR_IDENTIFY the five-colouring reached 'identify', where the reference aborts
+ *                      unconditionally (mesh_five_colour_module.f90:452)
+ *   UFE_TIMEOUT        a bounded device-side wait (inter-CTA colour barrier) ran out */
+enum {
+  UFE_OK = 0,
+  UFE_NOT_CONVERGED = 1,
+  UFE_RESET_ONCE = 2,
+  UFE_DIVERGED = -1,
+  UFE_BAD_MESH = -2,
+  UFE_COLOUR_IDENTIFY = -3,
+  UFE_TIMEOUT = -4,
+  UFE_CUDA_ERROR = -5,
+  UFE_BAD_ARG = -6,
+  UFE_NO_DEVICE = -7,
+  UFE_OUT_OF_MEMORY = -8,
+};
+
+enum { UFE_FP64 = 0, UFE_MIXED = 1 };
+enum { UFE_SLIDING_COULOMB_REGULARISED = 0, UFE_SLIDING_LINEAR = 1 };
+
+/* Mesh as held by the reference's type_mesh (data_types_module.f90:216-345), after
+ * make_Ac_mesh (mesh_ArakawaC_module.f90:24-241), make_combined_AaAc_mesh (286-540) and
+ * calculate_five_colouring_AaAc (mesh_five_colour_module.f90:18-137). */
+typedef struct ufe_mesh_desc {
+  int32_t nV, nAc, nVAaAc, nC_mem;
+  const double *V;             /* (nV,2) vertex x,y */
+  const int32_t *nC;           /* (nV) */
+  const int32_t *iAci;         /* (nV,nC_mem) Aa->Ac map */
+  const int32_t *Aci;          /* (nAc,4) [vi,vj,vl,vr] */
+  const int32_t *edge_index;   /* (nV) */
+  const int32_t *edge_index_Ac;/* (nAc) */
+  const int32_t *nCAaAc;       /* (nVAaAc) */
+  const int32_t *CAaAc;        /* (nVAaAc,nC_mem) */
+  const double *Nx_AaAc, *Ny_AaAc, *Nxx_AaAc, *Nxy_AaAc, *Nyy_AaAc; /* (nVAaAc,nC_mem+1) */
+  const int32_t *colour;       /* (nVAaAc) 1..5 */
+  const int32_t *colour_vi;    /* (nVAaAc,5) */
+  const int32_t *colour_nV;    /* (5) */
+} ufe_mesh_desc;
+
+/* SSA/SIA knobs (configuration_module.f90:124-126, 169-184) as a POD struct. */
+typedef struct ufe_params {
+  double SSA_RN_tol;
+  int32_t SSA_max_outer_loops;
+  double SSA_max_residual_UV;
+  double SSA_SOR_omega;
+  int32_t SSA_max_inner_loops;
+  double m_enh_ssa, m_enh_sia;
+  int32_t sliding_law;            /* UFE_SLIDING_* ; linear is this library's extension */
+  double beta_sq;                 /* linear law, used when ufe_ssa_in.beta_sq_AaAc is NULL */
+  int32_t use_analytical_GL_flux;
+  int32_t zero_velocities;        /* benchmark experiments that skip the SSA (431-449) */
+  int32_t nZ;
+  const double *zeta;             /* (nZ) */
+  int32_t precision;              /* UFE_FP64 or UFE_MIXED */
+  int32_t mixed_refold_sweeps;    /* mixed: FP64 defect recomputed every this many sweeps (0 = default) */
+} ufe_params;
+
+/* Inputs of solve_SSA (type_ice_model fields). Aa arrays have nV entries, Ac arrays nAc. */
+typedef struct ufe_ssa_in {
+  const double *Hi, *Hb, *SL, *dHs_dx_shelf, *dHs_dy_shelf, *A_flow_mean;
+  const int32_t *mask_sheet;
+  const double *Hi_Ac, *Hb_Ac, *SL_Ac, *dHs_dx_shelf_Ac, *dHs_dy_shelf_Ac, *A_flow_mean_Ac;
+  const double *beta_sq_AaAc;     /* (nVAaAc) linear law field, or NULL */
+  /* only with use_analytical_GL_flux */
+  const int32_t *mask_gl_Ac;
+  const double *dHi_dx_Ac, *dHi_dy_Ac, *dSL_dx_Ac, *dSL_dy_Ac, *dHb_dx_Ac, *dHb_dy_Ac;
+} ufe_ssa_in;
+
+/* Warm start in, solution out (INTENT(INOUT) in the reference). N_AaAc is the Picard state
+ * that persists in the ice model between calls; NULL means zeros and no write-back. */
+typedef struct ufe_ssa_inout {
+  double *U_SSA, *V_SSA;          /* (nV) */
+  double *Ux_SSA_Ac, *Uy_SSA_Ac;  /* (nAc) */
+  double *N_AaAc;                 /* (nVAaAc) or NULL */
+} ufe_ssa_inout;
+
+/* Optional outputs; any pointer may be NULL. */
+typedef struct ufe_ssa_out {
+  double *Up_SSA_Ac, *Uo_SSA_Ac;  /* (nAc) rotate_xy_to_po, mesh_ArakawaC_module.f90:815-844 */
+  double *eta_AaAc, *S_AaAc, *tau_c_AaAc, *phi_fric_AaAc; /* (nVAaAc) */
+} ufe_ssa_out;
+
+typedef struct ufe_ssa_stats {
+  int32_t status;
+  int32_t picard_iterations;
+  int32_t linear_solves;
+  int32_t resets;
+  int32_t not_converged;
+  int64_t total_sweeps;
+  double last_RN;
+  double last_max_residual;
+  int32_t sweeps[64];             /* SOR sweeps of the first 64 linear solves */
+  double device_ms;               /* device time of the solve (CUDA events) */
+} ufe_ssa_stats;
+
+/* Inputs and outputs of solve_SIA (ice_dynamics_module.f90:240-314). */
+typedef struct ufe_sia_in {
+  const int32_t *mask_sheet_Ac;   /* (nAc) */
+  const double *Hi_Ac, *dHs_dx_Ac, *dHs_dy_Ac, *dHs_dp_Ac, *dHs_do_Ac; /* (nAc) */
+  const double *A_flow_Ac;        /* (nAc,nZ) */
+} ufe_sia_in;
+
+typedef struct ufe_sia_out {
+  double *D_SIA_3D_Ac;            /* (nAc,nZ) or NULL */
+  double *D_SIA_Ac, *Ux_SIA_Ac, *Uy_SIA_Ac, *Up_SIA_Ac, *Uo_SIA_Ac; /* (nAc) */
+  double *U_SIA, *V_SIA, *D_SIA;  /* (nV) map_Ac_to_Aa */
+} ufe_sia_out;
+
+typedef struct ufe_mesh_s *ufe_mesh_h;
+
+/* Library version / device probe. Returns UFE_OK when an sm_103 device is usable. */
+int ufe_init(int device);
+const char *ufe_last_error_string(void);
+
+/* Upload a mesh: the colour-sorted device re-layout is built here (once per mesh).
+ * Replaces the per-call use of the mesh arrays by solve_SSA / solve_SIA. */
+int ufe_mesh_create(const ufe_mesh_desc *desc, ufe_mesh_h *out);
+int ufe_mesh_destroy(ufe_mesh_h mesh);
+/* The handle's CUDA stream (cudaStream_t), for callers that time on it. */
+void *ufe_mesh_stream(ufe_mesh_h mesh);
+
+/* solve_SSA, ice_dynamics_module.f90:408-557, including basal_yield_stress (780-844) and,
+ * with use_analytical_GL_flux, calculate_GL_flux (848-949). */
+int ufe_ssa_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_ssa_in *in,
+                  ufe_ssa_inout *inout, ufe_ssa_out *out, ufe_ssa_stats *stats);
+
+/* The same solve split into its transfer and compute parts: ufe_ssa_upload copies the
+ * inputs and warm start into the handle's device buffers, ufe_ssa_run solves from them
+ * (device-resident in, device-resident out, may be called repeatedly on the same
+ * uploaded inputs) and ufe_ssa_download copies the results back. */
+int ufe_ssa_upload(ufe_mesh_h mesh, const ufe_params *params, const ufe_ssa_in *in,
+                   const ufe_ssa_inout *inout);
+int ufe_ssa_run(ufe_mesh_h mesh, const ufe_params *params, ufe_ssa_stats *stats);
+int ufe_ssa_download(ufe_mesh_h mesh, ufe_ssa_inout *inout, ufe_ssa_out *out);
+
+/* solve_SIA, ice_dynamics_module.f90:240-314 with map_Ac_to_Aa (mesh_ArakawaC_module.f90:770-791). */
+int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
+                  ufe_sia_out *out);
+
+/* Host-side mesh substrate: builds the Ac and combined AaAc mesh, the AaAc and Aa
+ * neighbour functions and the five-colouring from a base triangulation, exactly as
+ * make_Ac_mesh (mesh_ArakawaC_module.f90:24-540), get_neighbour_functions
+ * (mesh_derivatives_module.f90:14-313) and calculate_five_colouring_AaAc
+ * (mesh_five_colour_module.f90:18-735) do. For callers that do not run the reference's
+ * Fortran mesh code. Output arrays are caller-allocated with nAc = nV + nTri - 1 and
+ * nVAaAc = nV + nAc; any output pointer may be NULL except those the later steps need. */
+typedef struct ufe_base_mesh {
+  int32_t nV, nTri, nC_mem;
+  const double *V;             /* (nV,2) */
+  const int32_t *nC, *C;       /* (nV), (nV,nC_mem) */
+  const int32_t *niTri, *iTri; /* (nV), (nV,nC_mem) */
+  const int32_t *Tri;          /* (nTri,3) */
+  const int32_t *edge_index;   /* (nV) */
+} ufe_base_mesh;
+
+typedef struct ufe_aaac_mesh {
+  int32_t nAc, nVAaAc;
+  double *Nx, *Ny, *Nxx, *Nxy, *Nyy;   /* (nV,nC_mem+1) Aa neighbour functions */
+  int32_t *iAci, *Aci;                 /* (nV,nC_mem), (nAc,4) */
+  double *VAc;                         /* (nAc,2) */
+  double *Nx_Ac, *Ny_Ac, *No_Ac;       /* (nAc,4) */
+  double *Np_Ac;                       /* (nAc) */
+  int32_t *edge_index_Ac;              /* (nAc) */
+  double *VAaAc;                       /* (nVAaAc,2) */
+  int32_t *nCAaAc, *CAaAc;             /* (nVAaAc), (nVAaAc,nC_mem) */
+  double *Nx_AaAc, *Ny_AaAc, *Nxx_AaAc, *Nxy_AaAc, *Nyy_AaAc; /* (nVAaAc,nC_mem+1) */
+  int32_t *colour, *colour_vi, *colour_nV; /* (nVAaAc), (nVAaAc,5), (5) */
+} ufe_aaac_mesh;
+
+int ufe_aaac_build(const ufe_base_mesh *base, ufe_aaac_mesh *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UFEMISM_GB300_H */

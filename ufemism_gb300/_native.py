@@ -1,0 +1,139 @@
+"""ctypes declarations of the C-ABI in include/ufemism_gb300.h.
+
+The shared library is built in-tree (``ufemism_gb300/_build/libufemism_gb300.so``). There is
+no CPU fallback: loading fails loudly if the library is missing, and every solve reports
+UFE_NO_DEVICE without a usable sm_103a GPU.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+from . import build as _build
+
+P = ct.c_void_p
+I32 = ct.c_int32
+F64 = ct.c_double
+
+UFE_OK, UFE_NOT_CONVERGED, UFE_RESET_ONCE = 0, 1, 2
+UFE_DIVERGED, UFE_BAD_MESH, UFE_COLOUR_IDENTIFY, UFE_TIMEOUT = -1, -2, -3, -4
+UFE_CUDA_ERROR, UFE_BAD_ARG, UFE_NO_DEVICE, UFE_OUT_OF_MEMORY = -5, -6, -7, -8
+UFE_FP64, UFE_MIXED = 0, 1
+UFE_SLIDING_COULOMB_REGULARISED, UFE_SLIDING_LINEAR = 0, 1
+
+STATUS_NAMES = {0: "UFE_OK", 1: "UFE_NOT_CONVERGED", 2: "UFE_RESET_ONCE", -1: "UFE_DIVERGED",
+                -2: "UFE_BAD_MESH", -3: "UFE_COLOUR_IDENTIFY", -4: "UFE_TIMEOUT", -5: "UFE_CUDA_ERROR",
+                -6: "UFE_BAD_ARG", -7: "UFE_NO_DEVICE", -8: "UFE_OUT_OF_MEMORY"}
+
+
+class MeshDesc(ct.Structure):
+    _fields_ = [("nV", I32), ("nAc", I32), ("nVAaAc", I32), ("nC_mem", I32)] + \
+               [(n, P) for n in ("V", "nC", "iAci", "Aci", "edge_index", "edge_index_Ac", "nCAaAc", "CAaAc",
+                                 "Nx_AaAc", "Ny_AaAc", "Nxx_AaAc", "Nxy_AaAc", "Nyy_AaAc", "colour",
+                                 "colour_vi", "colour_nV")]
+
+
+class Params(ct.Structure):
+    _fields_ = [("SSA_RN_tol", F64), ("SSA_max_outer_loops", I32), ("SSA_max_residual_UV", F64),
+                ("SSA_SOR_omega", F64), ("SSA_max_inner_loops", I32), ("m_enh_ssa", F64), ("m_enh_sia", F64),
+                ("sliding_law", I32), ("beta_sq", F64), ("use_analytical_GL_flux", I32),
+                ("zero_velocities", I32), ("nZ", I32), ("zeta", P), ("precision", I32),
+                ("mixed_refold_sweeps", I32)]
+
+
+SSA_IN_FIELDS = ("Hi", "Hb", "SL", "dHs_dx_shelf", "dHs_dy_shelf", "A_flow_mean", "mask_sheet", "Hi_Ac", "Hb_Ac",
+                 "SL_Ac", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac", "A_flow_mean_Ac", "beta_sq_AaAc", "mask_gl_Ac",
+                 "dHi_dx_Ac", "dHi_dy_Ac", "dSL_dx_Ac", "dSL_dy_Ac", "dHb_dx_Ac", "dHb_dy_Ac")
+
+
+class SsaIn(ct.Structure):
+    _fields_ = [(n, P) for n in SSA_IN_FIELDS]
+
+
+class SsaInout(ct.Structure):
+    _fields_ = [(n, P) for n in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")]
+
+
+class SsaOut(ct.Structure):
+    _fields_ = [(n, P) for n in ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")]
+
+
+class SsaStats(ct.Structure):
+    _fields_ = [("status", I32), ("picard_iterations", I32), ("linear_solves", I32), ("resets", I32),
+                ("not_converged", I32), ("total_sweeps", ct.c_int64), ("last_RN", F64),
+                ("last_max_residual", F64), ("sweeps", I32 * 64), ("device_ms", F64)]
+
+
+class SiaIn(ct.Structure):
+    _fields_ = [(n, P) for n in ("mask_sheet_Ac", "Hi_Ac", "dHs_dx_Ac", "dHs_dy_Ac", "dHs_dp_Ac", "dHs_do_Ac",
+                                 "A_flow_Ac")]
+
+
+class SiaOut(ct.Structure):
+    _fields_ = [(n, P) for n in ("D_SIA_3D_Ac", "D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac", "Uo_SIA_Ac",
+                                 "U_SIA", "V_SIA", "D_SIA")]
+
+
+class BaseMeshC(ct.Structure):
+    _fields_ = [("nV", I32), ("nTri", I32), ("nC_mem", I32)] + \
+               [(n, P) for n in ("V", "nC", "C", "niTri", "iTri", "Tri", "edge_index")]
+
+
+AAAC_FIELDS = ("Nx", "Ny", "Nxx", "Nxy", "Nyy", "iAci", "Aci", "VAc", "Nx_Ac", "Ny_Ac", "No_Ac", "Np_Ac",
+               "edge_index_Ac", "VAaAc", "nCAaAc", "CAaAc", "Nx_AaAc", "Ny_AaAc", "Nxx_AaAc", "Nxy_AaAc",
+               "Nyy_AaAc", "colour", "colour_vi", "colour_nV")
+
+
+class AaAcMeshC(ct.Structure):
+    _fields_ = [("nAc", I32), ("nVAaAc", I32)] + [(n, P) for n in AAAC_FIELDS]
+
+
+# Every symbol include/ufemism_gb300.h declares, with its prototype.
+PROTOTYPES = {
+    "ufe_init": (I32, [ct.c_int]),
+    "ufe_last_error_string": (ct.c_char_p, []),
+    "ufe_mesh_create": (I32, [ct.POINTER(MeshDesc), ct.POINTER(P)]),
+    "ufe_mesh_destroy": (I32, [P]),
+    "ufe_mesh_stream": (P, [P]),
+    "ufe_ssa_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SsaIn), ct.POINTER(SsaInout), ct.POINTER(SsaOut),
+                            ct.POINTER(SsaStats)]),
+    "ufe_ssa_upload": (I32, [P, ct.POINTER(Params), ct.POINTER(SsaIn), ct.POINTER(SsaInout)]),
+    "ufe_ssa_run": (I32, [P, ct.POINTER(Params), ct.POINTER(SsaStats)]),
+    "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
+    "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_aaac_build": (I32, [ct.POINTER(BaseMeshC), ct.POINTER(AaAcMeshC)]),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the native library (building it first if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError("libufemism_gb300.so is not built; run ufemism_gb300.build.build()")
+    L = ct.CDLL(_build.LIB)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return load().ufe_last_error_string().decode(errors="replace")
+
+
+class UfeError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__("%s failed: %s (%d): %s" % (where, STATUS_NAMES.get(status, "?"), status, last_error()))

@@ -1,0 +1,246 @@
+"""Python mirror of the reference interface for the ice-velocity solve.
+
+``solve_SSA`` / ``solve_SIA`` of ice_dynamics_module.f90 take (mesh, ice) and update the ice
+fields in place; here :class:`DeviceMesh` holds the uploaded mesh and ``solve_ssa`` /
+``solve_sia`` take dicts of the same ``type_ice_model`` fields (same names, Aa arrays of nV
+entries, Ac arrays of nAc, AaAc arrays of nVAaAc). All arithmetic runs in the CUDA library
+through the C-ABI; nothing here computes a solve on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as nat
+
+ZETA_DEFAULT = np.array([0.00, 0.10, 0.20, 0.30, 0.40, 0.50, 0.60, 0.70, 0.80, 0.90,
+                         0.925, 0.95, 0.975, 0.99, 1.00])  # configuration_module.f90:124-126
+
+
+def default_params(**kw) -> dict:
+    """Solver knobs (configuration_module.f90:169-184) with the values the benchmark
+    workloads use: Picard tolerance 1e-3, SOR omega 1.3, SOR tolerance 1e-4 m/yr,
+    m_enh = 1, linear sliding with beta^2 = 1e3 Pa yr/m. Keywords override."""
+    p = dict(SSA_RN_tol=1e-3, SSA_max_outer_loops=50, SSA_max_residual_UV=1e-4, SSA_SOR_omega=1.3,
+             SSA_max_inner_loops=10000, m_enh_ssa=1.0, m_enh_sia=1.0,
+             sliding_law=nat.UFE_SLIDING_LINEAR, beta_sq=1e3, use_analytical_GL_flux=0,
+             zero_velocities=0, zeta=ZETA_DEFAULT, precision=nat.UFE_FP64, mixed_refold_sweeps=0)
+    p.update(kw)
+    return p
+
+
+def _params_struct(p: dict):
+    zeta = np.ascontiguousarray(p["zeta"], dtype=np.float64)
+    s = nat.Params(p["SSA_RN_tol"], p["SSA_max_outer_loops"], p["SSA_max_residual_UV"], p["SSA_SOR_omega"],
+                   p["SSA_max_inner_loops"], p["m_enh_ssa"], p["m_enh_sia"], p["sliding_law"], p["beta_sq"],
+                   p["use_analytical_GL_flux"], p["zero_velocities"], zeta.size, zeta.ctypes.data,
+                   p["precision"], p.get("mixed_refold_sweeps", 0))
+    return s, zeta
+
+
+def _f64(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.asfortranarray(a, dtype=np.int32)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class AaAcMesh:
+    """Base triangulation plus the Ac / AaAc mesh, neighbour functions and colouring, in the
+    reference's layout (1-based index values, Fortran-order arrays)."""
+    base: object
+    nAc: int
+    nVAaAc: int
+    arrays: dict = field(default_factory=dict)
+
+    def __getattr__(self, name):
+        arrays = self.__dict__.get("arrays", {})
+        if name in arrays:
+            return arrays[name]
+        raise AttributeError(name)
+
+
+def build_aaac(base) -> AaAcMesh:
+    """Ac mesh, combined AaAc mesh, neighbour functions and five-colouring of ``base``
+    (make_Ac_mesh, get_neighbour_functions, calculate_five_colouring_AaAc) by the library's
+    host mesh substrate."""
+    L = nat.load()
+    nV, nTri, ncm = base.nV, base.nTri, base.C.shape[1]
+    nAc = nV + nTri - 1
+    nA = nV + nAc
+    z = lambda *s: np.zeros(s, dtype=np.float64, order="F")
+    zi = lambda *s: np.zeros(s, dtype=np.int32, order="F")
+    arr = dict(Nx=z(nV, ncm + 1), Ny=z(nV, ncm + 1), Nxx=z(nV, ncm + 1), Nxy=z(nV, ncm + 1), Nyy=z(nV, ncm + 1),
+               iAci=zi(nV, ncm), Aci=zi(nAc, 4), VAc=z(nAc, 2), Nx_Ac=z(nAc, 4), Ny_Ac=z(nAc, 4), No_Ac=z(nAc, 4),
+               Np_Ac=z(nAc), edge_index_Ac=zi(nAc), VAaAc=z(nA, 2), nCAaAc=zi(nA), CAaAc=zi(nA, ncm),
+               Nx_AaAc=z(nA, ncm + 1), Ny_AaAc=z(nA, ncm + 1), Nxx_AaAc=z(nA, ncm + 1), Nxy_AaAc=z(nA, ncm + 1),
+               Nyy_AaAc=z(nA, ncm + 1), colour=zi(nA), colour_vi=zi(nA, 5), colour_nV=zi(5))
+    keep = dict(V=_f64(base.V), nC=_i32(base.nC), C=_i32(base.C), niTri=_i32(base.niTri), iTri=_i32(base.iTri),
+                Tri=_i32(base.Tri), edge_index=_i32(base.edge_index))
+    b = nat.BaseMeshC(nV, nTri, ncm, *(_ptr(keep[k]) for k in ("V", "nC", "C", "niTri", "iTri", "Tri", "edge_index")))
+    o = nat.AaAcMeshC(nAc, nA, *(_ptr(arr[k]) for k in nat.AAAC_FIELDS))
+    rc = L.ufe_aaac_build(ct.byref(b), ct.byref(o))
+    if rc != nat.UFE_OK:
+        raise nat.UfeError(rc, "ufe_aaac_build")
+    return AaAcMesh(base=base, nAc=nAc, nVAaAc=nA, arrays=arr)
+
+
+def init(device: int = 0) -> None:
+    rc = nat.load().ufe_init(device)
+    if rc != nat.UFE_OK:
+        raise nat.UfeError(rc, "ufe_init")
+
+
+class DeviceMesh:
+    """An uploaded mesh (ufe_mesh_create). ``mesh`` is any object with the type_mesh
+    attributes: base (V, nC, edge_index) and the AaAc arrays."""
+
+    def __init__(self, mesh):
+        L = nat.load()
+        base = mesh.base
+        self.nV, self.nAc, self.nVAaAc = base.nV, mesh.nAc, mesh.nVAaAc
+        self._keep = dict(V=_f64(base.V), nC=_i32(base.nC), iAci=_i32(mesh.iAci), Aci=_i32(mesh.Aci),
+                          edge_index=_i32(base.edge_index), edge_index_Ac=_i32(mesh.edge_index_Ac),
+                          nCAaAc=_i32(mesh.nCAaAc), CAaAc=_i32(mesh.CAaAc), Nx_AaAc=_f64(mesh.Nx_AaAc),
+                          Ny_AaAc=_f64(mesh.Ny_AaAc), Nxx_AaAc=_f64(mesh.Nxx_AaAc), Nxy_AaAc=_f64(mesh.Nxy_AaAc),
+                          Nyy_AaAc=_f64(mesh.Nyy_AaAc), colour=_i32(mesh.colour), colour_vi=_i32(mesh.colour_vi),
+                          colour_nV=_i32(mesh.colour_nV))
+        k = self._keep
+        d = nat.MeshDesc(self.nV, self.nAc, self.nVAaAc, k["CAaAc"].shape[1],
+                         *(_ptr(k[n]) for n in ("V", "nC", "iAci", "Aci", "edge_index", "edge_index_Ac", "nCAaAc",
+                                                "CAaAc", "Nx_AaAc", "Ny_AaAc", "Nxx_AaAc", "Nxy_AaAc", "Nyy_AaAc",
+                                                "colour", "colour_vi", "colour_nV")))
+        h = ct.c_void_p()
+        rc = L.ufe_mesh_create(ct.byref(d), ct.byref(h))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_mesh_create")
+        self._h = h
+        self._keep = None  # the library copied everything it needs
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        return nat.load().ufe_mesh_stream(self._h) or 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            nat.load().ufe_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- SSA
+    def _ssa_structs(self, fields: dict, warm: dict | None):
+        keep = {}
+
+        def g(k, dt=np.float64):
+            v = fields.get(k)
+            if v is None:
+                return None
+            a = np.ascontiguousarray(v, dtype=dt)
+            keep[k] = a
+            return a.ctypes.data
+
+        ints = ("mask_sheet", "mask_gl_Ac")
+        si = nat.SsaIn(*(g(k, np.int32 if k in ints else np.float64) for k in nat.SSA_IN_FIELDS))
+        warm = warm or {}
+        io = {}
+        for k, n in (("U_SSA", self.nV), ("V_SSA", self.nV), ("Ux_SSA_Ac", self.nAc), ("Uy_SSA_Ac", self.nAc)):
+            io[k] = np.array(warm.get(k, np.zeros(n)), dtype=np.float64, copy=True)
+        io["N_AaAc"] = np.array(warm.get("N_AaAc", np.zeros(self.nVAaAc)), dtype=np.float64, copy=True)
+        sio = nat.SsaInout(*(io[k].ctypes.data for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")))
+        return si, sio, io, keep
+
+    def solve_ssa(self, fields: dict, params: dict, warm: dict | None = None, check: bool = True):
+        """solve_SSA. Returns (status, outputs, stats). Outputs hold the solution U_SSA, V_SSA,
+        Ux_SSA_Ac, Uy_SSA_Ac, N_AaAc and Up_SSA_Ac, Uo_SSA_Ac, eta_AaAc, S_AaAc, tau_c_AaAc,
+        phi_fric_AaAc."""
+        L = nat.load()
+        si, sio, io, keep = self._ssa_structs(fields, warm)
+        out = {k: np.zeros(self.nAc) for k in ("Up_SSA_Ac", "Uo_SSA_Ac")}
+        out.update({k: np.zeros(self.nVAaAc) for k in ("eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")})
+        so = nat.SsaOut(*(out[k].ctypes.data for k in ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc",
+                                                        "tau_c_AaAc", "phi_fric_AaAc")))
+        ps, _z = _params_struct(params)
+        st = nat.SsaStats()
+        rc = L.ufe_ssa_solve(self._h, ct.byref(ps), ct.byref(si), ct.byref(sio), ct.byref(so), ct.byref(st))
+        if check and rc < 0:
+            raise nat.UfeError(rc, "ufe_ssa_solve")
+        out.update(io)
+        return rc, out, stats_dict(st)
+
+    def ssa_upload(self, fields: dict, params: dict, warm: dict | None = None):
+        L = nat.load()
+        si, sio, io, keep = self._ssa_structs(fields, warm)
+        ps, _z = _params_struct(params)
+        rc = L.ufe_ssa_upload(self._h, ct.byref(ps), ct.byref(si), ct.byref(sio))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_ssa_upload")
+
+    def ssa_run(self, params: dict, check: bool = True):
+        L = nat.load()
+        ps, _z = _params_struct(params)
+        st = nat.SsaStats()
+        rc = L.ufe_ssa_run(self._h, ct.byref(ps), ct.byref(st))
+        if check and rc < 0:
+            raise nat.UfeError(rc, "ufe_ssa_run")
+        return rc, stats_dict(st)
+
+    def ssa_download(self):
+        L = nat.load()
+        io = {k: np.zeros(self.nV) for k in ("U_SSA", "V_SSA")}
+        io.update({k: np.zeros(self.nAc) for k in ("Ux_SSA_Ac", "Uy_SSA_Ac", "Up_SSA_Ac", "Uo_SSA_Ac")})
+        io.update({k: np.zeros(self.nVAaAc) for k in ("N_AaAc", "eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")})
+        sio = nat.SsaInout(*(io[k].ctypes.data for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")))
+        so = nat.SsaOut(*(io[k].ctypes.data for k in ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc", "tau_c_AaAc",
+                                                       "phi_fric_AaAc")))
+        rc = L.ufe_ssa_download(self._h, ct.byref(sio), ct.byref(so))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_ssa_download")
+        return io
+
+    # ---------------------------------------------------------------- SIA
+    def solve_sia(self, fields: dict, params: dict, want_3d: bool = True):
+        L = nat.load()
+        nZ = len(params["zeta"])
+        keep = dict(mask_sheet_Ac=np.ascontiguousarray(fields["mask_sheet_Ac"], dtype=np.int32))
+        for k in ("Hi_Ac", "dHs_dx_Ac", "dHs_dy_Ac", "dHs_dp_Ac", "dHs_do_Ac"):
+            keep[k] = np.ascontiguousarray(fields[k], dtype=np.float64)
+        keep["A_flow_Ac"] = np.asfortranarray(fields["A_flow_Ac"], dtype=np.float64)
+        si = nat.SiaIn(*(keep[k].ctypes.data for k in ("mask_sheet_Ac", "Hi_Ac", "dHs_dx_Ac", "dHs_dy_Ac",
+                                                        "dHs_dp_Ac", "dHs_do_Ac", "A_flow_Ac")))
+        out = dict(D_SIA_3D_Ac=np.zeros((self.nAc, nZ), order="F") if want_3d else None)
+        for k in ("D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac", "Uo_SIA_Ac"):
+            out[k] = np.zeros(self.nAc)
+        for k in ("U_SIA", "V_SIA", "D_SIA"):
+            out[k] = np.zeros(self.nV)
+        so = nat.SiaOut(*(_ptr(out[k]) for k in ("D_SIA_3D_Ac", "D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac",
+                                                  "Uo_SIA_Ac", "U_SIA", "V_SIA", "D_SIA")))
+        ps, _z = _params_struct(params)
+        rc = L.ufe_sia_solve(self._h, ct.byref(ps), ct.byref(si), ct.byref(so))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_sia_solve")
+        return out
+
+
+def stats_dict(st) -> dict:
+    n = min(64, st.linear_solves)
+    return dict(status=st.status, picard_iterations=st.picard_iterations, linear_solves=st.linear_solves,
+                resets=st.resets, not_converged=st.not_converged, total_sweeps=st.total_sweeps,
+                last_RN=st.last_RN, last_max_residual=st.last_max_residual, sweeps=list(st.sweeps)[:n],
+                device_ms=st.device_ms)

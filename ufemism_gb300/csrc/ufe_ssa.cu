@@ -1,0 +1,1089 @@
+// SSA velocity solve on the device: the whole Picard + coloured-SOR loop of solve_SSA in one
+// persistent cooperative kernel, between one gather of the inputs and one scatter of the
+// results. Convergence is decided on the device; no per-iteration host round trip.
+//
+// Reference routines (ice_dynamics_module.f90):
+//   solve_SSA 408-557          Picard loop, RN test, reset handling          -> ssa_persistent
+//   SSA_effective_viscosity 695-726 + get_mesh_derivatives_AaAc
+//                              (mesh_ArakawaC_module.f90:583-618)            -> phase_viscosity
+//   SSA_sliding_term 727-779 (+ linear law), centre coefficients and RHS 580-595
+//                                                                            -> phase_coefficients
+//   solve_SSA_linearised 597-691, five-colour SOR 607-664                    -> phase_sweep
+//   apply_Neumann_boundary_AaAc (mesh_ArakawaC_module.f90:660-724)           -> phase_boundary
+//   basal_yield_stress 780-844                                               -> k_gather
+//   calculate_GL_flux 848-949                                                -> k_gl_flux
+//   scatter 548-552 + rotate_xy_to_po (mesh_ArakawaC_module.f90:815-844)     -> k_scatter
+//
+// FP64 path: every multiply and add of the reference is evaluated in its order (the file is
+// compiled with --fmad=false), with two precombined coefficient sets: (4Nxx+Nyy, 4Nyy+Nxx)
+// per neighbour (the same doubles the reference forms each time) and the row sum of Nxy for
+// the cross term, which the reference forms as U(ai)*Nxy(ai,1) + U(ai)*Nxy(ai,2) + ...
+// (get_mesh_curvatures_vertex_AaAc multiplies the home value into every term).
+//
+// Mixed path: FP64 defect correction around FP32 sweeps. With u0 fixed (FP64), the defect
+// r0 = b - A(eta) u0 is formed in FP64; the sweeps run the same coloured SOR on A d = r0 in
+// FP32 from d = 0. SOR is affine-equivariant, so u0 + d follows the FP64 iterates exactly
+// in exact arithmetic, and the residual the sweep tests against SSA_max_residual_UV is that
+// of the FP64 iteration; FP32 rounding is relative to |d|, not |u|. Every `refold` sweeps
+// d is folded into u0 and the defect recomputed in FP64. The viscosity uses FP32 arithmetic
+// on FP64 differences u_j - u_i. Convergence norms (RN, max residual) are FP64.
+#include <cooperative_groups.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ufe_internal.h"
+
+namespace ufe {
+
+// ---------------------------------------------------------------------------------------
+// Control block and kernel arguments
+// ---------------------------------------------------------------------------------------
+struct SsaCtl {
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int err;
+  int status;
+  unsigned long long maxres[3];   // max |res| per sweep (ring of three), as ordered bits
+  int picard_iterations;
+  int linear_solves;
+  int resets;
+  int not_converged;
+  long long total_sweeps;
+  double last_RN;
+  double last_max_residual;
+  int sweeps[64];
+};
+
+struct SsaArgs {
+  // mesh
+  const int *col;
+  const double2 *cuv;
+  const double2 *nxy;
+  const float2 *cuv32;
+  const float2 *nxy32;
+  const uint8_t *deg;
+  const int64_t *slice_ptr;
+  const double2 *h_nxy;
+  const double2 *h_cuv;
+  const double *sNxy;
+  const float2 *h_nxy32;
+  const float *sNxy32;
+  const int *bnd_ptr;
+  const int *bnd_nbr;
+  int grp_off[kGroups + 1];
+  int n_edge;
+  int edge_first;
+  int nP;
+  int ncm;
+  // fields in device row order
+  const double *Hi, *Hb, *SL, *hx, *hy, *Af, *beta, *tau;
+  const uint8_t *skip;    // Dirichlet rows (grounding-line Ac rows under the GL-flux option), may be null
+  double2 *UV;            // FP64 velocities (u0 in the mixed path)
+  float2 *dUV;            // mixed: correction d
+  float2 *r0;             // mixed: defect
+  float2 *euv32;          // mixed: FP32 centre coefficients
+  double *eta, *Na, *Nb, *S;
+  double2 *rhs, *euv;
+  double *rn_part;        // [2 * gridDim.x]
+  SsaCtl *ctl;
+  // parameters
+  double omega, tol, rn_tol, m_enh, uq, expo, beta_const;
+  int max_inner, max_outer, sliding_law, has_beta;
+  int refold;
+  long long timeout_ns;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Grid-wide barrier for a cooperative (co-resident) launch. The spin is bounded: after
+// timeout_ns the CTA records UFE_TIMEOUT and returns false; callers then leave the kernel.
+__device__ __forceinline__ bool grid_barrier(SsaCtl *ctl, unsigned int &gen, long long timeout_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int g = gen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&ctl->bar_count, 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&ctl->bar_count, 0u);
+      __threadfence();
+      atomicAdd(&ctl->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer_ns();
+      unsigned int ns = 8;
+      while (ld_acquire_u32(&ctl->bar_gen) == g) {
+        __nanosleep(ns);
+        if (ns < 64) ns <<= 1;
+        if ((long long)(globaltimer_ns() - t0) > timeout_ns) {
+          atomicCAS(&ctl->err, 0, (int)UFE_TIMEOUT);
+          break;
+        }
+      }
+    }
+    __threadfence();
+    gen = g + 1;
+    s_ok = *(volatile int *)&ctl->err == 0;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block max of a non-negative double, then one atomicMax per CTA on its bit pattern (the
+// IEEE ordering of non-negative doubles equals the ordering of their bit patterns).
+__device__ __forceinline__ void block_max_to(unsigned long long *dst, double v) {
+  __shared__ double s_w[32];
+  v = warp_max(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) s_w[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0.0;
+    x = warp_max(x);
+    if (l == 0 && x > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(x));
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ bool is_floating(double Hi, double Hb, double SL) {
+  return Hi < ((SL - Hb) * kSeawaterDensity) / kIceDensity;   // general_ice_model_data_module.f90:464-475
+}
+
+// ---------------------------------------------------------------------------------------
+// Phases
+// ---------------------------------------------------------------------------------------
+
+// Effective viscosity and N = eta * max(0.1, H) on every row; block partial sums of
+// (N - Nprev)^2 and N^2 for RN. FP64: reference order (home term first).
+template <bool kMixed>
+__device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev) {
+  const int warps_per_block = blockDim.x >> 5;
+  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int nw = gridDim.x * warps_per_block;
+  const int lane = threadIdx.x & 31;
+  const int nslices = a.nP / kSlice;
+  double sdn = 0.0, sn = 0.0;
+  for (int s = gw; s < nslices; s += nw) {
+    const int p = s * kSlice + lane;
+    const int n = a.deg[p];
+    if (n == 0) continue;
+    const int64_t e0 = a.slice_ptr[s] + lane;
+    const double2 ui = a.UV[p];
+    double ux, uy, vx, vy;
+    if (!kMixed) {
+      const double2 h = a.h_nxy[p];
+      ux = h.x * ui.x; uy = h.y * ui.x; vx = h.x * ui.y; vy = h.y * ui.y;
+      for (int k = 0; k < n; ++k) {
+        const int64_t e = e0 + (int64_t)k * kSlice;
+        const int j = a.col[e];
+        const double2 c = a.nxy[e];
+        const double2 uj = a.UV[j];
+        ux = ux + c.x * uj.x;
+        uy = uy + c.y * uj.x;
+        vx = vx + c.x * uj.y;
+        vy = vy + c.y * uj.y;
+      }
+    } else {
+      // d/dx u = sum_k Nx_k (u_k - u_i) + u_i * (Nx_home + sum_k Nx_k); the row sum is zero
+      // up to rounding (linear fields are reproduced exactly).
+      const float2 rs = a.h_nxy32[p];
+      float fux = rs.x * (float)ui.x, fuy = rs.y * (float)ui.x;
+      float fvx = rs.x * (float)ui.y, fvy = rs.y * (float)ui.y;
+      for (int k = 0; k < n; ++k) {
+        const int64_t e = e0 + (int64_t)k * kSlice;
+        const int j = a.col[e];
+        const float2 c = a.nxy32[e];
+        const double2 uj = a.UV[j];
+        const float du = (float)(uj.x - ui.x), dv = (float)(uj.y - ui.y);
+        fux = fmaf(c.x, du, fux);
+        fuy = fmaf(c.y, du, fuy);
+        fvx = fmaf(c.x, dv, fvx);
+        fvy = fmaf(c.y, dv, fvy);
+      }
+      ux = fux; uy = fuy; vx = fvx; vy = fvy;
+    }
+    double eta;
+    if (!kMixed) {
+      const double t = uy + vx;
+      const double e2 = (((ux * ux + vy * vy) + ux * vy) + 0.25 * (t * t)) + 1e-12;
+      eta = pow((a.m_enh * 0.5) * a.Af[p], -1.0 / 3.0) * pow(e2, (1.0 - 3.0) / (2.0 * 3.0));
+    } else {
+      const float fx = (float)ux, fy = (float)uy, gx = (float)vx, gy = (float)vy;
+      const float t = fy + gx;
+      const float e2 = (((fx * fx + gy * gy) + fx * gy) + 0.25f * (t * t)) + 1e-12f;
+      const float ef = powf((float)((a.m_enh * 0.5) * a.Af[p]), -1.0f / 3.0f) * powf(e2, -1.0f / 3.0f);
+      eta = (double)ef;
+    }
+    const double Nn = eta * fmax(0.1, a.Hi[p]);
+    a.eta[p] = eta;
+    N[p] = Nn;
+    const double dn = Nn - Nprev[p];
+    sdn += dn * dn;
+    sn += Nn * Nn;
+  }
+  // deterministic block reduction
+  __shared__ double s_a[32], s_b[32];
+  sdn = warp_sum(sdn);
+  sn = warp_sum(sn);
+  const int w = threadIdx.x >> 5;
+  if (lane == 0) { s_a[w] = sdn; s_b[w] = sn; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0.0, y = 0.0;
+    for (int k = 0; k < warps_per_block; ++k) { x += s_a[k]; y += s_b[k]; }
+    a.rn_part[2 * blockIdx.x] = x;
+    a.rn_part[2 * blockIdx.x + 1] = y;
+  }
+}
+
+// RN = sqrt(sum (N - Nprev)^2 / sum N^2), reduced in a fixed order by every CTA.
+__device__ double final_rn(const SsaArgs &a) {
+  __shared__ double s_rn;
+  if (threadIdx.x < 32) {
+    double x = 0.0, y = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
+      x += *(volatile double *)&a.rn_part[2 * b];
+      y += *(volatile double *)&a.rn_part[2 * b + 1];
+    }
+    x = warp_sum(x);
+    y = warp_sum(y);
+    if (threadIdx.x == 0) s_rn = sqrt(x / y);
+  }
+  __syncthreads();
+  return s_rn;
+}
+
+// Sliding term S, centre coefficients (eu, ev) and right-hand sides for every row.
+template <bool kMixed>
+__device__ void phase_coefficients(const SsaArgs &a) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  for (int p = tid; p < a.nP; p += nt) {
+    if (a.deg[p] == 0) continue;
+    double S;
+    if (a.sliding_law == UFE_SLIDING_COULOMB_REGULARISED) {
+      const double2 u = a.UV[p];
+      S = (a.tau[p] * pow((1e-3 * 1e-3 + u.x * u.x) + u.y * u.y, a.expo)) / a.uq;
+    } else {
+      S = a.has_beta ? a.beta[p] : a.beta_const;
+    }
+    a.S[p] = S;
+    if (p >= a.edge_first) continue;   // edge rows are set by the boundary condition
+    const double eta = a.eta[p];
+    const double H = a.Hi[p];
+    a.rhs[p] = make_double2(((kIceDensity * kGrav) * a.hx[p]) / eta, ((kIceDensity * kGrav) * a.hy[p]) / eta);
+    const double2 h = a.h_cuv[p];
+    double2 c;
+    if (!is_floating(H, a.Hb[p], a.SL[p])) {
+      c = make_double2(h.x - S / (fmax(0.1, H) * eta), h.y - S / (fmax(0.1, H) * eta));
+    } else {
+      c = h;
+    }
+    a.euv[p] = c;
+    if (kMixed) a.euv32[p] = make_float2((float)c.x, (float)c.y);
+  }
+}
+
+// One colour of the FP64 SOR sweep; returns this thread's max |res|.
+__device__ double phase_sweep64(const SsaArgs &a, int g) {
+  const int warps_per_block = blockDim.x >> 5;
+  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int nw = gridDim.x * warps_per_block;
+  const int lane = threadIdx.x & 31;
+  const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
+  const double omega = a.omega;
+  double mx = 0.0;
+  for (int s = s0 + gw; s < s1; s += nw) {
+    const int p = s * kSlice + lane;
+    const int n = a.deg[p];
+    if (n == 0) continue;
+    if (a.skip && a.skip[p]) continue;
+    const int64_t e0 = a.slice_ptr[s] + lane;
+    double su = 0.0, sv = 0.0;
+    int k = 0;
+    for (; k + 4 <= n; k += 4) {
+      int j[4];
+      double2 c[4], u[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) j[q] = a.col[e0 + (int64_t)(k + q) * kSlice];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[q] = a.cuv[e0 + (int64_t)(k + q) * kSlice];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) u[q] = a.UV[j[q]];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        su = su + u[q].x * c[q].x;
+        sv = sv + u[q].y * c[q].y;
+      }
+    }
+    for (; k < n; ++k) {
+      const int64_t e = e0 + (int64_t)k * kSlice;
+      const int j = a.col[e];
+      const double2 c = a.cuv[e];
+      const double2 u = a.UV[j];
+      su = su + u.x * c.x;
+      sv = sv + u.y * c.y;
+    }
+    const double2 ui = a.UV[p];
+    const double sxy = a.sNxy[p];
+    const double Uxy = ui.x * sxy, Vxy = ui.y * sxy;
+    const double2 ec = a.euv[p];
+    const double2 b = a.rhs[p];
+    const double lhsx = (su + 3.0 * Vxy) + ec.x * ui.x;
+    const double lhsy = (sv + 3.0 * Uxy) + ec.y * ui.y;
+    const double ru = (lhsx - b.x) / ec.x;
+    const double rv = (lhsy - b.y) / ec.y;
+    mx = fmax(mx, fabs(ru));
+    mx = fmax(mx, fabs(rv));
+    a.UV[p] = make_double2(ui.x - omega * ru, ui.y - omega * rv);
+  }
+  return mx;
+}
+
+// One colour of the FP32 correction sweep of the mixed path.
+__device__ double phase_sweep32(const SsaArgs &a, int g) {
+  const int warps_per_block = blockDim.x >> 5;
+  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int nw = gridDim.x * warps_per_block;
+  const int lane = threadIdx.x & 31;
+  const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
+  const float omega = (float)a.omega;
+  float mx = 0.0f;
+  for (int s = s0 + gw; s < s1; s += nw) {
+    const int p = s * kSlice + lane;
+    const int n = a.deg[p];
+    if (n == 0) continue;
+    if (a.skip && a.skip[p]) continue;
+    const int64_t e0 = a.slice_ptr[s] + lane;
+    float su = 0.0f, sv = 0.0f;
+    int k = 0;
+    for (; k + 4 <= n; k += 4) {
+      int j[4];
+      float2 c[4], u[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) j[q] = a.col[e0 + (int64_t)(k + q) * kSlice];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) c[q] = a.cuv32[e0 + (int64_t)(k + q) * kSlice];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) u[q] = a.dUV[j[q]];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        su = fmaf(u[q].x, c[q].x, su);
+        sv = fmaf(u[q].y, c[q].y, sv);
+      }
+    }
+    for (; k < n; ++k) {
+      const int64_t e = e0 + (int64_t)k * kSlice;
+      const int j = a.col[e];
+      const float2 c = a.cuv32[e];
+      const float2 u = a.dUV[j];
+      su = fmaf(u.x, c.x, su);
+      sv = fmaf(u.y, c.y, sv);
+    }
+    const float2 di = a.dUV[p];
+    const float sxy = a.sNxy32[p];
+    const float2 ec = a.euv32[p];
+    const float2 r = a.r0[p];
+    const float lx = fmaf(ec.x, di.x, fmaf(3.0f * sxy, di.y, su)) - r.x;
+    const float ly = fmaf(ec.y, di.y, fmaf(3.0f * sxy, di.x, sv)) - r.y;
+    const float ru = lx / ec.x, rv = ly / ec.y;
+    mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
+    a.dUV[p] = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
+  }
+  return (double)mx;
+}
+
+// Neumann boundary (apply_Neumann_boundary_AaAc): each edge row becomes the mean of its
+// non-edge neighbours; the four corners the mean of all their neighbours, where an edge
+// neighbour's new value is recomputed in place (same arithmetic, same result) so that the
+// corners need no second pass. SUM(vals) in the reference runs over nC_mem slots whose
+// unused entries are +0, hence the trailing "+ 0.0".
+template <bool kMixed>
+__device__ __forceinline__ double2 edge_mean(const SsaArgs &a, int k) {
+  const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
+  double sx = 0.0, sy = 0.0;
+  for (int q = b0; q < b1; ++q) {
+    const int j = a.bnd_nbr[q];
+    double2 u = a.UV[j];
+    if (kMixed) {
+      const float2 d = a.dUV[j];
+      u.x = u.x + (double)d.x;
+      u.y = u.y + (double)d.y;
+    }
+    sx = sx + u.x;
+    sy = sy + u.y;
+  }
+  const int nvals = b1 - b0;
+  if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
+  return make_double2(sx / (double)nvals, sy / (double)nvals);
+}
+
+template <bool kMixed>
+__device__ void phase_boundary(const SsaArgs &a) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  const int nb = a.n_edge + 4;
+  for (int k = tid; k < nb; k += nt) {
+    const int p = a.edge_first + k;
+    double2 v;
+    if (k < a.n_edge) {
+      v = edge_mean<kMixed>(a, k);
+    } else {
+      const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
+      double sx = 0.0, sy = 0.0;
+      for (int q = b0; q < b1; ++q) {
+        const int j = a.bnd_nbr[q];
+        double2 u;
+        if (j < 0) {
+          u = edge_mean<kMixed>(a, -j - 1);
+        } else {
+          u = a.UV[j];
+          if (kMixed) {
+            const float2 d = a.dUV[j];
+            u.x = u.x + (double)d.x;
+            u.y = u.y + (double)d.y;
+          }
+        }
+        sx = sx + u.x;
+        sy = sy + u.y;
+      }
+      const int nvals = b1 - b0;
+      if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
+      v = make_double2(sx / (double)nvals, sy / (double)nvals);
+    }
+    if (!kMixed) {
+      a.UV[p] = v;
+    } else {
+      const double2 u0 = a.UV[p];
+      a.dUV[p] = make_float2((float)(v.x - u0.x), (float)(v.y - u0.y));
+    }
+  }
+}
+
+// Mixed path: u0 += d, d = 0 on every row.
+__device__ void phase_fold(const SsaArgs &a) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  for (int p = tid; p < a.nP; p += nt) {
+    const float2 d = a.dUV[p];
+    if (d.x != 0.0f || d.y != 0.0f) {
+      double2 u = a.UV[p];
+      u.x = u.x + (double)d.x;
+      u.y = u.y + (double)d.y;
+      a.UV[p] = u;
+      a.dUV[p] = make_float2(0.0f, 0.0f);
+    }
+  }
+}
+
+// Mixed path: FP64 defect r0 = RHS - LHS(u0) on the swept rows.
+__device__ void phase_defect(const SsaArgs &a) {
+  const int warps_per_block = blockDim.x >> 5;
+  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int nw = gridDim.x * warps_per_block;
+  const int lane = threadIdx.x & 31;
+  const int s1 = a.edge_first / kSlice;
+  for (int s = gw; s < s1; s += nw) {
+    const int p = s * kSlice + lane;
+    const int n = a.deg[p];
+    if (n == 0) continue;
+    const int64_t e0 = a.slice_ptr[s] + lane;
+    double su = 0.0, sv = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const int64_t e = e0 + (int64_t)k * kSlice;
+      const int j = __ldcs(a.col + e);
+      const double2 c = __ldcs(a.cuv + e);
+      const double2 u = a.UV[j];
+      su = su + u.x * c.x;
+      sv = sv + u.y * c.y;
+    }
+    const double2 ui = a.UV[p];
+    const double sxy = a.sNxy[p];
+    const double2 ec = a.euv[p];
+    const double2 b = a.rhs[p];
+    const double lhsx = (su + 3.0 * (ui.y * sxy)) + ec.x * ui.x;
+    const double lhsy = (sv + 3.0 * (ui.x * sxy)) + ec.y * ui.y;
+    a.r0[p] = make_float2((float)(b.x - lhsx), (float)(b.y - lhsy));
+  }
+}
+
+__device__ void phase_zero_velocity(const SsaArgs &a, bool mixed) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nt = gridDim.x * blockDim.x;
+  for (int p = tid; p < a.nP; p += nt) {
+    a.UV[p] = make_double2(0.0, 0.0);
+    if (mixed) a.dUV[p] = make_float2(0.0f, 0.0f);
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// The persistent solver
+// ---------------------------------------------------------------------------------------
+template <bool kMixed>
+__global__ void __launch_bounds__(256) ssa_persistent(SsaArgs a) {
+  SsaCtl *ctl = a.ctl;
+  unsigned int gen = 0;
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  double *N = a.Na, *Nprev = a.Nb;
+  int did_reset_before = 0;
+  int it = 0;
+  bool picard_done = false;
+  while (!picard_done && it < a.max_outer) {
+    ++it;
+    // N_prev <- N, then the new viscosity into N
+    { double *t = N; N = Nprev; Nprev = t; }
+    phase_viscosity<kMixed>(a, N, Nprev);
+    if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    const double RN = final_rn(a);
+    if (leader) { ctl->picard_iterations = it; ctl->last_RN = RN; }
+    if (RN < a.rn_tol) { picard_done = true; break; }
+    phase_coefficients<kMixed>(a);
+    if (leader) { ctl->maxres[0] = 0ull; ctl->maxres[1] = 0ull; ctl->maxres[2] = 0ull; }
+    if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    if (kMixed) {
+      phase_defect(a);
+      if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    }
+    // coloured SOR
+    int sweeps = 0;
+    bool lin_done = false;
+    int did_reset = 0;
+    double maxres = 0.0;
+    while (!lin_done && sweeps < a.max_inner) {
+      ++sweeps;
+      const int slot = sweeps % 3;
+      if (leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
+      double mx = 0.0;
+      for (int g = 0; g < 5; ++g) {
+        mx = fmax(mx, kMixed ? phase_sweep32(a, g) : phase_sweep64(a, g));
+        if (g == 4) block_max_to(&ctl->maxres[slot], mx);
+        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+      }
+      phase_boundary<kMixed>(a);
+      if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+      maxres = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxres[slot]);
+      if (maxres < a.tol) {
+        lin_done = true;
+      } else if (maxres > 1e6) {
+        phase_zero_velocity(a, kMixed);
+        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+        did_reset = 1;
+        lin_done = true;
+      } else if (sweeps == a.max_inner) {
+        if (leader) ctl->not_converged += 1;
+      } else if (kMixed && a.refold > 0 && sweeps % a.refold == 0) {
+        phase_fold(a);
+        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+        phase_defect(a);
+        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+      }
+    }
+    if (kMixed && !did_reset) {
+      phase_fold(a);
+      if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    }
+    if (leader) {
+      if (ctl->linear_solves < 64) ctl->sweeps[ctl->linear_solves] = sweeps;
+      ctl->linear_solves += 1;
+      ctl->total_sweeps += sweeps;
+      ctl->last_max_residual = maxres;
+      if (did_reset) ctl->resets += 1;
+    }
+    if (did_reset) {
+      if (did_reset_before) {
+        if (leader) ctl->status = UFE_DIVERGED;
+        break;
+      }
+      did_reset_before = 1;
+    }
+  }
+  // Final N lives in N; make Na hold it for the scatter.
+  if (N != a.Na) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    for (int p = tid; p < a.nP; p += nt) a.Na[p] = N[p];
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Gather / scatter / GL flux
+// ---------------------------------------------------------------------------------------
+struct StageIn {   // device staging of the caller's arrays (original order)
+  const double *Hi, *Hb, *SL, *hx, *hy, *Af;          // Aa (nV)
+  const double *Hi_Ac, *Hb_Ac, *SL_Ac, *hx_Ac, *hy_Ac, *Af_Ac;  // Ac (nAc)
+  const double *beta;                                  // (nA) or null
+  const double *U, *V, *Ux, *Uy;                       // warm start
+  const double *N;                                     // (nA) or null
+};
+
+struct Fields {
+  double *Hi, *Hb, *SL, *hx, *hy, *Af, *beta, *tau, *phi;
+  double2 *UV;
+  float2 *dUV;
+  double *Na, *Nb;
+};
+
+// Gather into device order, and basal_yield_stress (Martin et al. 2011) per row.
+__global__ void k_gather(int nP, int nV, const int *orig_of_dev, StageIn in, Fields f) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nP) return;
+  const int r = orig_of_dev[p];
+  if (r < 0) {
+    f.Hi[p] = 0.0; f.Hb[p] = 0.0; f.SL[p] = 0.0; f.hx[p] = 0.0; f.hy[p] = 0.0; f.Af[p] = 1.0;
+    f.tau[p] = 0.0; f.phi[p] = 0.0; f.UV[p] = make_double2(0.0, 0.0); f.dUV[p] = make_float2(0.f, 0.f);
+    f.Na[p] = 0.0; f.Nb[p] = 0.0;
+    if (f.beta) f.beta[p] = 0.0;
+    return;
+  }
+  double Hi, Hb, SL, hx, hy, Af, U, V;
+  if (r < nV) {
+    Hi = in.Hi[r]; Hb = in.Hb[r]; SL = in.SL[r]; hx = in.hx[r]; hy = in.hy[r]; Af = in.Af[r];
+    U = in.U[r]; V = in.V[r];
+  } else {
+    const int a = r - nV;
+    Hi = in.Hi_Ac[a]; Hb = in.Hb_Ac[a]; SL = in.SL_Ac[a]; hx = in.hx_Ac[a]; hy = in.hy_Ac[a]; Af = in.Af_Ac[a];
+    U = in.Ux[a]; V = in.Uy[a];
+  }
+  f.Hi[p] = Hi; f.Hb[p] = Hb; f.SL[p] = SL; f.hx[p] = hx; f.hy[p] = hy; f.Af[p] = Af;
+  f.UV[p] = make_double2(U, V);
+  f.dUV[p] = make_float2(0.f, 0.f);
+  const double Nin = in.N ? in.N[r] : 0.0;
+  f.Na[p] = Nin;
+  f.Nb[p] = Nin;
+  if (f.beta) f.beta[p] = in.beta ? in.beta[r] : 0.0;
+  // basal_yield_stress, ice_dynamics_module.f90:780-844
+  const double pf1 = -1000.0, pf2 = 0.0, p_min = 5.0, p_max = 20.0;
+  const double lambda_p = fmax(0.0, fmin(1.0, (1.0 - (Hb - SL) / 1000.0)));
+  const double pwp = (((0.96 * kIceDensity) * kGrav) * fmax(0.1, Hi)) * lambda_p;
+  const double phi = fmax(p_min, fmin(p_max, (p_min + (p_max - p_min) * (1.0 + (Hb - pf2) / (pf2 - pf1)))));
+  f.phi[p] = phi;
+  f.tau[p] = tan((kPi / 180.0) * phi) * (((kIceDensity * kGrav) * fmax(0.1, Hi)) - pwp);
+}
+
+struct GlIn {
+  const int *mask_gl_Ac, *mask_sheet;
+  const double *Hi, *Hb, *SL, *Af;   // Aa
+  const double *dHi_dx, *dHi_dy, *dSL_dx, *dSL_dy, *dHb_dx, *dHb_dy;  // Ac
+};
+
+__device__ double norm2_scaled(double a, double b) {
+  // NORM2([a,b]) as gfortran evaluates it: scaled one-pass sum of squares.
+  double scale = 0.0, ssq = 1.0;
+  const double v[2] = {a, b};
+  for (int i = 0; i < 2; ++i) {
+    if (v[i] != 0.0) {
+      const double ax = fabs(v[i]);
+      if (scale < ax) {
+        const double r = scale / ax;
+        ssq = 1.0 + (ssq * r) * r;
+        scale = ax;
+      } else {
+        const double r = ax / scale;
+        ssq = ssq + r * r;
+      }
+    }
+  }
+  return scale * sqrt(ssq);
+}
+
+// calculate_GL_flux (Tsai et al. 2015 flux for the Coulomb law), ice_dynamics_module.f90:848-949:
+// prescribes Ux/Uy on grounding-line Ac rows and marks them as skipped by the sweep.
+__global__ void k_gl_flux(int nAc, int nV, const int *dev_of_orig, const int2 *Aci12, GlIn g,
+                          const double *phi_dev, double2 *UV, uint8_t *skip, double factor_const) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nAc) return;
+  const int p = dev_of_orig[nV + a];
+  skip[p] = 0;
+  if (g.mask_gl_Ac[a] == 0) return;
+  const int vi = Aci12[a].x, vj = Aci12[a].y;
+  const double rsw = kSeawaterDensity / kIceDensity;
+  const double TAFi = g.Hi[vi] - ((g.SL[vi] - g.Hb[vi]) * rsw);
+  const double TAFj = g.Hi[vj] - ((g.SL[vj] - g.Hb[vj]) * rsw);
+  const double lambda_GL = TAFi / (TAFi - TAFj);
+  const double Hi_GL = (g.Hi[vi] * (1.0 - lambda_GL)) + (g.Hi[vj] * lambda_GL);
+  double phi_GL, A_GL;
+  if (g.mask_sheet[vi] == 1) { phi_GL = phi_dev[dev_of_orig[vi]]; A_GL = g.Af[vi]; }
+  else { phi_GL = phi_dev[dev_of_orig[vj]]; A_GL = g.Af[vj]; }
+  // factor_const = (8 Q0) then * A * (rho g)^n * (1 - rho_i/rho_sw)^(n-1) / 4^n, n = 3
+  const double one_m = 1.0 - (kIceDensity / kSeawaterDensity);
+  const double factor_Tsai = (((factor_const * A_GL) * pow(kIceDensity * kGrav, 3.0)) * (one_m * one_m)) / pow(4.0, 3.0);
+  const double Qabs = (factor_Tsai * pow(Hi_GL, 3.0 + 2.0)) / tan(phi_GL * (kPi / 180.0));
+  double Fx = -(g.dHi_dx[a] - ((g.dSL_dx[a] - g.dHb_dx[a]) * rsw));
+  double Fy = -(g.dHi_dy[a] - ((g.dSL_dy[a] - g.dHb_dy[a]) * rsw));
+  const double F = norm2_scaled(Fx, Fy);
+  Fx = Fx / F;
+  Fy = Fy / F;
+  UV[p] = make_double2((Qabs * Fx) / Hi_GL, (Qabs * Fy) / Hi_GL);
+  skip[p] = 1;
+}
+
+struct StageOut {
+  double *U, *V, *Ux, *Uy, *Up, *Uo;   // Aa (nV) / Ac (nAc)
+  double *N, *eta, *S, *tau, *phi;     // (nA)
+};
+
+__global__ void k_scatter(int nA, int nV, const int *dev_of_orig, const double2 *V, const int2 *Aci12,
+                          const double2 *UV, const double *N, const double *eta, const double *S,
+                          const double *tau, const double *phi, StageOut o) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nA) return;
+  const int p = dev_of_orig[r];
+  const double2 u = UV[p];
+  o.N[r] = N[p];
+  o.eta[r] = eta[p];
+  o.S[r] = S[p];
+  o.tau[r] = tau[p];
+  o.phi[r] = phi[p];
+  if (r < nV) {
+    o.U[r] = u.x;
+    o.V[r] = u.y;
+  } else {
+    const int a = r - nV;
+    o.Ux[a] = u.x;
+    o.Uy[a] = u.y;
+    const int2 ij = Aci12[a];
+    const double Dx = V[ij.y].x - V[ij.x].x;
+    const double Dy = V[ij.y].y - V[ij.x].y;
+    const double D = sqrt(Dx * Dx + Dy * Dy);
+    o.Up[a] = (u.x * Dx) / D + (u.y * Dy) / D;
+    o.Uo[a] = (u.y * Dx) / D - (u.x * Dy) / D;
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------------------
+struct SsaWork {
+  int nP = 0, nV = 0, nAc = 0, nA = 0;
+  // staging (original order)
+  double *stage_in = nullptr;    // 12 nV-or-nAc fields + beta + warm start + N
+  double *stage_out = nullptr;
+  int *gl_int = nullptr;         // mask_gl_Ac (nAc) + mask_sheet (nV)
+  double *gl_dbl = nullptr;      // 6 Ac slope fields
+  // device-order fields
+  double *f = nullptr;           // Hi, Hb, SL, hx, hy, Af, beta, tau, phi, eta, Na, Nb, S
+  double2 *UV = nullptr, *rhs = nullptr, *euv = nullptr;
+  float2 *dUV = nullptr, *r0 = nullptr, *euv32 = nullptr;
+  uint8_t *skip = nullptr;
+  double *rn_part = nullptr;
+  SsaCtl *ctl = nullptr;
+  SsaCtl *ctl_host = nullptr;    // pinned
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // state of the last upload
+  bool uploaded = false;
+  bool has_beta = false, has_N = false, gl = false;
+  bool zero = false;             // the reference's early-out applies
+  int grid = 0, block = 256;
+  int grid_mixed = 0;
+};
+
+void ssa_free(SsaWork *w) {
+  if (!w) return;
+  void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
+                  w->dUV, w->r0, w->euv32, w->skip, w->rn_part, w->ctl};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (w->ctl_host) cudaFreeHost(w->ctl_host);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+}
+
+namespace {
+
+enum { F_HI, F_HB, F_SL, F_HX, F_HY, F_AF, F_BETA, F_TAU, F_PHI, F_ETA, F_NA, F_NB, F_S, F_COUNT };
+// stage_in layout (doubles): Aa block 6*nV, Ac block 6*nAc, beta nA, U nV, V nV, Ux nAc, Uy nAc, N nA
+// stage_out layout: U nV, V nV, Ux nAc, Uy nAc, Up nAc, Uo nAc, N nA, eta nA, S nA, tau nA, phi nA
+
+int ensure_work(ufe_mesh_h h) {
+  if (h->ssa) return UFE_OK;
+  const DevMesh &m = h->m;
+  SsaWork *w = new SsaWork();
+  w->nP = m.nP; w->nV = m.nV; w->nAc = m.nAc; w->nA = m.nA;
+  const size_t nin = 6 * (size_t)m.nV + 6 * (size_t)m.nAc + 2 * (size_t)m.nA + 2 * (size_t)m.nV + 2 * (size_t)m.nAc;
+  const size_t nout = 2 * (size_t)m.nV + 4 * (size_t)m.nAc + 5 * (size_t)m.nA;
+  int rc = cuda_status(cudaMalloc(&w->stage_in, nin * sizeof(double)), "ssa stage_in");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->stage_out, nout * sizeof(double)), "ssa stage_out");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->gl_int, ((size_t)m.nAc + m.nV) * sizeof(int)), "ssa gl_int");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->gl_dbl, 6 * (size_t)m.nAc * sizeof(double)), "ssa gl_dbl");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->f, (size_t)F_COUNT * m.nP * sizeof(double)), "ssa fields");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->UV, (size_t)m.nP * sizeof(double2)), "ssa UV");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->rhs, (size_t)m.nP * sizeof(double2)), "ssa rhs");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->euv, (size_t)m.nP * sizeof(double2)), "ssa euv");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->dUV, (size_t)m.nP * sizeof(float2)), "ssa dUV");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->r0, (size_t)m.nP * sizeof(float2)), "ssa r0");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->euv32, (size_t)m.nP * sizeof(float2)), "ssa euv32");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->skip, (size_t)m.nP), "ssa skip");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(SsaCtl)), "ssa ctl");
+  if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(SsaCtl)), "ssa ctl host");
+  if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
+  if (!rc) rc = cuda_status(cudaEventCreate(&w->ev1), "event");
+  if (!rc) rc = cuda_status(cudaMemsetAsync(w->skip, 0, (size_t)m.nP, h->stream), "memset skip");
+  // Persistent grid: every CTA co-resident (cooperative launch).
+  int per_sm64 = 0, per_sm32 = 0;
+  if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm64, ssa_persistent<false>, w->block, 0), "occupancy");
+  if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, ssa_persistent<true>, w->block, 0), "occupancy");
+  if (!rc && (per_sm64 < 1 || per_sm32 < 1)) { set_error("ssa kernel does not fit on an SM"); rc = UFE_CUDA_ERROR; }
+  if (!rc) {
+    w->grid = h->num_sms * (per_sm64 < 4 ? per_sm64 : 4);
+    w->grid_mixed = h->num_sms * (per_sm32 < 4 ? per_sm32 : 4);
+    if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)(w->grid > w->grid_mixed ? w->grid : w->grid_mixed) * sizeof(double)), "rn_part");
+  }
+  if (rc) { ssa_free(w); return rc; }
+  h->ssa = w;
+  return UFE_OK;
+}
+
+int h2d(double *dst, const double *src, size_t n, cudaStream_t s) {
+  return cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+}
+int d2h(double *dst, const double *src, size_t n, cudaStream_t s) {
+  if (!dst) return UFE_OK;
+  return cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H");
+}
+
+}  // namespace
+
+}  // namespace ufe
+
+using namespace ufe;
+
+extern "C" int ufe_ssa_upload(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, const ufe_ssa_inout *io) {
+  if (!h || !p || !in || !io) { set_error("ufe_ssa_upload: null argument"); return UFE_BAD_ARG; }
+  if (!in->Hi || !in->Hb || !in->SL || !in->dHs_dx_shelf || !in->dHs_dy_shelf || !in->A_flow_mean ||
+      !in->mask_sheet || !in->Hi_Ac || !in->Hb_Ac || !in->SL_Ac || !in->dHs_dx_shelf_Ac ||
+      !in->dHs_dy_shelf_Ac || !in->A_flow_mean_Ac || !io->U_SSA || !io->V_SSA || !io->Ux_SSA_Ac || !io->Uy_SSA_Ac) {
+    set_error("ufe_ssa_upload: missing input array");
+    return UFE_BAD_ARG;
+  }
+  if (p->use_analytical_GL_flux && (!in->mask_gl_Ac || !in->dHi_dx_Ac || !in->dHi_dy_Ac || !in->dSL_dx_Ac ||
+                                    !in->dSL_dy_Ac || !in->dHb_dx_Ac || !in->dHb_dy_Ac)) {
+    set_error("ufe_ssa_upload: use_analytical_GL_flux needs mask_gl_Ac and the Ac slopes of Hi, SL, Hb");
+    return UFE_BAD_ARG;
+  }
+  if (p->use_analytical_GL_flux && p->sliding_law != UFE_SLIDING_COULOMB_REGULARISED) {
+    set_error("ufe_ssa_upload: the GL flux is implemented for the Coulomb_regularised law only (as in the reference)");
+    return UFE_BAD_ARG;
+  }
+  int rc = ensure_work(h);
+  if (rc) return rc;
+  SsaWork *w = h->ssa;
+  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA;
+  cudaStream_t s = h->stream;
+  double *st = w->stage_in;
+  const double *aa[6] = {in->Hi, in->Hb, in->SL, in->dHs_dx_shelf, in->dHs_dy_shelf, in->A_flow_mean};
+  const double *ac[6] = {in->Hi_Ac, in->Hb_Ac, in->SL_Ac, in->dHs_dx_shelf_Ac, in->dHs_dy_shelf_Ac, in->A_flow_mean_Ac};
+  for (int k = 0; k < 6 && !rc; ++k) rc = h2d(st + k * nV, aa[k], nV, s);
+  for (int k = 0; k < 6 && !rc; ++k) rc = h2d(st + 6 * nV + k * nAc, ac[k], nAc, s);
+  double *beta = st + 6 * nV + 6 * nAc;
+  double *U = beta + nA, *V = U + nV, *Ux = V + nV, *Uy = Ux + nAc, *N = Uy + nAc;
+  w->has_beta = in->beta_sq_AaAc != nullptr;
+  if (!rc && w->has_beta) rc = h2d(beta, in->beta_sq_AaAc, nA, s);
+  if (!rc) rc = h2d(U, io->U_SSA, nV, s);
+  if (!rc) rc = h2d(V, io->V_SSA, nV, s);
+  if (!rc) rc = h2d(Ux, io->Ux_SSA_Ac, nAc, s);
+  if (!rc) rc = h2d(Uy, io->Uy_SSA_Ac, nAc, s);
+  w->has_N = io->N_AaAc != nullptr;
+  if (!rc && w->has_N) rc = h2d(N, io->N_AaAc, nA, s);
+  w->gl = p->use_analytical_GL_flux != 0;
+  if (!rc && w->gl) {
+    rc = cuda_status(cudaMemcpyAsync(w->gl_int, in->mask_gl_Ac, nAc * sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(w->gl_int + nAc, in->mask_sheet, nV * sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
+    const double *gs[6] = {in->dHi_dx_Ac, in->dHi_dy_Ac, in->dSL_dx_Ac, in->dSL_dy_Ac, in->dHb_dx_Ac, in->dHb_dy_Ac};
+    for (int k = 0; k < 6 && !rc; ++k) rc = h2d(w->gl_dbl + k * nAc, gs[k], nAc, s);
+  }
+  // Early-outs of solve_SSA (431-452): benchmark experiments without SSA, or no grounded ice.
+  long long sheet = 0;
+  for (size_t v = 0; v < nV; ++v) sheet += in->mask_sheet[v];
+  w->zero = p->zero_velocities != 0 || sheet == 0;
+  w->uploaded = rc == UFE_OK;
+  return rc;
+}
+
+extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *stats) {
+  if (!h || !p) { set_error("ufe_ssa_run: null argument"); return UFE_BAD_ARG; }
+  SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) { set_error("ufe_ssa_run: no inputs uploaded"); return UFE_BAD_ARG; }
+  if (p->precision != UFE_FP64 && p->precision != UFE_MIXED) { set_error("ufe_ssa_run: unknown precision"); return UFE_BAD_ARG; }
+  if (p->sliding_law != UFE_SLIDING_COULOMB_REGULARISED && p->sliding_law != UFE_SLIDING_LINEAR) {
+    set_error("ufe_ssa_run: sliding law not implemented");
+    return UFE_BAD_ARG;
+  }
+  if (p->SSA_max_inner_loops < 1 || p->SSA_max_outer_loops < 1) { set_error("ufe_ssa_run: loop limits must be >= 1"); return UFE_BAD_ARG; }
+  const DevMesh &m = h->m;
+  cudaStream_t s = h->stream;
+  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA, nP = w->nP;
+  int rc = UFE_OK;
+  const bool mixed = p->precision == UFE_MIXED;
+
+  double *F = w->f;
+  Fields fl;
+  fl.Hi = F + F_HI * nP; fl.Hb = F + F_HB * nP; fl.SL = F + F_SL * nP; fl.hx = F + F_HX * nP;
+  fl.hy = F + F_HY * nP; fl.Af = F + F_AF * nP; fl.beta = w->has_beta ? F + F_BETA * nP : nullptr;
+  fl.tau = F + F_TAU * nP; fl.phi = F + F_PHI * nP; fl.UV = w->UV; fl.dUV = w->dUV;
+  fl.Na = F + F_NA * nP; fl.Nb = F + F_NB * nP;
+  double *st = w->stage_in;
+  StageIn si;
+  si.Hi = st; si.Hb = st + nV; si.SL = st + 2 * nV; si.hx = st + 3 * nV; si.hy = st + 4 * nV; si.Af = st + 5 * nV;
+  double *acb = st + 6 * nV;
+  si.Hi_Ac = acb; si.Hb_Ac = acb + nAc; si.SL_Ac = acb + 2 * nAc; si.hx_Ac = acb + 3 * nAc;
+  si.hy_Ac = acb + 4 * nAc; si.Af_Ac = acb + 5 * nAc;
+  si.beta = w->has_beta ? acb + 6 * nAc : nullptr;
+  si.U = acb + 6 * nAc + nA; si.V = si.U + nV; si.Ux = si.V + nV; si.Uy = si.Ux + nAc;
+  si.N = w->has_N ? si.Uy + nAc : nullptr;
+
+  std::memset(w->ctl_host, 0, sizeof(SsaCtl));
+  rc = cuda_status(cudaEventRecord(w->ev0, s), "event");
+  if (!rc) rc = cuda_status(cudaMemsetAsync(w->ctl, 0, sizeof(SsaCtl), s), "memset ctl");
+  if (!rc) {
+    k_gather<<<(unsigned)((nP + 255) / 256), 256, 0, s>>>((int)nP, (int)nV, m.orig_of_dev, si, fl);
+    rc = cuda_status(cudaGetLastError(), "k_gather");
+  }
+  if (!rc && w->gl && !w->zero) {
+    GlIn g;
+    g.mask_gl_Ac = w->gl_int; g.mask_sheet = w->gl_int + nAc;
+    g.Hi = si.Hi; g.Hb = si.Hb; g.SL = si.SL; g.Af = si.Af;
+    g.dHi_dx = w->gl_dbl; g.dHi_dy = w->gl_dbl + nAc; g.dSL_dx = w->gl_dbl + 2 * nAc;
+    g.dSL_dy = w->gl_dbl + 3 * nAc; g.dHb_dx = w->gl_dbl + 4 * nAc; g.dHb_dy = w->gl_dbl + 5 * nAc;
+    k_gl_flux<<<(unsigned)((nAc + 255) / 256), 256, 0, s>>>((int)nAc, (int)nV, m.dev_of_orig, m.Aci12, g, fl.phi, w->UV, w->skip, 8.0 * 0.61);
+    rc = cuda_status(cudaGetLastError(), "k_gl_flux");
+  }
+  if (!rc && !w->zero) {
+    SsaArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.col = m.col; a.cuv = m.cuv; a.nxy = m.nxy; a.cuv32 = m.cuv32; a.nxy32 = m.nxy32; a.deg = m.deg;
+    a.slice_ptr = m.slice_ptr; a.h_nxy = m.h_nxy; a.h_cuv = m.h_cuv; a.sNxy = m.sNxy;
+    a.h_nxy32 = m.h_nxy32; a.sNxy32 = m.sNxy32; a.bnd_ptr = m.bnd_ptr; a.bnd_nbr = m.bnd_nbr;
+    for (int g = 0; g <= kGroups; ++g) a.grp_off[g] = m.grp_off[g];
+    a.n_edge = m.n_edge; a.edge_first = m.edge_first; a.nP = m.nP; a.ncm = m.ncm;
+    a.Hi = fl.Hi; a.Hb = fl.Hb; a.SL = fl.SL; a.hx = fl.hx; a.hy = fl.hy; a.Af = fl.Af;
+    a.beta = fl.beta; a.tau = fl.tau;
+    a.skip = w->gl ? w->skip : nullptr;
+    a.UV = w->UV; a.dUV = w->dUV; a.r0 = w->r0; a.euv32 = w->euv32;
+    a.eta = F + F_ETA * nP; a.Na = fl.Na; a.Nb = fl.Nb; a.S = F + F_S * nP;
+    a.rhs = w->rhs; a.euv = w->euv; a.rn_part = w->rn_part; a.ctl = w->ctl;
+    a.omega = p->SSA_SOR_omega; a.tol = p->SSA_max_residual_UV; a.rn_tol = p->SSA_RN_tol;
+    a.m_enh = p->m_enh_ssa;
+    a.uq = std::pow(100.0, 0.30);          // u_threshold**q_plastic
+    a.expo = 0.5 * (0.30 - 1.0);           // 0.5*(q_plastic-1)
+    a.beta_const = p->beta_sq;
+    a.max_inner = p->SSA_max_inner_loops; a.max_outer = p->SSA_max_outer_loops;
+    a.sliding_law = p->sliding_law; a.has_beta = w->has_beta;
+    a.refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 32;
+    a.timeout_ns = 20LL * 1000 * 1000 * 1000;
+    void *args[] = {&a};
+    const int grid = mixed ? w->grid_mixed : w->grid;
+    if (mixed)
+      rc = cuda_status(cudaLaunchCooperativeKernel((void *)ssa_persistent<true>, dim3(grid), dim3(w->block), args, 0, s), "ssa_persistent<mixed>");
+    else
+      rc = cuda_status(cudaLaunchCooperativeKernel((void *)ssa_persistent<false>, dim3(grid), dim3(w->block), args, 0, s), "ssa_persistent<fp64>");
+  }
+  if (!rc) {
+    StageOut o;
+    double *so = w->stage_out;
+    o.U = so; o.V = so + nV; o.Ux = so + 2 * nV; o.Uy = o.Ux + nAc; o.Up = o.Uy + nAc; o.Uo = o.Up + nAc;
+    o.N = o.Uo + nAc; o.eta = o.N + nA; o.S = o.eta + nA; o.tau = o.S + nA; o.phi = o.tau + nA;
+    if (w->zero) {
+      // velocities zero, Picard state untouched
+      rc = cuda_status(cudaMemsetAsync(w->UV, 0, nP * sizeof(double2), s), "memset UV");
+    }
+    if (!rc) {
+      k_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>((int)nA, (int)nV, m.dev_of_orig, m.V, m.Aci12, w->UV,
+                                                            fl.Na, F + F_ETA * nP, F + F_S * nP, fl.tau, fl.phi, o);
+      rc = cuda_status(cudaGetLastError(), "k_scatter");
+    }
+  }
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(w->ctl_host, w->ctl, sizeof(SsaCtl), cudaMemcpyDeviceToHost, s), "ctl D2H");
+  if (!rc) rc = cuda_status(cudaEventRecord(w->ev1, s), "event");
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa solve");
+  if (rc) return rc;
+  const SsaCtl &c = *w->ctl_host;
+  int status = UFE_OK;
+  if (c.err) {
+    status = c.err;
+    set_error("ufe_ssa_run: a device-side barrier wait timed out");
+  } else if (c.status == UFE_DIVERGED) {
+    status = UFE_DIVERGED;
+    set_error("solve_SSA: SSA remains unstable after resetting velocities to zero");
+  } else if (c.resets == 1) {
+    status = UFE_RESET_ONCE;
+  } else if (c.not_converged > 0) {
+    status = UFE_NOT_CONVERGED;
+  }
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->status = status;
+    stats->picard_iterations = c.picard_iterations;
+    stats->linear_solves = c.linear_solves;
+    stats->resets = c.resets;
+    stats->not_converged = c.not_converged;
+    stats->total_sweeps = c.total_sweeps;
+    stats->last_RN = c.last_RN;
+    stats->last_max_residual = c.last_max_residual;
+    for (int k = 0; k < 64; ++k) stats->sweeps[k] = c.sweeps[k];
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+    stats->device_ms = ms;
+  }
+  return status;
+}
+
+extern "C" int ufe_ssa_download(ufe_mesh_h h, ufe_ssa_inout *io, ufe_ssa_out *out) {
+  if (!h || !io) { set_error("ufe_ssa_download: null argument"); return UFE_BAD_ARG; }
+  SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) { set_error("ufe_ssa_download: nothing solved"); return UFE_BAD_ARG; }
+  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA;
+  cudaStream_t s = h->stream;
+  const double *so = w->stage_out;
+  int rc = d2h(io->U_SSA, so, nV, s);
+  if (!rc) rc = d2h(io->V_SSA, so + nV, nV, s);
+  if (!rc) rc = d2h(io->Ux_SSA_Ac, so + 2 * nV, nAc, s);
+  if (!rc) rc = d2h(io->Uy_SSA_Ac, so + 2 * nV + nAc, nAc, s);
+  const double *acb = so + 2 * nV + 2 * nAc;
+  if (out) {
+    if (!rc) rc = d2h(out->Up_SSA_Ac, acb, nAc, s);
+    if (!rc) rc = d2h(out->Uo_SSA_Ac, acb + nAc, nAc, s);
+  }
+  const double *ab = acb + 2 * nAc;
+  if (!rc && io->N_AaAc && !w->zero) rc = d2h(io->N_AaAc, ab, nA, s);
+  if (out && !w->zero) {
+    if (!rc) rc = d2h(out->eta_AaAc, ab + nA, nA, s);
+    if (!rc) rc = d2h(out->S_AaAc, ab + 2 * nA, nA, s);
+    if (!rc) rc = d2h(out->tau_c_AaAc, ab + 3 * nA, nA, s);
+    if (!rc) rc = d2h(out->phi_fric_AaAc, ab + 4 * nA, nA, s);
+  }
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa download");
+  return rc;
+}
+
+extern "C" int ufe_ssa_solve(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, ufe_ssa_inout *io,
+                             ufe_ssa_out *out, ufe_ssa_stats *stats) {
+  int rc = ufe_ssa_upload(h, p, in, io);
+  if (rc < 0) return rc;
+  const int status = ufe_ssa_run(h, p, stats);
+  if (status < 0 && status != UFE_DIVERGED) return status;
+  rc = ufe_ssa_download(h, io, out);
+  if (rc < 0) return rc;
+  return status;
+}
