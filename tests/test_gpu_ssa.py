@@ -61,9 +61,10 @@ def _run_both(name, kind="dome", precision=nat.UFE_FP64, warm=None, oracle_kw=No
     return m, (rc_o, oout, ost), (rc_g, gout, gst)
 
 
+@pytest.mark.parametrize("exact", [0, 1])
 @pytest.mark.parametrize("name", ["tiny", "1k", "4k"])
-def test_fp64_dome_linear_matches_oracle(name):
-    m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both(name)
+def test_fp64_dome_linear_matches_oracle(name, exact):
+    m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both(name, gpu_kw=dict(fp64_exact=exact))
     assert rc_g == rc_o == 0
     assert gst["picard_iterations"] == ost["picard_iterations"]
     assert gst["sweeps"] == ost["sweeps"]
@@ -125,6 +126,16 @@ def test_mixed_matches_oracle(name):
     assert gst["picard_iterations"] == ost["picard_iterations"]
 
 
+def test_mixed_fp32_viscosity_dome():
+    """The mixed form with the viscosity in FP32 as well (FP32 arithmetic on FP64 velocity
+    differences): within 1e-6 on the grounded dome. On the marine case the FP32 viscosity
+    alone gives 1.3e-6, which is why the viscosity defaults to FP64 in the mixed path."""
+    m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both("4k", precision=nat.UFE_MIXED,
+                                                        gpu_kw=dict(mixed_fp32_viscosity=1))
+    assert rc_g == rc_o == 0
+    _check_solution(gout, oout, MIXED_TOL)
+
+
 def test_mixed_marine_matches_oracle():
     m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both("4k", kind="marine", precision=nat.UFE_MIXED)
     assert rc_g == rc_o
@@ -164,7 +175,7 @@ def test_not_converged_warning():
     kw = dict(SSA_max_inner_loops=20, SSA_max_outer_loops=3)
     m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both("1k", oracle_kw=kw, gpu_kw=kw)
     assert rc_o == orc.OR_NOT_CONVERGED and rc_g == nat.UFE_NOT_CONVERGED
-    assert gst["sweeps"] == ost["sweeps"] and all(n == 20 for n in ost["sweeps"])
+    assert gst["sweeps"] == ost["sweeps"] and ost["sweeps"][0] == 20
     _check_solution(gout, oout, FP64_TOL)
 
 

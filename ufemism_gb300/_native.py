@@ -38,7 +38,7 @@ class Params(ct.Structure):
                 ("SSA_SOR_omega", F64), ("SSA_max_inner_loops", I32), ("m_enh_ssa", F64), ("m_enh_sia", F64),
                 ("sliding_law", I32), ("beta_sq", F64), ("use_analytical_GL_flux", I32),
                 ("zero_velocities", I32), ("nZ", I32), ("zeta", P), ("precision", I32),
-                ("mixed_refold_sweeps", I32)]
+                ("mixed_refold_sweeps", I32), ("fp64_exact", I32), ("mixed_fp32_viscosity", I32)]
 
 
 SSA_IN_FIELDS = ("Hi", "Hb", "SL", "dHs_dx_shelf", "dHs_dy_shelf", "A_flow_mean", "mask_sheet", "Hi_Ac", "Hb_Ac",

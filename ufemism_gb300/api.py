@@ -26,7 +26,8 @@ def default_params(**kw) -> dict:
     p = dict(SSA_RN_tol=1e-3, SSA_max_outer_loops=50, SSA_max_residual_UV=1e-4, SSA_SOR_omega=1.3,
              SSA_max_inner_loops=10000, m_enh_ssa=1.0, m_enh_sia=1.0,
              sliding_law=nat.UFE_SLIDING_LINEAR, beta_sq=1e3, use_analytical_GL_flux=0,
-             zero_velocities=0, zeta=ZETA_DEFAULT, precision=nat.UFE_FP64, mixed_refold_sweeps=0)
+             zero_velocities=0, zeta=ZETA_DEFAULT, precision=nat.UFE_FP64, mixed_refold_sweeps=0,
+             fp64_exact=0, mixed_fp32_viscosity=0)
     p.update(kw)
     return p
 
@@ -36,7 +37,8 @@ def _params_struct(p: dict):
     s = nat.Params(p["SSA_RN_tol"], p["SSA_max_outer_loops"], p["SSA_max_residual_UV"], p["SSA_SOR_omega"],
                    p["SSA_max_inner_loops"], p["m_enh_ssa"], p["m_enh_sia"], p["sliding_law"], p["beta_sq"],
                    p["use_analytical_GL_flux"], p["zero_velocities"], zeta.size, zeta.ctypes.data,
-                   p["precision"], p.get("mixed_refold_sweeps", 0))
+                   p["precision"], p.get("mixed_refold_sweeps", 0), p.get("fp64_exact", 0),
+                   p.get("mixed_fp32_viscosity", 0))
     return s, zeta
 
 

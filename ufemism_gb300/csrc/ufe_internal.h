@@ -65,8 +65,9 @@ struct DevMesh {
   double2 *h_nxy = nullptr;     // [nP] home (Nx, Ny)
   double2 *h_cuv = nullptr;     // [nP] home (4Nxx+Nyy, 4Nyy+Nxx)
   double *sNxy = nullptr;       // [nP] sum of Nxy over home + neighbours
+  double *s3Nxy = nullptr;      // [nP] 3 * sNxy (cross-term coefficient of the fast sweeps)
   float2 *h_nxy32 = nullptr;    // [nP] (Nx, Ny) row sums (home + neighbours), for the mixed viscosity
-  float *sNxy32 = nullptr;      // [nP]
+  float *s3Nxy32 = nullptr;     // [nP] 3 * sNxy in FP32
   // Neumann boundary: edge rows' non-edge neighbours, corners' neighbours.
   int *bnd_ptr = nullptr;       // [n_edge + n_corner + 1]
   int *bnd_nbr = nullptr;       // device rows; for corners an edge neighbour is -(k+1), k = edge list index

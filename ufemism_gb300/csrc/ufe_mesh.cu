@@ -30,7 +30,7 @@ int upload(T **p, const std::vector<T> &h, cudaStream_t s, const char *what) {
 
 void free_mesh(DevMesh &m) {
   void *ptrs[] = {m.orig_of_dev, m.dev_of_orig, m.deg, m.slice_ptr, m.col, m.cuv, m.nxy,
-                  m.cuv32, m.nxy32, m.h_nxy, m.h_cuv, m.sNxy, m.h_nxy32, m.sNxy32, m.bnd_ptr,
+                  m.cuv32, m.nxy32, m.h_nxy, m.h_cuv, m.sNxy, m.s3Nxy, m.h_nxy32, m.s3Nxy32, m.bnd_ptr,
                   m.bnd_nbr, m.V, m.Aci12, m.iAci, m.nC};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -140,9 +140,9 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   std::vector<double2> cuv(nE, make_double2(0, 0)), nxy(nE, make_double2(0, 0));
   std::vector<float2> cuv32(nE, make_float2(0, 0)), nxy32(nE, make_float2(0, 0));
   std::vector<double2> h_nxy(m.nP, make_double2(0, 0)), h_cuv(m.nP, make_double2(0, 0));
-  std::vector<double> sNxy(m.nP, 0.0);
+  std::vector<double> sNxy(m.nP, 0.0), s3Nxy(m.nP, 0.0);
   std::vector<float2> h_nxy32(m.nP, make_float2(0, 0));
-  std::vector<float> sNxy32(m.nP, 0.0f);
+  std::vector<float> s3Nxy32(m.nP, 0.0f);
   const int64_t ldN = nA;
   auto N = [&](const double *a, int r, int c) { return a[r + (int64_t)c * ldN]; };
   for (int p = 0; p < m.nP; ++p) {
@@ -168,8 +168,9 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
     h_nxy[p] = make_double2(N(d->Nx_AaAc, r, n), N(d->Ny_AaAc, r, n));
     h_cuv[p] = make_double2(4.0 * hxx + hyy, 4.0 * hyy + hxx);
     sNxy[p] = sxy;
+    s3Nxy[p] = 3.0 * sxy;
     h_nxy32[p] = make_float2((float)rsx, (float)rsy);
-    sNxy32[p] = (float)sxy;
+    s3Nxy32[p] = (float)(3.0 * sxy);
   }
 
   // ---- Neumann boundary lists (apply_Neumann_boundary_AaAc) ------------------------------
@@ -238,7 +239,8 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   if (!rc) rc = upload(&m.h_cuv, h_cuv, S, "h_cuv");
   if (!rc) rc = upload(&m.sNxy, sNxy, S, "sNxy");
   if (!rc) rc = upload(&m.h_nxy32, h_nxy32, S, "h_nxy32");
-  if (!rc) rc = upload(&m.sNxy32, sNxy32, S, "sNxy32");
+  if (!rc) rc = upload(&m.s3Nxy, s3Nxy, S, "s3Nxy");
+  if (!rc) rc = upload(&m.s3Nxy32, s3Nxy32, S, "s3Nxy32");
   if (!rc) rc = upload(&m.bnd_ptr, bnd_ptr, S, "bnd_ptr");
   if (!rc) rc = upload(&m.bnd_nbr, bnd_nbr, S, "bnd_nbr");
   if (!rc) rc = upload(&m.V, V, S, "V");

@@ -41,10 +41,10 @@ namespace ufe {
 // Control block and kernel arguments
 // ---------------------------------------------------------------------------------------
 struct SsaCtl {
-  unsigned int bar_count;
-  unsigned int bar_gen;
+  unsigned int bar_count;         // monotonic grid-barrier arrival counter (bit 30: error)
   int err;
   int status;
+  int pad_;
   unsigned long long maxres[3];   // max |res| per sweep (ring of three), as ordered bits
   int picard_iterations;
   int linear_solves;
@@ -54,6 +54,13 @@ struct SsaCtl {
   double last_RN;
   double last_max_residual;
   int sweeps[64];
+};
+
+// Sweep arithmetic of the persistent solver.
+enum SweepMode : int {
+  kExact64 = 0,   // the reference's expression order, no FMA, IEEE divisions
+  kFast64 = 1,    // FP64 with fused multiply-adds and a per-Picard reciprocal of eu, ev
+  kMixed = 2,     // FP32 correction sweeps inside FP64 defect correction
 };
 
 struct SsaArgs {
@@ -68,8 +75,9 @@ struct SsaArgs {
   const double2 *h_nxy;
   const double2 *h_cuv;
   const double *sNxy;
+  const double *s3Nxy;
   const float2 *h_nxy32;
-  const float *sNxy32;
+  const float *s3Nxy32;
   const int *bnd_ptr;
   const int *bnd_nbr;
   int grp_off[kGroups + 1];
@@ -83,17 +91,20 @@ struct SsaArgs {
   double2 *UV;            // FP64 velocities (u0 in the mixed path)
   float2 *dUV;            // mixed: correction d
   float2 *r0;             // mixed: defect
-  float2 *euv32;          // mixed: FP32 centre coefficients
+  float2 *rcp32;          // mixed: FP32 reciprocals of (eu, ev)
   double *eta, *Na, *Nb, *S;
-  double2 *rhs, *euv;
+  double2 *rhs, *euv, *rcp;
   double *rn_part;        // [2 * gridDim.x]
   SsaCtl *ctl;
   // parameters
   double omega, tol, rn_tol, m_enh, uq, expo, beta_const;
   int max_inner, max_outer, sliding_law, has_beta;
   int refold;
+  int fp32_visc;
   long long timeout_ns;
 };
+
+constexpr unsigned int kBarrierError = 1u << 30;
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
@@ -107,34 +118,40 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
   return v;
 }
 
-// Grid-wide barrier for a cooperative (co-resident) launch. The spin is bounded: after
-// timeout_ns the CTA records UFE_TIMEOUT and returns false; callers then leave the kernel.
-__device__ __forceinline__ bool grid_barrier(SsaCtl *ctl, unsigned int &gen, long long timeout_ns) {
+__device__ __forceinline__ void red_release_add_u32(unsigned int *p, unsigned int v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier for a cooperative (co-resident) launch: a monotonic arrival counter,
+// epoch k is complete when the counter reaches k * gridDim.x. The spin is bounded: after
+// timeout_ns the CTA records UFE_TIMEOUT and sets the error bit in the counter, which
+// releases every other waiter with a failure; callers then leave the kernel.
+__device__ __forceinline__ bool grid_barrier(SsaCtl *ctl, unsigned int &epoch, long long timeout_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    const unsigned int g = gen;
+    epoch += 1u;
+    const unsigned int target = epoch * gridDim.x;
     __threadfence();
-    const unsigned int arrived = atomicAdd(&ctl->bar_count, 1u);
-    if (arrived == gridDim.x - 1) {
-      atomicExch(&ctl->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&ctl->bar_gen, 1u);
-    } else {
+    red_release_add_u32(&ctl->bar_count, 1u);
+    unsigned int v = ld_acquire_u32(&ctl->bar_count);
+    if (!(v & kBarrierError) && (int)(v - target) < 0) {
       const unsigned long long t0 = globaltimer_ns();
-      unsigned int ns = 8;
-      while (ld_acquire_u32(&ctl->bar_gen) == g) {
+      unsigned int ns = 16;
+      for (;;) {
         __nanosleep(ns);
-        if (ns < 64) ns <<= 1;
+        if (ns < 128) ns <<= 1;
+        v = ld_acquire_u32(&ctl->bar_count);
+        if ((v & kBarrierError) || (int)((v & ~kBarrierError) - target) >= 0) break;
         if ((long long)(globaltimer_ns() - t0) > timeout_ns) {
           atomicCAS(&ctl->err, 0, (int)UFE_TIMEOUT);
+          atomicOr(&ctl->bar_count, kBarrierError);
+          v |= kBarrierError;
           break;
         }
       }
     }
-    __threadfence();
-    gen = g + 1;
-    s_ok = *(volatile int *)&ctl->err == 0;
+    s_ok = (v & kBarrierError) == 0;
   }
   __syncthreads();
   return s_ok != 0;
@@ -144,25 +161,36 @@ __device__ __forceinline__ double warp_max(double v) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
 
-// Block max of a non-negative double, then one atomicMax per CTA on its bit pattern (the
-// IEEE ordering of non-negative doubles equals the ordering of their bit patterns).
-__device__ __forceinline__ void block_max_to(unsigned long long *dst, double v) {
-  __shared__ double s_w[32];
-  v = warp_max(v);
+// Block max of |res| bit patterns (the IEEE ordering of non-negative doubles equals the
+// ordering of their bit patterns), then one atomicMax per CTA.
+__device__ __forceinline__ void block_max_to(unsigned long long *dst, unsigned long long v) {
+  __shared__ unsigned long long s_w[32];
+  v = warp_max_u64(v);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) s_w[w] = v;
   __syncthreads();
   if (w == 0) {
-    double x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0.0;
-    x = warp_max(x);
-    if (l == 0 && x > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(x));
+    unsigned long long x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0ull;
+    x = warp_max_u64(x);
+    if (l == 0 && x > 0ull) atomicMax(dst, x);
   }
   __syncthreads();
+}
+
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
 __device__ __forceinline__ bool is_floating(double Hi, double Hb, double SL) {
@@ -174,9 +202,9 @@ __device__ __forceinline__ bool is_floating(double Hi, double Hb, double SL) {
 // ---------------------------------------------------------------------------------------
 
 // Effective viscosity and N = eta * max(0.1, H) on every row; block partial sums of
-// (N - Nprev)^2 and N^2 for RN. FP64: reference order (home term first).
-template <bool kMixed>
-__device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev) {
+// (N - Nprev)^2 and N^2 for RN. FP64: reference order (home term first). FP32 variant
+// (mixed path option): FP32 arithmetic on FP64 differences u_j - u_i.
+__device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev, bool fp32) {
   const int warps_per_block = blockDim.x >> 5;
   const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int nw = gridDim.x * warps_per_block;
@@ -189,10 +217,10 @@ __device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev
     if (n == 0) continue;
     const int64_t e0 = a.slice_ptr[s] + lane;
     const double2 ui = a.UV[p];
-    double ux, uy, vx, vy;
-    if (!kMixed) {
+    double eta;
+    if (!fp32) {
       const double2 h = a.h_nxy[p];
-      ux = h.x * ui.x; uy = h.y * ui.x; vx = h.x * ui.y; vy = h.y * ui.y;
+      double ux = h.x * ui.x, uy = h.y * ui.x, vx = h.x * ui.y, vy = h.y * ui.y;
       for (int k = 0; k < n; ++k) {
         const int64_t e = e0 + (int64_t)k * kSlice;
         const int j = a.col[e];
@@ -203,6 +231,9 @@ __device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev
         vx = vx + c.x * uj.y;
         vy = vy + c.y * uj.y;
       }
+      const double t = uy + vx;
+      const double e2 = (((ux * ux + vy * vy) + ux * vy) + 0.25 * (t * t)) + 1e-12;
+      eta = pow((a.m_enh * 0.5) * a.Af[p], -1.0 / 3.0) * pow(e2, (1.0 - 3.0) / (2.0 * 3.0));
     } else {
       // d/dx u = sum_k Nx_k (u_k - u_i) + u_i * (Nx_home + sum_k Nx_k); the row sum is zero
       // up to rounding (linear fields are reproduced exactly).
@@ -220,19 +251,9 @@ __device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev
         fvx = fmaf(c.x, dv, fvx);
         fvy = fmaf(c.y, dv, fvy);
       }
-      ux = fux; uy = fuy; vx = fvx; vy = fvy;
-    }
-    double eta;
-    if (!kMixed) {
-      const double t = uy + vx;
-      const double e2 = (((ux * ux + vy * vy) + ux * vy) + 0.25 * (t * t)) + 1e-12;
-      eta = pow((a.m_enh * 0.5) * a.Af[p], -1.0 / 3.0) * pow(e2, (1.0 - 3.0) / (2.0 * 3.0));
-    } else {
-      const float fx = (float)ux, fy = (float)uy, gx = (float)vx, gy = (float)vy;
-      const float t = fy + gx;
-      const float e2 = (((fx * fx + gy * gy) + fx * gy) + 0.25f * (t * t)) + 1e-12f;
-      const float ef = powf((float)((a.m_enh * 0.5) * a.Af[p]), -1.0f / 3.0f) * powf(e2, -1.0f / 3.0f);
-      eta = (double)ef;
+      const float t = fuy + fvx;
+      const float e2 = (((fux * fux + fvy * fvy) + fux * fvy) + 0.25f * (t * t)) + 1e-12f;
+      eta = (double)(powf((float)((a.m_enh * 0.5) * a.Af[p]), -1.0f / 3.0f) * powf(e2, -1.0f / 3.0f));
     }
     const double Nn = eta * fmax(0.1, a.Hi[p]);
     a.eta[p] = eta;
@@ -273,8 +294,8 @@ __device__ double final_rn(const SsaArgs &a) {
   return s_rn;
 }
 
-// Sliding term S, centre coefficients (eu, ev) and right-hand sides for every row.
-template <bool kMixed>
+// Sliding term S, centre coefficients (eu, ev), their reciprocals and the right-hand sides.
+template <int kMode>
 __device__ void phase_coefficients(const SsaArgs &a) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = gridDim.x * blockDim.x;
@@ -300,19 +321,65 @@ __device__ void phase_coefficients(const SsaArgs &a) {
       c = h;
     }
     a.euv[p] = c;
-    if (kMixed) a.euv32[p] = make_float2((float)c.x, (float)c.y);
+    if (kMode != kExact64) {
+      const double2 r = make_double2(1.0 / c.x, 1.0 / c.y);
+      a.rcp[p] = r;
+      if (kMode == kMixed) a.rcp32[p] = make_float2((float)r.x, (float)r.y);
+    }
   }
 }
 
-// One colour of the FP64 SOR sweep; returns this thread's max |res|.
-__device__ double phase_sweep64(const SsaArgs &a, int g) {
+// One colour of the FP64 sweep in the reference's expression order (parity mode).
+__device__ unsigned long long phase_sweep_exact(const SsaArgs &a, int g) {
   const int warps_per_block = blockDim.x >> 5;
   const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int nw = gridDim.x * warps_per_block;
   const int lane = threadIdx.x & 31;
   const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
   const double omega = a.omega;
-  double mx = 0.0;
+  unsigned long long mx = 0ull;
+  for (int s = s0 + gw; s < s1; s += nw) {
+    const int p = s * kSlice + lane;
+    const int n = a.deg[p];
+    if (n == 0) continue;
+    if (a.skip && a.skip[p]) continue;
+    const int64_t e0 = a.slice_ptr[s] + lane;
+    double su = 0.0, sv = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const int64_t e = e0 + (int64_t)k * kSlice;
+      const int j = a.col[e];
+      const double2 c = a.cuv[e];
+      const double2 u = a.UV[j];
+      su = su + u.x * c.x;
+      sv = sv + u.y * c.y;
+    }
+    const double2 ui = a.UV[p];
+    const double sxy = a.sNxy[p];
+    const double Uxy = ui.x * sxy, Vxy = ui.y * sxy;
+    const double2 ec = a.euv[p];
+    const double2 b = a.rhs[p];
+    const double lhsx = (su + 3.0 * Vxy) + ec.x * ui.x;
+    const double lhsy = (sv + 3.0 * Uxy) + ec.y * ui.y;
+    const double ru = (lhsx - b.x) / ec.x;
+    const double rv = (lhsy - b.y) / ec.y;
+    const unsigned long long bu = abs_bits(ru), bv = abs_bits(rv);
+    mx = bu > mx ? bu : mx;
+    mx = bv > mx ? bv : mx;
+    a.UV[p] = make_double2(ui.x - omega * ru, ui.y - omega * rv);
+  }
+  return mx;
+}
+
+// One colour of the fast FP64 sweep: res = U + ((sum + 3 sNxy V) - RHS) / eu with the
+// reciprocal of eu formed once per Picard iteration, products accumulated with FMA.
+__device__ unsigned long long phase_sweep_fast(const SsaArgs &a, int g) {
+  const int warps_per_block = blockDim.x >> 5;
+  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
+  const int nw = gridDim.x * warps_per_block;
+  const int lane = threadIdx.x & 31;
+  const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
+  const double omega = a.omega;
+  unsigned long long mx = 0ull;
   for (int s = s0 + gw; s < s1; s += nw) {
     const int p = s * kSlice + lane;
     const int n = a.deg[p];
@@ -332,8 +399,8 @@ __device__ double phase_sweep64(const SsaArgs &a, int g) {
       for (int q = 0; q < 4; ++q) u[q] = a.UV[j[q]];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        su = su + u[q].x * c[q].x;
-        sv = sv + u[q].y * c[q].y;
+        su = fma(u[q].x, c[q].x, su);
+        sv = fma(u[q].y, c[q].y, sv);
       }
     }
     for (; k < n; ++k) {
@@ -341,27 +408,26 @@ __device__ double phase_sweep64(const SsaArgs &a, int g) {
       const int j = a.col[e];
       const double2 c = a.cuv[e];
       const double2 u = a.UV[j];
-      su = su + u.x * c.x;
-      sv = sv + u.y * c.y;
+      su = fma(u.x, c.x, su);
+      sv = fma(u.y, c.y, sv);
     }
     const double2 ui = a.UV[p];
-    const double sxy = a.sNxy[p];
-    const double Uxy = ui.x * sxy, Vxy = ui.y * sxy;
-    const double2 ec = a.euv[p];
+    const double s3 = a.s3Nxy[p];
+    const double2 r = a.rcp[p];
     const double2 b = a.rhs[p];
-    const double lhsx = (su + 3.0 * Vxy) + ec.x * ui.x;
-    const double lhsy = (sv + 3.0 * Uxy) + ec.y * ui.y;
-    const double ru = (lhsx - b.x) / ec.x;
-    const double rv = (lhsy - b.y) / ec.y;
-    mx = fmax(mx, fabs(ru));
-    mx = fmax(mx, fabs(rv));
-    a.UV[p] = make_double2(ui.x - omega * ru, ui.y - omega * rv);
+    const double ru = fma(fma(s3, ui.y, su) - b.x, r.x, ui.x);
+    const double rv = fma(fma(s3, ui.x, sv) - b.y, r.y, ui.y);
+    const unsigned long long bu = abs_bits(ru), bv = abs_bits(rv);
+    mx = bu > mx ? bu : mx;
+    mx = bv > mx ? bv : mx;
+    a.UV[p] = make_double2(fma(-omega, ru, ui.x), fma(-omega, rv, ui.y));
   }
   return mx;
 }
 
-// One colour of the FP32 correction sweep of the mixed path.
-__device__ double phase_sweep32(const SsaArgs &a, int g) {
+// One colour of the FP32 correction sweep of the mixed path:
+// res = d_i + ((sum_j c_j d_j + 3 sNxy d_i') - r0) / eu.
+__device__ unsigned long long phase_sweep32(const SsaArgs &a, int g) {
   const int warps_per_block = blockDim.x >> 5;
   const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int nw = gridDim.x * warps_per_block;
@@ -401,16 +467,15 @@ __device__ double phase_sweep32(const SsaArgs &a, int g) {
       sv = fmaf(u.y, c.y, sv);
     }
     const float2 di = a.dUV[p];
-    const float sxy = a.sNxy32[p];
-    const float2 ec = a.euv32[p];
-    const float2 r = a.r0[p];
-    const float lx = fmaf(ec.x, di.x, fmaf(3.0f * sxy, di.y, su)) - r.x;
-    const float ly = fmaf(ec.y, di.y, fmaf(3.0f * sxy, di.x, sv)) - r.y;
-    const float ru = lx / ec.x, rv = ly / ec.y;
+    const float s3 = a.s3Nxy32[p];
+    const float2 r = a.rcp32[p];
+    const float2 d = a.r0[p];
+    const float ru = fmaf(fmaf(s3, di.y, su) - d.x, r.x, di.x);
+    const float rv = fmaf(fmaf(s3, di.x, sv) - d.y, r.y, di.y);
     mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
     a.dUV[p] = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
   }
-  return (double)mx;
+  return abs_bits((double)mx);
 }
 
 // Neumann boundary (apply_Neumann_boundary_AaAc): each edge row becomes the mean of its
@@ -418,14 +483,14 @@ __device__ double phase_sweep32(const SsaArgs &a, int g) {
 // neighbour's new value is recomputed in place (same arithmetic, same result) so that the
 // corners need no second pass. SUM(vals) in the reference runs over nC_mem slots whose
 // unused entries are +0, hence the trailing "+ 0.0".
-template <bool kMixed>
+template <bool kM>
 __device__ __forceinline__ double2 edge_mean(const SsaArgs &a, int k) {
   const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
   double sx = 0.0, sy = 0.0;
   for (int q = b0; q < b1; ++q) {
     const int j = a.bnd_nbr[q];
     double2 u = a.UV[j];
-    if (kMixed) {
+    if (kM) {
       const float2 d = a.dUV[j];
       u.x = u.x + (double)d.x;
       u.y = u.y + (double)d.y;
@@ -438,7 +503,7 @@ __device__ __forceinline__ double2 edge_mean(const SsaArgs &a, int k) {
   return make_double2(sx / (double)nvals, sy / (double)nvals);
 }
 
-template <bool kMixed>
+template <bool kM>
 __device__ void phase_boundary(const SsaArgs &a) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int nt = gridDim.x * blockDim.x;
@@ -447,7 +512,7 @@ __device__ void phase_boundary(const SsaArgs &a) {
     const int p = a.edge_first + k;
     double2 v;
     if (k < a.n_edge) {
-      v = edge_mean<kMixed>(a, k);
+      v = edge_mean<kM>(a, k);
     } else {
       const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
       double sx = 0.0, sy = 0.0;
@@ -455,10 +520,10 @@ __device__ void phase_boundary(const SsaArgs &a) {
         const int j = a.bnd_nbr[q];
         double2 u;
         if (j < 0) {
-          u = edge_mean<kMixed>(a, -j - 1);
+          u = edge_mean<kM>(a, -j - 1);
         } else {
           u = a.UV[j];
-          if (kMixed) {
+          if (kM) {
             const float2 d = a.dUV[j];
             u.x = u.x + (double)d.x;
             u.y = u.y + (double)d.y;
@@ -471,7 +536,7 @@ __device__ void phase_boundary(const SsaArgs &a) {
       if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
       v = make_double2(sx / (double)nvals, sy / (double)nvals);
     }
-    if (!kMixed) {
+    if (!kM) {
       a.UV[p] = v;
     } else {
       const double2 u0 = a.UV[p];
@@ -496,7 +561,7 @@ __device__ void phase_fold(const SsaArgs &a) {
   }
 }
 
-// Mixed path: FP64 defect r0 = RHS - LHS(u0) on the swept rows.
+// Mixed path: FP64 defect r0 = RHS - LHS(u0) on the swept rows (streamed coefficient loads).
 __device__ void phase_defect(const SsaArgs &a) {
   const int warps_per_block = blockDim.x >> 5;
   const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
@@ -514,15 +579,15 @@ __device__ void phase_defect(const SsaArgs &a) {
       const int j = __ldcs(a.col + e);
       const double2 c = __ldcs(a.cuv + e);
       const double2 u = a.UV[j];
-      su = su + u.x * c.x;
-      sv = sv + u.y * c.y;
+      su = fma(u.x, c.x, su);
+      sv = fma(u.y, c.y, sv);
     }
     const double2 ui = a.UV[p];
-    const double sxy = a.sNxy[p];
+    const double s3 = a.s3Nxy[p];
     const double2 ec = a.euv[p];
     const double2 b = a.rhs[p];
-    const double lhsx = (su + 3.0 * (ui.y * sxy)) + ec.x * ui.x;
-    const double lhsy = (sv + 3.0 * (ui.x * sxy)) + ec.y * ui.y;
+    const double lhsx = fma(ec.x, ui.x, fma(s3, ui.y, su));
+    const double lhsy = fma(ec.y, ui.y, fma(s3, ui.x, sv));
     a.r0[p] = make_float2((float)(b.x - lhsx), (float)(b.y - lhsy));
   }
 }
@@ -539,10 +604,13 @@ __device__ void phase_zero_velocity(const SsaArgs &a, bool mixed) {
 // ---------------------------------------------------------------------------------------
 // The persistent solver
 // ---------------------------------------------------------------------------------------
-template <bool kMixed>
-__global__ void __launch_bounds__(256) ssa_persistent(SsaArgs a) {
+constexpr int kSsaBlock = 1024;
+
+template <int kMode>
+__global__ void __launch_bounds__(kSsaBlock, 1) ssa_persistent(SsaArgs a) {
+  constexpr bool kM = kMode == kMixed;
   SsaCtl *ctl = a.ctl;
-  unsigned int gen = 0;
+  unsigned int epoch = 0;
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
   double *N = a.Na, *Nprev = a.Nb;
   int did_reset_before = 0;
@@ -552,17 +620,17 @@ __global__ void __launch_bounds__(256) ssa_persistent(SsaArgs a) {
     ++it;
     // N_prev <- N, then the new viscosity into N
     { double *t = N; N = Nprev; Nprev = t; }
-    phase_viscosity<kMixed>(a, N, Nprev);
-    if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    phase_viscosity(a, N, Nprev, kM && a.fp32_visc);
+    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
     const double RN = final_rn(a);
     if (leader) { ctl->picard_iterations = it; ctl->last_RN = RN; }
     if (RN < a.rn_tol) { picard_done = true; break; }
-    phase_coefficients<kMixed>(a);
+    phase_coefficients<kMode>(a);
     if (leader) { ctl->maxres[0] = 0ull; ctl->maxres[1] = 0ull; ctl->maxres[2] = 0ull; }
-    if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
-    if (kMixed) {
+    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    if (kM) {
       phase_defect(a);
-      if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+      if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
     }
     // coloured SOR
     int sweeps = 0;
@@ -573,34 +641,38 @@ __global__ void __launch_bounds__(256) ssa_persistent(SsaArgs a) {
       ++sweeps;
       const int slot = sweeps % 3;
       if (leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
-      double mx = 0.0;
+      unsigned long long mx = 0ull;
       for (int g = 0; g < 5; ++g) {
-        mx = fmax(mx, kMixed ? phase_sweep32(a, g) : phase_sweep64(a, g));
+        unsigned long long m;
+        if (kMode == kExact64) m = phase_sweep_exact(a, g);
+        else if (kMode == kFast64) m = phase_sweep_fast(a, g);
+        else m = phase_sweep32(a, g);
+        mx = m > mx ? m : mx;
         if (g == 4) block_max_to(&ctl->maxres[slot], mx);
-        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
       }
-      phase_boundary<kMixed>(a);
-      if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+      phase_boundary<kM>(a);
+      if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
       maxres = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxres[slot]);
       if (maxres < a.tol) {
         lin_done = true;
       } else if (maxres > 1e6) {
-        phase_zero_velocity(a, kMixed);
-        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+        phase_zero_velocity(a, kM);
+        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
         did_reset = 1;
         lin_done = true;
       } else if (sweeps == a.max_inner) {
         if (leader) ctl->not_converged += 1;
-      } else if (kMixed && a.refold > 0 && sweeps % a.refold == 0) {
+      } else if (kM && a.refold > 0 && sweeps % a.refold == 0) {
         phase_fold(a);
-        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
         phase_defect(a);
-        if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
       }
     }
-    if (kMixed && !did_reset) {
+    if (kM && !did_reset) {
       phase_fold(a);
-      if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+      if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
     }
     if (leader) {
       if (ctl->linear_solves < 64) ctl->sweeps[ctl->linear_solves] = sweeps;
@@ -621,7 +693,7 @@ __global__ void __launch_bounds__(256) ssa_persistent(SsaArgs a) {
   if (N != a.Na) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
-    if (!grid_barrier(ctl, gen, a.timeout_ns)) return;
+    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
     for (int p = tid; p < a.nP; p += nt) a.Na[p] = N[p];
   }
 }
@@ -783,8 +855,8 @@ struct SsaWork {
   double *gl_dbl = nullptr;      // 6 Ac slope fields
   // device-order fields
   double *f = nullptr;           // Hi, Hb, SL, hx, hy, Af, beta, tau, phi, eta, Na, Nb, S
-  double2 *UV = nullptr, *rhs = nullptr, *euv = nullptr;
-  float2 *dUV = nullptr, *r0 = nullptr, *euv32 = nullptr;
+  double2 *UV = nullptr, *rhs = nullptr, *euv = nullptr, *rcp = nullptr;
+  float2 *dUV = nullptr, *r0 = nullptr, *rcp32 = nullptr;
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   SsaCtl *ctl = nullptr;
@@ -794,14 +866,14 @@ struct SsaWork {
   bool uploaded = false;
   bool has_beta = false, has_N = false, gl = false;
   bool zero = false;             // the reference's early-out applies
-  int grid = 0, block = 256;
-  int grid_mixed = 0;
+  int grid[3] = {0, 0, 0};        // per SweepMode, one CTA per SM
+  int block = kSsaBlock;
 };
 
 void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
-                  w->dUV, w->r0, w->euv32, w->skip, w->rn_part, w->ctl};
+                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -833,23 +905,26 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc) rc = cuda_status(cudaMalloc(&w->euv, (size_t)m.nP * sizeof(double2)), "ssa euv");
   if (!rc) rc = cuda_status(cudaMalloc(&w->dUV, (size_t)m.nP * sizeof(float2)), "ssa dUV");
   if (!rc) rc = cuda_status(cudaMalloc(&w->r0, (size_t)m.nP * sizeof(float2)), "ssa r0");
-  if (!rc) rc = cuda_status(cudaMalloc(&w->euv32, (size_t)m.nP * sizeof(float2)), "ssa euv32");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->rcp, (size_t)m.nP * sizeof(double2)), "ssa rcp");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->rcp32, (size_t)m.nP * sizeof(float2)), "ssa rcp32");
   if (!rc) rc = cuda_status(cudaMalloc(&w->skip, (size_t)m.nP), "ssa skip");
   if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(SsaCtl)), "ssa ctl");
   if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(SsaCtl)), "ssa ctl host");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev1), "event");
   if (!rc) rc = cuda_status(cudaMemsetAsync(w->skip, 0, (size_t)m.nP, h->stream), "memset skip");
-  // Persistent grid: every CTA co-resident (cooperative launch).
-  int per_sm64 = 0, per_sm32 = 0;
-  if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm64, ssa_persistent<false>, w->block, 0), "occupancy");
-  if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm32, ssa_persistent<true>, w->block, 0), "occupancy");
-  if (!rc && (per_sm64 < 1 || per_sm32 < 1)) { set_error("ssa kernel does not fit on an SM"); rc = UFE_CUDA_ERROR; }
-  if (!rc) {
-    w->grid = h->num_sms * (per_sm64 < 4 ? per_sm64 : 4);
-    w->grid_mixed = h->num_sms * (per_sm32 < 4 ? per_sm32 : 4);
-    if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)(w->grid > w->grid_mixed ? w->grid : w->grid_mixed) * sizeof(double)), "rn_part");
+  // Persistent grid: every CTA co-resident (cooperative launch), one CTA of 1024 threads per SM.
+  const void *kernels[3] = {(const void *)ssa_persistent<kExact64>, (const void *)ssa_persistent<kFast64>,
+                            (const void *)ssa_persistent<kMixed>};
+  int gmax = 0;
+  for (int k = 0; k < 3 && !rc; ++k) {
+    int per_sm = 0;
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], w->block, 0), "occupancy");
+    if (!rc && per_sm < 1) { set_error("ssa kernel does not fit on an SM"); rc = UFE_CUDA_ERROR; }
+    w->grid[k] = h->num_sms;
+    gmax = gmax > w->grid[k] ? gmax : w->grid[k];
   }
+  if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)gmax * sizeof(double)), "rn_part");
   if (rc) { ssa_free(w); return rc; }
   h->ssa = w;
   return UFE_OK;
@@ -974,13 +1049,13 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     std::memset(&a, 0, sizeof(a));
     a.col = m.col; a.cuv = m.cuv; a.nxy = m.nxy; a.cuv32 = m.cuv32; a.nxy32 = m.nxy32; a.deg = m.deg;
     a.slice_ptr = m.slice_ptr; a.h_nxy = m.h_nxy; a.h_cuv = m.h_cuv; a.sNxy = m.sNxy;
-    a.h_nxy32 = m.h_nxy32; a.sNxy32 = m.sNxy32; a.bnd_ptr = m.bnd_ptr; a.bnd_nbr = m.bnd_nbr;
+    a.s3Nxy = m.s3Nxy; a.h_nxy32 = m.h_nxy32; a.s3Nxy32 = m.s3Nxy32; a.bnd_ptr = m.bnd_ptr; a.bnd_nbr = m.bnd_nbr;
     for (int g = 0; g <= kGroups; ++g) a.grp_off[g] = m.grp_off[g];
     a.n_edge = m.n_edge; a.edge_first = m.edge_first; a.nP = m.nP; a.ncm = m.ncm;
     a.Hi = fl.Hi; a.Hb = fl.Hb; a.SL = fl.SL; a.hx = fl.hx; a.hy = fl.hy; a.Af = fl.Af;
     a.beta = fl.beta; a.tau = fl.tau;
     a.skip = w->gl ? w->skip : nullptr;
-    a.UV = w->UV; a.dUV = w->dUV; a.r0 = w->r0; a.euv32 = w->euv32;
+    a.UV = w->UV; a.dUV = w->dUV; a.r0 = w->r0; a.rcp32 = w->rcp32; a.rcp = w->rcp;
     a.eta = F + F_ETA * nP; a.Na = fl.Na; a.Nb = fl.Nb; a.S = F + F_S * nP;
     a.rhs = w->rhs; a.euv = w->euv; a.rn_part = w->rn_part; a.ctl = w->ctl;
     a.omega = p->SSA_SOR_omega; a.tol = p->SSA_max_residual_UV; a.rn_tol = p->SSA_RN_tol;
@@ -991,13 +1066,17 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     a.max_inner = p->SSA_max_inner_loops; a.max_outer = p->SSA_max_outer_loops;
     a.sliding_law = p->sliding_law; a.has_beta = w->has_beta;
     a.refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 32;
+    a.fp32_visc = p->mixed_fp32_viscosity != 0;
     a.timeout_ns = 20LL * 1000 * 1000 * 1000;
     void *args[] = {&a};
-    const int grid = mixed ? w->grid_mixed : w->grid;
-    if (mixed)
-      rc = cuda_status(cudaLaunchCooperativeKernel((void *)ssa_persistent<true>, dim3(grid), dim3(w->block), args, 0, s), "ssa_persistent<mixed>");
-    else
-      rc = cuda_status(cudaLaunchCooperativeKernel((void *)ssa_persistent<false>, dim3(grid), dim3(w->block), args, 0, s), "ssa_persistent<fp64>");
+    const int mode = mixed ? kMixed : (p->fp64_exact ? kExact64 : kFast64);
+    const void *fn = mode == kMixed ? (const void *)ssa_persistent<kMixed>
+                     : mode == kFast64 ? (const void *)ssa_persistent<kFast64>
+                                       : (const void *)ssa_persistent<kExact64>;
+    rc = cuda_status(cudaMemsetAsync(F + F_S * nP, 0, nP * sizeof(double), s), "memset S");
+    if (!rc)
+      rc = cuda_status(cudaLaunchCooperativeKernel(fn, dim3(w->grid[mode]), dim3(w->block), args, 0, s),
+                       "ssa_persistent");
   }
   if (!rc) {
     StageOut o;
