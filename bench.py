@@ -254,8 +254,33 @@ def run_reference(args):
     return 0
 
 
+def profile_case(args):
+    """One capped solve for profiler captures: a single linear solve of exactly
+    ``--profile-sweeps`` SOR sweeps (SSA_max_outer_loops = 1) on the chosen workload size,
+    repeated ``--steps`` times after ``--warmup`` untimed runs."""
+    import torch
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api
+    api.init(0)
+    base, mesh, ssa, sia = make_workload(args.size)
+    dm = api.DeviceMesh(mesh)
+    prec = {"mixed": nat.UFE_MIXED, "fp64": nat.UFE_FP64, "exact": nat.UFE_FP64}[args.profile_case]
+    p = api.default_params(precision=prec, SSA_max_outer_loops=1, SSA_max_inner_loops=args.profile_sweeps,
+                           fp64_exact=1 if args.profile_case == "exact" else 0)
+    dm.ssa_upload(ssa, p)
+    times, st = timed_runs(dm, p, args.steps, args.warmup, dm.stream)
+    ms = float(np.mean(times))
+    print(json.dumps({"profile_case": args.profile_case, "size": args.size, "sweeps": st["total_sweeps"],
+                      "ms_per_solve": ms, "us_per_sweep": 1e3 * ms / max(1, st["total_sweeps"])}))
+    dm.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-case", choices=["mixed", "fp64", "exact"], default=None,
+                    help="run one capped solve (for profiler captures) instead of the benchmark")
+    ap.add_argument("--profile-sweeps", type=int, default=60)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -266,6 +291,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_case:
+        return profile_case(args)
 
     rank, world, local = dist_info()
     import torch

@@ -17,6 +17,7 @@ namespace ufe {
 constexpr int kMaxDeg = 32;    // neighbours per AaAc row the kernels accept (nconmax <= 31)
 constexpr int kSlice = 32;     // rows per SELL slice (one warp, one row per lane)
 constexpr int kGroups = 6;     // colours 1..5 (rows swept by SOR), then the edge rows
+constexpr int kMaxRuns = 24;   // distinct slice widths per group (degrees are <= nconmax)
 
 // Physical constants, parameters_module.f90:9-21.
 constexpr double kIceDensity = 910.0;
@@ -46,6 +47,14 @@ struct DevMesh {
   int nSlices = 0;
   int grp_off[kGroups + 1] = {};  // device row offsets of the groups (multiples of 32)
   int grp_rows[kGroups] = {};   // real rows per group
+  // Runs of equal slice width inside each group (rows are sorted by degree, so widths only
+  // fall): run r of group g covers slices [run_s0, next run's run_s0) of width run_w, whose
+  // first SELL entry is run_e0. Kernels compute a slice's entry offset from this table
+  // instead of loading it.
+  int n_runs[kGroups] = {};
+  int run_s0[kGroups][kMaxRuns] = {};
+  int run_w[kGroups][kMaxRuns] = {};
+  int64_t run_e0[kGroups][kMaxRuns] = {};
   int n_edge = 0;               // edge rows excluding the corners
   int n_corner = 0;             // 4
   int edge_first = 0;           // device row of the first edge row (== grp_off[5])

@@ -136,7 +136,23 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
     nE += (int64_t)w * kSlice;
   }
   m.nE = nE;
-  std::vector<int> col(nE, 0);
+  for (int g = 0; g < kGroups; ++g) {
+    const int sa = m.grp_off[g] / kSlice, sb = m.grp_off[g + 1] / kSlice;
+    int prev_w = -1;
+    for (int s = sa; s < sb; ++s) {
+      const int w = (int)(((s + 1 < m.nSlices ? slice_ptr[s + 1] : nE) - slice_ptr[s]) / kSlice);
+      if (w != prev_w) {
+        if (m.n_runs[g] == kMaxRuns) { set_error("ufe_mesh_create: too many slice widths in a colour"); return UFE_BAD_MESH; }
+        m.run_s0[g][m.n_runs[g]] = s;
+        m.run_w[g][m.n_runs[g]] = w;
+        m.run_e0[g][m.n_runs[g]] = slice_ptr[s];
+        ++m.n_runs[g];
+        prev_w = w;
+      }
+    }
+  }
+  // padding entries (beyond a row's degree inside its slice) hold -1
+  std::vector<int> col(nE, -1);
   std::vector<double2> cuv(nE, make_double2(0, 0)), nxy(nE, make_double2(0, 0));
   std::vector<float2> cuv32(nE, make_float2(0, 0)), nxy32(nE, make_float2(0, 0));
   std::vector<double2> h_nxy(m.nP, make_double2(0, 0)), h_cuv(m.nP, make_double2(0, 0));

@@ -85,6 +85,10 @@ struct SsaArgs {
   int edge_first;
   int nP;
   int ncm;
+  int n_runs[kGroups];
+  int run_s0[kGroups][kMaxRuns];
+  int run_w[kGroups][kMaxRuns];
+  long long run_e0[kGroups][kMaxRuns];
   // fields in device row order
   const double *Hi, *Hb, *SL, *hx, *hy, *Af, *beta, *tau;
   const uint8_t *skip;    // Dirichlet rows (grounding-line Ac rows under the GL-flux option), may be null
@@ -370,8 +374,21 @@ __device__ unsigned long long phase_sweep_exact(const SsaArgs &a, int g) {
   return mx;
 }
 
+// First SELL entry of slice s of group g and the slice width, from the run table in the
+// kernel parameters (no memory access on the critical path).
+__device__ __forceinline__ int64_t slice_entry(const SsaArgs &a, int g, int s, int &w) {
+  int r = 0;
+  while (r + 1 < a.n_runs[g] && a.run_s0[g][r + 1] <= s) ++r;
+  w = a.run_w[g][r];
+  return a.run_e0[g][r] + (int64_t)(s - a.run_s0[g][r]) * w * kSlice;
+}
+
+constexpr int kBatch = 8;   // neighbour entries loaded in one batch (rows of higher degree load the rest)
+
 // One colour of the fast FP64 sweep: res = U + ((sum + 3 sNxy V) - RHS) / eu with the
 // reciprocal of eu formed once per Picard iteration, products accumulated with FMA.
+// Per row two dependent L2 round trips: (indices, coefficients, home values), then the
+// neighbour gathers. Padding entries hold column -1.
 __device__ unsigned long long phase_sweep_fast(const SsaArgs &a, int g) {
   const int warps_per_block = blockDim.x >> 5;
   const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
@@ -381,40 +398,35 @@ __device__ unsigned long long phase_sweep_fast(const SsaArgs &a, int g) {
   const double omega = a.omega;
   unsigned long long mx = 0ull;
   for (int s = s0 + gw; s < s1; s += nw) {
+    int w;
+    const int64_t e0 = slice_entry(a, g, s, w) + lane;
     const int p = s * kSlice + lane;
-    const int n = a.deg[p];
-    if (n == 0) continue;
-    if (a.skip && a.skip[p]) continue;
-    const int64_t e0 = a.slice_ptr[s] + lane;
-    double su = 0.0, sv = 0.0;
-    int k = 0;
-    for (; k + 4 <= n; k += 4) {
-      int j[4];
-      double2 c[4], u[4];
+    int j[kBatch];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) j[q] = a.col[e0 + (int64_t)(k + q) * kSlice];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) c[q] = a.cuv[e0 + (int64_t)(k + q) * kSlice];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) u[q] = a.UV[j[q]];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        su = fma(u[q].x, c[q].x, su);
-        sv = fma(u[q].y, c[q].y, sv);
-      }
-    }
-    for (; k < n; ++k) {
-      const int64_t e = e0 + (int64_t)k * kSlice;
-      const int j = a.col[e];
-      const double2 c = a.cuv[e];
-      const double2 u = a.UV[j];
-      su = fma(u.x, c.x, su);
-      sv = fma(u.y, c.y, sv);
-    }
+    for (int q = 0; q < kBatch; ++q) j[q] = q < w ? a.col[e0 + (int64_t)q * kSlice] : -1;
     const double2 ui = a.UV[p];
     const double s3 = a.s3Nxy[p];
     const double2 r = a.rcp[p];
     const double2 b = a.rhs[p];
+    if (j[0] < 0 || (a.skip && a.skip[p])) continue;   // padding row, or a Dirichlet row
+    double su = 0.0, sv = 0.0;
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q) {
+      if (j[q] >= 0) {
+        const double2 c = a.cuv[e0 + (int64_t)q * kSlice];
+        const double2 u = a.UV[j[q]];
+        su = fma(u.x, c.x, su);
+        sv = fma(u.y, c.y, sv);
+      }
+    }
+    for (int k = kBatch; k < w; ++k) {
+      const int jj = a.col[e0 + (int64_t)k * kSlice];
+      if (jj < 0) break;
+      const double2 c = a.cuv[e0 + (int64_t)k * kSlice];
+      const double2 u = a.UV[jj];
+      su = fma(u.x, c.x, su);
+      sv = fma(u.y, c.y, sv);
+    }
     const double ru = fma(fma(s3, ui.y, su) - b.x, r.x, ui.x);
     const double rv = fma(fma(s3, ui.x, sv) - b.y, r.y, ui.y);
     const unsigned long long bu = abs_bits(ru), bv = abs_bits(rv);
@@ -436,40 +448,41 @@ __device__ unsigned long long phase_sweep32(const SsaArgs &a, int g) {
   const float omega = (float)a.omega;
   float mx = 0.0f;
   for (int s = s0 + gw; s < s1; s += nw) {
+    int w;
+    const int64_t e0 = slice_entry(a, g, s, w) + lane;
     const int p = s * kSlice + lane;
-    const int n = a.deg[p];
-    if (n == 0) continue;
-    if (a.skip && a.skip[p]) continue;
-    const int64_t e0 = a.slice_ptr[s] + lane;
-    float su = 0.0f, sv = 0.0f;
-    int k = 0;
-    for (; k + 4 <= n; k += 4) {
-      int j[4];
-      float2 c[4], u[4];
+    int j[kBatch];
+    float2 c[kBatch];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) j[q] = a.col[e0 + (int64_t)(k + q) * kSlice];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) c[q] = a.cuv32[e0 + (int64_t)(k + q) * kSlice];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) u[q] = a.dUV[j[q]];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        su = fmaf(u[q].x, c[q].x, su);
-        sv = fmaf(u[q].y, c[q].y, sv);
-      }
-    }
-    for (; k < n; ++k) {
-      const int64_t e = e0 + (int64_t)k * kSlice;
-      const int j = a.col[e];
-      const float2 c = a.cuv32[e];
-      const float2 u = a.dUV[j];
-      su = fmaf(u.x, c.x, su);
-      sv = fmaf(u.y, c.y, sv);
+    for (int q = 0; q < kBatch; ++q) {
+      j[q] = q < w ? a.col[e0 + (int64_t)q * kSlice] : -1;
+      c[q] = q < w ? a.cuv32[e0 + (int64_t)q * kSlice] : make_float2(0.f, 0.f);
     }
     const float2 di = a.dUV[p];
     const float s3 = a.s3Nxy32[p];
     const float2 r = a.rcp32[p];
     const float2 d = a.r0[p];
+    if (j[0] < 0 || (a.skip && a.skip[p])) continue;   // padding row, or a Dirichlet row
+    float2 u[kBatch];
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q)
+      if (j[q] >= 0) u[q] = a.dUV[j[q]];
+    float su = 0.0f, sv = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q) {
+      if (j[q] >= 0) {
+        su = fmaf(u[q].x, c[q].x, su);
+        sv = fmaf(u[q].y, c[q].y, sv);
+      }
+    }
+    for (int k = kBatch; k < w; ++k) {
+      const int jj = a.col[e0 + (int64_t)k * kSlice];
+      if (jj < 0) break;
+      const float2 cc = a.cuv32[e0 + (int64_t)k * kSlice];
+      const float2 v = a.dUV[jj];
+      su = fmaf(v.x, cc.x, su);
+      sv = fmaf(v.y, cc.y, sv);
+    }
     const float ru = fmaf(fmaf(s3, di.y, su) - d.x, r.x, di.x);
     const float rv = fmaf(fmaf(s3, di.x, sv) - d.y, r.y, di.y);
     mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
@@ -1052,6 +1065,14 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     a.s3Nxy = m.s3Nxy; a.h_nxy32 = m.h_nxy32; a.s3Nxy32 = m.s3Nxy32; a.bnd_ptr = m.bnd_ptr; a.bnd_nbr = m.bnd_nbr;
     for (int g = 0; g <= kGroups; ++g) a.grp_off[g] = m.grp_off[g];
     a.n_edge = m.n_edge; a.edge_first = m.edge_first; a.nP = m.nP; a.ncm = m.ncm;
+    for (int g = 0; g < kGroups; ++g) {
+      a.n_runs[g] = m.n_runs[g];
+      for (int r = 0; r < kMaxRuns; ++r) {
+        a.run_s0[g][r] = m.run_s0[g][r];
+        a.run_w[g][r] = m.run_w[g][r];
+        a.run_e0[g][r] = m.run_e0[g][r];
+      }
+    }
     a.Hi = fl.Hi; a.Hb = fl.Hb; a.SL = fl.SL; a.hx = fl.hx; a.hy = fl.hy; a.Af = fl.Af;
     a.beta = fl.beta; a.tau = fl.tau;
     a.skip = w->gl ? w->skip : nullptr;
