@@ -17,7 +17,8 @@ namespace ufe {
 constexpr int kMaxDeg = 32;    // neighbours per AaAc row the kernels accept (nconmax <= 31)
 constexpr int kSlice = 32;     // rows per SELL slice (one warp, one row per lane)
 constexpr int kGroups = 6;     // colours 1..5 (rows swept by SOR), then the edge rows
-constexpr int kMaxRuns = 24;   // distinct slice widths per group (degrees are <= nconmax)
+constexpr int kMaxPatchSlices = 1024;  // slices of 32 rows per patch (one patch per SM)
+constexpr int kMaxSync = 64;   // patches one patch may synchronise with
 
 // Physical constants, parameters_module.f90:9-21.
 constexpr double kIceDensity = 910.0;
@@ -35,38 +36,38 @@ int aaac_build(const ufe_base_mesh *b, ufe_aaac_mesh *o, std::string *msg);
 
 // Device re-layout of the combined AaAc mesh.
 //
-// Rows are permuted into groups: the non-edge rows of colour 1, ..., colour 5 (the rows
-// the SOR sweep updates, each colour an independent set), then all edge rows (updated by
-// the Neumann boundary condition) with the four corners last. Inside a colour the rows
-// are sorted by degree (descending, stable in the reference's row order) so that the
-// sliced-ELL slices of 32 rows are nearly uniform. Every group starts on a multiple of 32;
-// the gaps are padding rows (degree 0) that kernels skip.
+// Rows are cut into spatially compact patches (Morton order of the row coordinates), one
+// per CTA of the persistent solver. Inside a patch they are permuted into groups: the
+// non-edge rows of colour 1, ..., colour 5 (the rows the SOR sweep updates, each colour an
+// independent set), then the patch's edge rows (updated by the Neumann boundary condition)
+// with corners last. Inside a colour the rows are sorted by degree (descending, stable in
+// Morton order) so that the sliced-ELL slices of 32 rows are nearly uniform. Every group
+// starts on a multiple of 32; the gaps are padding rows (degree 0) that kernels skip.
 struct DevMesh {
   int nV = 0, nAc = 0, nA = 0, ncm = 0;
   int nP = 0;                   // padded device rows
   int nSlices = 0;
-  int grp_off[kGroups + 1] = {};  // device row offsets of the groups (multiples of 32)
-  int grp_rows[kGroups] = {};   // real rows per group
-  // Runs of equal slice width inside each group (rows are sorted by degree, so widths only
-  // fall): run r of group g covers slices [run_s0, next run's run_s0) of width run_w, whose
-  // first SELL entry is run_e0. Kernels compute a slice's entry offset from this table
-  // instead of loading it.
-  int n_runs[kGroups] = {};
-  int run_s0[kGroups][kMaxRuns] = {};
-  int run_w[kGroups][kMaxRuns] = {};
-  int64_t run_e0[kGroups][kMaxRuns] = {};
-  int n_edge = 0;               // edge rows excluding the corners
-  int n_corner = 0;             // 4
-  int edge_first = 0;           // device row of the first edge row (== grp_off[5])
+  int n_patch = 0;              // spatial patches = CTAs of the persistent SSA solver
+  int max_patch_slices = 0;
+  int max_sync = 0;
+  int n_edge_total = 0;         // edge rows including the four corners
+  int bnd_total = 0;            // entries of bnd_nbr
   int64_t nE = 0;               // padded SELL entries
 
-  // Host copies kept for scatter bookkeeping.
   // Device arrays:
   int *orig_of_dev = nullptr;   // [nP] original 0-based AaAc row, -1 = padding
   int *dev_of_orig = nullptr;   // [nA]
   uint8_t *deg = nullptr;       // [nP]
   int64_t *slice_ptr = nullptr; // [nSlices] first SELL entry of the slice
-  int *col = nullptr;           // [nE] neighbour device row
+  int *slice_e0 = nullptr;      // [nSlices] the same as int32
+  uint8_t *slice_w = nullptr;   // [nSlices] slice width (entries per row)
+  uint8_t *slice_g = nullptr;   // [nSlices] group: colour 0..4, 5 = edge rows
+  int *patch_slice = nullptr;   // [n_patch][kGroups + 1] first slice of each group of a patch
+  int *patch_edge0 = nullptr;   // [n_patch + 1] first edge ordinal of a patch
+  int *edge_row = nullptr;      // [n_edge_total] device row of each edge ordinal
+  int *sync_ptr = nullptr;      // [n_patch + 1] CSR of the patches each patch synchronises with
+  int *sync_list = nullptr;
+  int *col = nullptr;           // [nE] neighbour device row, -1 = padding
   double2 *cuv = nullptr;       // [nE] (4Nxx+Nyy, 4Nyy+Nxx)
   double2 *nxy = nullptr;       // [nE] (Nx, Ny)
   float2 *cuv32 = nullptr;      // [nE]
@@ -77,9 +78,10 @@ struct DevMesh {
   double *s3Nxy = nullptr;      // [nP] 3 * sNxy (cross-term coefficient of the fast sweeps)
   float2 *h_nxy32 = nullptr;    // [nP] (Nx, Ny) row sums (home + neighbours), for the mixed viscosity
   float *s3Nxy32 = nullptr;     // [nP] 3 * sNxy in FP32
-  // Neumann boundary: edge rows' non-edge neighbours, corners' neighbours.
-  int *bnd_ptr = nullptr;       // [n_edge + n_corner + 1]
-  int *bnd_nbr = nullptr;       // device rows; for corners an edge neighbour is -(k+1), k = edge list index
+  // Neumann boundary lists by edge ordinal: edge rows' non-edge neighbours; corners' neighbours
+  // with an edge neighbour k encoded as -(k+1).
+  int *bnd_ptr = nullptr;       // [n_edge_total + 1]
+  int *bnd_nbr = nullptr;
   // Geometry for the po rotation and the GL flux.
   double2 *V = nullptr;         // [nV] vertex x,y
   int2 *Aci12 = nullptr;        // [nAc] (vi, vj) 0-based

@@ -31,7 +31,8 @@ int upload(T **p, const std::vector<T> &h, cudaStream_t s, const char *what) {
 void free_mesh(DevMesh &m) {
   void *ptrs[] = {m.orig_of_dev, m.dev_of_orig, m.deg, m.slice_ptr, m.col, m.cuv, m.nxy,
                   m.cuv32, m.nxy32, m.h_nxy, m.h_cuv, m.sNxy, m.s3Nxy, m.h_nxy32, m.s3Nxy32, m.bnd_ptr,
-                  m.bnd_nbr, m.V, m.Aci12, m.iAci, m.nC};
+                  m.bnd_nbr, m.V, m.Aci12, m.iAci, m.nC, m.patch_slice, m.patch_edge0, m.edge_row,
+                  m.sync_ptr, m.sync_list, m.slice_e0, m.slice_w, m.slice_g};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   m = DevMesh();
@@ -71,9 +72,8 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   for (int k = 0; k < 4; ++k)
     if (!is_edge(k)) { set_error("ufe_mesh_create: vertices 1..4 must be the domain corners"); return UFE_BAD_MESH; }
 
-  // Colour groups in colour_vi order (ascending row within a colour), edge rows removed.
+  // Colours (colour_vi lists), validated as a partition of the rows.
   std::vector<int> colour_of(nA, -1);
-  std::vector<std::vector<int>> groups(kGroups);
   int64_t total = 0;
   for (int c = 0; c < 5; ++c) {
     const int n_c = d->colour_nV[c];
@@ -83,7 +83,6 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
       const int r = d->colour_vi[k + (int64_t)c * nA] - 1;
       if (r < 0 || r >= nA || colour_of[r] >= 0) { set_error("ufe_mesh_create: colour_vi is not a partition"); return UFE_BAD_MESH; }
       colour_of[r] = c;
-      if (!is_edge(r)) groups[c].push_back(r);
     }
   }
   if (total != nA) { set_error("ufe_mesh_create: colour_nV does not sum to nVAaAc"); return UFE_BAD_MESH; }
@@ -92,39 +91,115 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   for (int r = 0; r < nA; ++r)
     for (int c = 0; c < d->nCAaAc[r]; ++c)
       if (colour_of[CA(r, c)] == colour_of[r]) { set_error("ufe_mesh_create: two adjacent rows share a colour"); return UFE_BAD_MESH; }
-  for (int c = 0; c < 5; ++c)
-    std::stable_sort(groups[c].begin(), groups[c].end(),
-                     [&](int a, int b) { return d->nCAaAc[a] > d->nCAaAc[b]; });
-  for (int r = 4; r < nA; ++r)
-    if (is_edge(r)) groups[5].push_back(r);
-  const int n_edge = (int)groups[5].size();
-  for (int r = 0; r < 4; ++r) groups[5].push_back(r);
+  std::vector<int> edge_ord_of(nA, -1);   // filled below
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < d->nCAaAc[r]; ++c)
+      if (CA(r, c) < 4) { set_error("ufe_mesh_create: corner connected to corner"); return UFE_BAD_MESH; }
+
+  int dev = 0, num_sms = 0;
+  int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+  if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  if (rc || num_sms < 1) return UFE_NO_DEVICE;
+
+  // ---- spatial patches: one per CTA of the persistent solver ------------------------------
+  // Rows in Morton order of their coordinates (Aa vertex, or the midpoint of the Ac edge),
+  // cut into equal-count patches. Within a patch: the non-edge rows of colour 1..5, each
+  // sorted by degree (stable in Morton order), then the patch's edge rows with corners last.
+  // Every (patch, group) starts on a multiple of 32 rows.
+  std::vector<double> xr(nA), yr(nA);
+  double xmin = 1e300, xmax = -1e300, ymin = 1e300, ymax = -1e300;
+  for (int v = 0; v < nV; ++v) {
+    xmin = std::min(xmin, d->V[v]); xmax = std::max(xmax, d->V[v]);
+    ymin = std::min(ymin, d->V[v + (int64_t)nV]); ymax = std::max(ymax, d->V[v + (int64_t)nV]);
+  }
+  for (int r = 0; r < nA; ++r) {
+    if (r < nV) { xr[r] = d->V[r]; yr[r] = d->V[r + (int64_t)nV]; continue; }
+    const int a = r - nV;
+    const int vi = d->Aci[a] - 1, vj = d->Aci[a + (int64_t)nAc] - 1;
+    if (vi < 0 || vi >= nV || vj < 0 || vj >= nV) { set_error("ufe_mesh_create: Aci out of range"); return UFE_BAD_MESH; }
+    xr[r] = 0.5 * (d->V[vi] + d->V[vj]);
+    yr[r] = 0.5 * (d->V[vi + (int64_t)nV] + d->V[vj + (int64_t)nV]);
+  }
+  auto morton = [&](int r) {
+    const double sx = xmax > xmin ? (xr[r] - xmin) / (xmax - xmin) : 0.0;
+    const double sy = ymax > ymin ? (yr[r] - ymin) / (ymax - ymin) : 0.0;
+    uint64_t ix = (uint64_t)std::min(65535.0, std::max(0.0, sx * 65536.0));
+    uint64_t iy = (uint64_t)std::min(65535.0, std::max(0.0, sy * 65536.0));
+    uint64_t k = 0;
+    for (int b = 0; b < 16; ++b) k |= ((ix >> b) & 1u) << (2 * b) | ((iy >> b) & 1u) << (2 * b + 1);
+    return k;
+  };
+  std::vector<uint64_t> key(nA);
+  for (int r = 0; r < nA; ++r) key[r] = morton(r);
+  std::vector<int> order(nA);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+  const int n_patch = std::max(1, std::min(num_sms, nA / 1024));
+  std::vector<int> patch_of(nA);
+  std::vector<std::vector<std::vector<int>>> plist(n_patch, std::vector<std::vector<int>>(kGroups));
+  for (int k = 0; k < nA; ++k) {
+    const int r = order[k];
+    const int b = (int)((int64_t)k * n_patch / nA);
+    patch_of[r] = b;
+    if (r < 4) continue;   // corners go last in their patch's edge group
+    plist[b][is_edge(r) ? 5 : colour_of[r]].push_back(r);
+  }
+  for (int r = 0; r < 4; ++r) plist[patch_of[r]][5].push_back(r);
+  for (int b = 0; b < n_patch; ++b)
+    for (int g = 0; g < 5; ++g)
+      std::stable_sort(plist[b][g].begin(), plist[b][g].end(),
+                       [&](int x, int y) { return d->nCAaAc[x] > d->nCAaAc[y]; });
 
   // ---- device row numbering -------------------------------------------------------------
   DevMesh m;
-  m.nV = nV; m.nAc = nAc; m.nA = nA; m.ncm = ncm;
+  m.nV = nV; m.nAc = nAc; m.nA = nA; m.ncm = ncm; m.n_patch = n_patch;
+  std::vector<int> patch_slice((size_t)n_patch * (kGroups + 1));
+  std::vector<int> edge_row, patch_edge0(n_patch + 1, 0);
   int off = 0;
-  for (int g = 0; g < kGroups; ++g) {
-    m.grp_off[g] = off;
-    m.grp_rows[g] = (int)groups[g].size();
-    off += ((int)groups[g].size() + kSlice - 1) / kSlice * kSlice;
+  for (int b = 0; b < n_patch; ++b) {
+    for (int g = 0; g < kGroups; ++g) {
+      patch_slice[(size_t)b * (kGroups + 1) + g] = off / kSlice;
+      off += ((int)plist[b][g].size() + kSlice - 1) / kSlice * kSlice;
+    }
+    patch_slice[(size_t)b * (kGroups + 1) + kGroups] = off / kSlice;
   }
-  m.grp_off[kGroups] = off;
   m.nP = off;
   m.nSlices = off / kSlice;
-  m.n_edge = n_edge;
-  m.n_corner = 4;
-  m.edge_first = m.grp_off[5];
   std::vector<int> orig_of_dev(m.nP, -1), dev_of_orig(nA, -1);
-  for (int g = 0; g < kGroups; ++g)
-    for (size_t k = 0; k < groups[g].size(); ++k) {
-      orig_of_dev[m.grp_off[g] + k] = groups[g][k];
-      dev_of_orig[groups[g][k]] = m.grp_off[g] + (int)k;
+  std::vector<uint8_t> slice_g(m.nSlices, 255);
+  int max_patch_slices = 0;
+  for (int b = 0; b < n_patch; ++b) {
+    for (int g = 0; g < kGroups; ++g) {
+      const int p0 = patch_slice[(size_t)b * (kGroups + 1) + g] * kSlice;
+      for (size_t k = 0; k < plist[b][g].size(); ++k) {
+        orig_of_dev[p0 + k] = plist[b][g][k];
+        dev_of_orig[plist[b][g][k]] = p0 + (int)k;
+      }
+      for (int s = patch_slice[(size_t)b * (kGroups + 1) + g]; s < patch_slice[(size_t)b * (kGroups + 1) + g + 1]; ++s)
+        slice_g[s] = (uint8_t)g;
+      if (g == 5) {
+        patch_edge0[b] = (int)edge_row.size();
+        for (size_t k = 0; k < plist[b][5].size(); ++k) {
+          edge_ord_of[plist[b][5][k]] = (int)edge_row.size();
+          edge_row.push_back(p0 + (int)k);
+        }
+        patch_edge0[b + 1] = (int)edge_row.size();
+      }
     }
+    max_patch_slices = std::max(max_patch_slices, patch_slice[(size_t)b * (kGroups + 1) + kGroups] -
+                                                      patch_slice[(size_t)b * (kGroups + 1)]);
+  }
+  m.max_patch_slices = max_patch_slices;
+  m.n_edge_total = (int)edge_row.size();
+  if (max_patch_slices > kMaxPatchSlices) {
+    set_error("ufe_mesh_create: mesh too large for one patch per SM (more than 1024 slices of 32 rows per patch)");
+    return UFE_BAD_ARG;
+  }
 
   // ---- sliced ELL ------------------------------------------------------------------------
   std::vector<uint8_t> deg(m.nP, 0);
   std::vector<int64_t> slice_ptr(m.nSlices);
+  std::vector<uint8_t> slice_w(m.nSlices);
   int64_t nE = 0;
   for (int s = 0; s < m.nSlices; ++s) {
     int w = 0;
@@ -133,24 +208,13 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
       if (r >= 0) w = std::max(w, d->nCAaAc[r]);
     }
     slice_ptr[s] = nE;
+    slice_w[s] = (uint8_t)w;
     nE += (int64_t)w * kSlice;
   }
   m.nE = nE;
-  for (int g = 0; g < kGroups; ++g) {
-    const int sa = m.grp_off[g] / kSlice, sb = m.grp_off[g + 1] / kSlice;
-    int prev_w = -1;
-    for (int s = sa; s < sb; ++s) {
-      const int w = (int)(((s + 1 < m.nSlices ? slice_ptr[s + 1] : nE) - slice_ptr[s]) / kSlice);
-      if (w != prev_w) {
-        if (m.n_runs[g] == kMaxRuns) { set_error("ufe_mesh_create: too many slice widths in a colour"); return UFE_BAD_MESH; }
-        m.run_s0[g][m.n_runs[g]] = s;
-        m.run_w[g][m.n_runs[g]] = w;
-        m.run_e0[g][m.n_runs[g]] = slice_ptr[s];
-        ++m.n_runs[g];
-        prev_w = w;
-      }
-    }
-  }
+  if (nE >= ((int64_t)1 << 31)) { set_error("ufe_mesh_create: more than 2^31 neighbour entries"); return UFE_BAD_ARG; }
+  std::vector<int> slice_e0(m.nSlices);
+  for (int s = 0; s < m.nSlices; ++s) slice_e0[s] = (int)slice_ptr[s];
   // padding entries (beyond a row's degree inside its slice) hold -1
   std::vector<int> col(nE, -1);
   std::vector<double2> cuv(nE, make_double2(0, 0)), nxy(nE, make_double2(0, 0));
@@ -189,27 +253,50 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
     s3Nxy32[p] = (float)(3.0 * sxy);
   }
 
-  // ---- Neumann boundary lists (apply_Neumann_boundary_AaAc) ------------------------------
+  // ---- Neumann boundary lists (apply_Neumann_boundary_AaAc), by edge ordinal ------------
+  // An edge row lists its non-edge neighbours; a corner lists all its neighbours, an edge
+  // neighbour k encoded as -(k + 1) so that the corner recomputes that edge row's new value.
   std::vector<int> bnd_ptr(1, 0), bnd_nbr;
-  std::vector<int> edge_list_index(nA, -1);
-  for (int k = 0; k < n_edge; ++k) edge_list_index[groups[5][k]] = k;
-  for (int k = 0; k < n_edge; ++k) {
-    const int r = groups[5][k];
+  std::vector<std::vector<int>> reads(n_patch);   // patches whose rows each patch reads
+  for (int k = 0; k < m.n_edge_total; ++k) {
+    const int r = orig_of_dev[edge_row[k]];
+    const bool corner = r < 4;
     for (int c = 0; c < d->nCAaAc[r]; ++c) {
       const int j = CA(r, c);
-      if (!is_edge(j)) bnd_nbr.push_back(dev_of_orig[j]);
+      if (!is_edge(j)) {
+        bnd_nbr.push_back(dev_of_orig[j]);
+      } else if (corner) {
+        bnd_nbr.push_back(-(edge_ord_of[j] + 1));
+        for (int c2 = 0; c2 < d->nCAaAc[j]; ++c2)   // second-hop reads of the recompute
+          if (!is_edge(CA(j, c2))) reads[patch_of[r]].push_back(patch_of[CA(j, c2)]);
+      }
     }
     if ((int)bnd_nbr.size() == bnd_ptr.back()) { set_error("ufe_mesh_create: edge row without non-edge neighbour"); return UFE_BAD_MESH; }
     bnd_ptr.push_back((int)bnd_nbr.size());
   }
-  for (int r = 0; r < 4; ++r) {
-    for (int c = 0; c < d->nCAaAc[r]; ++c) {
-      const int j = CA(r, c);
-      if (j < 4) { set_error("ufe_mesh_create: corner connected to corner"); return UFE_BAD_MESH; }
-      bnd_nbr.push_back(is_edge(j) ? -(edge_list_index[j] + 1) : dev_of_orig[j]);
-    }
-    bnd_ptr.push_back((int)bnd_nbr.size());
+  m.bnd_total = (int)bnd_nbr.size();
+
+  // ---- neighbour-patch synchronisation sets ------------------------------------------------
+  // Patch b must not start a colour phase before every patch it reads from has finished the
+  // previous phase, nor before every patch that reads from b has: the set is the symmetric
+  // closure of the read relation (direct neighbours, plus the corners' second hop).
+  for (int r = 0; r < nA; ++r)
+    for (int c = 0; c < d->nCAaAc[r]; ++c) reads[patch_of[r]].push_back(patch_of[CA(r, c)]);
+  std::vector<std::vector<int>> sync(n_patch);
+  for (int b = 0; b < n_patch; ++b)
+    for (int q : reads[b])
+      if (q != b) { sync[b].push_back(q); sync[q].push_back(b); }
+  std::vector<int> sync_ptr(1, 0), sync_list;
+  int max_sync = 0;
+  for (int b = 0; b < n_patch; ++b) {
+    std::sort(sync[b].begin(), sync[b].end());
+    sync[b].erase(std::unique(sync[b].begin(), sync[b].end()), sync[b].end());
+    max_sync = std::max(max_sync, (int)sync[b].size());
+    sync_list.insert(sync_list.end(), sync[b].begin(), sync[b].end());
+    sync_ptr.push_back((int)sync_list.size());
   }
+  m.max_sync = max_sync;
+  if (max_sync > kMaxSync) { set_error("ufe_mesh_create: a patch touches too many other patches"); return UFE_BAD_MESH; }
 
   // ---- geometry ---------------------------------------------------------------------------
   std::vector<double2> V(nV);
@@ -234,12 +321,9 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   }
 
   // ---- upload -------------------------------------------------------------------------------
-  int dev = 0;
-  int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
-  if (rc) return UFE_NO_DEVICE;
   ufe_mesh_s *h = new ufe_mesh_s();
   h->device = dev;
-  cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  h->num_sms = num_sms;
   rc = cuda_status(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "cudaStreamCreate");
   auto S = h->stream;
   if (!rc) rc = upload(&m.orig_of_dev, orig_of_dev, S, "orig_of_dev");
@@ -263,6 +347,14 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   if (!rc) rc = upload(&m.Aci12, Aci12, S, "Aci12");
   if (!rc) rc = upload(&m.iAci, iAci, S, "iAci");
   if (!rc) rc = upload(&m.nC, nC, S, "nC");
+  if (!rc) rc = upload(&m.patch_slice, patch_slice, S, "patch_slice");
+  if (!rc) rc = upload(&m.patch_edge0, patch_edge0, S, "patch_edge0");
+  if (!rc) rc = upload(&m.edge_row, edge_row, S, "edge_row");
+  if (!rc) rc = upload(&m.sync_ptr, sync_ptr, S, "sync_ptr");
+  if (!rc) rc = upload(&m.sync_list, sync_list, S, "sync_list");
+  if (!rc) rc = upload(&m.slice_e0, slice_e0, S, "slice_e0");
+  if (!rc) rc = upload(&m.slice_w, slice_w, S, "slice_w");
+  if (!rc) rc = upload(&m.slice_g, slice_g, S, "slice_g");
   if (!rc) rc = cuda_status(cudaStreamSynchronize(S), "mesh upload");
   h->m = m;
   if (rc) {

@@ -80,15 +80,18 @@ struct SsaArgs {
   const float *s3Nxy32;
   const int *bnd_ptr;
   const int *bnd_nbr;
-  int grp_off[kGroups + 1];
-  int n_edge;
-  int edge_first;
+  const int *slice_e0;
+  const uint8_t *slice_w;
+  const uint8_t *slice_g;
+  const int *patch_slice;
+  const int *patch_edge0;
+  const int *edge_row;
+  const int *sync_ptr;
+  const int *sync_list;
+  unsigned int *prog;      // per-CTA progress counters (stride 32 words)
   int nP;
+  int nSlices;
   int ncm;
-  int n_runs[kGroups];
-  int run_s0[kGroups][kMaxRuns];
-  int run_w[kGroups][kMaxRuns];
-  long long run_e0[kGroups][kMaxRuns];
   // fields in device row order
   const double *Hi, *Hb, *SL, *hx, *hy, *Af, *beta, *tau;
   const uint8_t *skip;    // Dirichlet rows (grounding-line Ac rows under the GL-flux option), may be null
@@ -313,7 +316,7 @@ __device__ void phase_coefficients(const SsaArgs &a) {
       S = a.has_beta ? a.beta[p] : a.beta_const;
     }
     a.S[p] = S;
-    if (p >= a.edge_first) continue;   // edge rows are set by the boundary condition
+    if (a.slice_g[p / kSlice] == 5) continue;   // edge rows are set by the boundary condition
     const double eta = a.eta[p];
     const double H = a.Hi[p];
     a.rhs[p] = make_double2(((kIceDensity * kGrav) * a.hx[p]) / eta, ((kIceDensity * kGrav) * a.hy[p]) / eta);
@@ -333,21 +336,28 @@ __device__ void phase_coefficients(const SsaArgs &a) {
   }
 }
 
+// This CTA's patch: the first slice of each group, and per slice its first SELL entry and
+// width, staged in shared memory at kernel start.
+struct PatchSmem {
+  int ps[kGroups + 1];
+  int e0[kMaxPatchSlices];
+  unsigned char w[kMaxPatchSlices];
+  int edge0, edge1;
+  int nsync;
+  int sync[kMaxSync];
+};
+
 // One colour of the FP64 sweep in the reference's expression order (parity mode).
-__device__ unsigned long long phase_sweep_exact(const SsaArgs &a, int g) {
-  const int warps_per_block = blockDim.x >> 5;
-  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-  const int nw = gridDim.x * warps_per_block;
-  const int lane = threadIdx.x & 31;
-  const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
+__device__ unsigned long long phase_sweep_exact(const SsaArgs &a, const PatchSmem &ps, int g) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const double omega = a.omega;
   unsigned long long mx = 0ull;
-  for (int s = s0 + gw; s < s1; s += nw) {
+  for (int s = ps.ps[g] + wid; s < ps.ps[g + 1]; s += nwarps) {
     const int p = s * kSlice + lane;
     const int n = a.deg[p];
     if (n == 0) continue;
     if (a.skip && a.skip[p]) continue;
-    const int64_t e0 = a.slice_ptr[s] + lane;
+    const int64_t e0 = ps.e0[s - ps.ps[0]] + lane;
     double su = 0.0, sv = 0.0;
     for (int k = 0; k < n; ++k) {
       const int64_t e = e0 + (int64_t)k * kSlice;
@@ -374,32 +384,19 @@ __device__ unsigned long long phase_sweep_exact(const SsaArgs &a, int g) {
   return mx;
 }
 
-// First SELL entry of slice s of group g and the slice width, from the run table in the
-// kernel parameters (no memory access on the critical path).
-__device__ __forceinline__ int64_t slice_entry(const SsaArgs &a, int g, int s, int &w) {
-  int r = 0;
-  while (r + 1 < a.n_runs[g] && a.run_s0[g][r + 1] <= s) ++r;
-  w = a.run_w[g][r];
-  return a.run_e0[g][r] + (int64_t)(s - a.run_s0[g][r]) * w * kSlice;
-}
-
 constexpr int kBatch = 8;   // neighbour entries loaded in one batch (rows of higher degree load the rest)
 
 // One colour of the fast FP64 sweep: res = U + ((sum + 3 sNxy V) - RHS) / eu with the
 // reciprocal of eu formed once per Picard iteration, products accumulated with FMA.
 // Per row two dependent L2 round trips: (indices, coefficients, home values), then the
 // neighbour gathers. Padding entries hold column -1.
-__device__ unsigned long long phase_sweep_fast(const SsaArgs &a, int g) {
-  const int warps_per_block = blockDim.x >> 5;
-  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-  const int nw = gridDim.x * warps_per_block;
-  const int lane = threadIdx.x & 31;
-  const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
+__device__ unsigned long long phase_sweep_fast(const SsaArgs &a, const PatchSmem &ps, int g) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const double omega = a.omega;
   unsigned long long mx = 0ull;
-  for (int s = s0 + gw; s < s1; s += nw) {
-    int w;
-    const int64_t e0 = slice_entry(a, g, s, w) + lane;
+  for (int s = ps.ps[g] + wid; s < ps.ps[g + 1]; s += nwarps) {
+    const int w = ps.w[s - ps.ps[0]];
+    const int64_t e0 = ps.e0[s - ps.ps[0]] + lane;
     const int p = s * kSlice + lane;
     int j[kBatch];
 #pragma unroll
@@ -439,17 +436,13 @@ __device__ unsigned long long phase_sweep_fast(const SsaArgs &a, int g) {
 
 // One colour of the FP32 correction sweep of the mixed path:
 // res = d_i + ((sum_j c_j d_j + 3 sNxy d_i') - r0) / eu.
-__device__ unsigned long long phase_sweep32(const SsaArgs &a, int g) {
-  const int warps_per_block = blockDim.x >> 5;
-  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-  const int nw = gridDim.x * warps_per_block;
-  const int lane = threadIdx.x & 31;
-  const int s0 = a.grp_off[g] / kSlice, s1 = a.grp_off[g + 1] / kSlice;
+__device__ unsigned long long phase_sweep32(const SsaArgs &a, const PatchSmem &ps, int g) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const float omega = (float)a.omega;
   float mx = 0.0f;
-  for (int s = s0 + gw; s < s1; s += nw) {
-    int w;
-    const int64_t e0 = slice_entry(a, g, s, w) + lane;
+  for (int s = ps.ps[g] + wid; s < ps.ps[g + 1]; s += nwarps) {
+    const int w = ps.w[s - ps.ps[0]];
+    const int64_t e0 = ps.e0[s - ps.ps[0]] + lane;
     const int p = s * kSlice + lane;
     int j[kBatch];
     float2 c[kBatch];
@@ -517,38 +510,30 @@ __device__ __forceinline__ double2 edge_mean(const SsaArgs &a, int k) {
 }
 
 template <bool kM>
-__device__ void phase_boundary(const SsaArgs &a) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
-  const int nb = a.n_edge + 4;
-  for (int k = tid; k < nb; k += nt) {
-    const int p = a.edge_first + k;
-    double2 v;
-    if (k < a.n_edge) {
-      v = edge_mean<kM>(a, k);
-    } else {
-      const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
-      double sx = 0.0, sy = 0.0;
-      for (int q = b0; q < b1; ++q) {
-        const int j = a.bnd_nbr[q];
-        double2 u;
-        if (j < 0) {
-          u = edge_mean<kM>(a, -j - 1);
-        } else {
-          u = a.UV[j];
-          if (kM) {
-            const float2 d = a.dUV[j];
-            u.x = u.x + (double)d.x;
-            u.y = u.y + (double)d.y;
-          }
+__device__ void phase_boundary(const SsaArgs &a, const PatchSmem &ps) {
+  for (int k = ps.edge0 + threadIdx.x; k < ps.edge1; k += blockDim.x) {
+    const int p = a.edge_row[k];
+    const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
+    double sx = 0.0, sy = 0.0;
+    for (int q = b0; q < b1; ++q) {
+      const int j = a.bnd_nbr[q];
+      double2 u;
+      if (j < 0) {
+        u = edge_mean<kM>(a, -j - 1);   // a corner's edge neighbour, recomputed
+      } else {
+        u = a.UV[j];
+        if (kM) {
+          const float2 d = a.dUV[j];
+          u.x = u.x + (double)d.x;
+          u.y = u.y + (double)d.y;
         }
-        sx = sx + u.x;
-        sy = sy + u.y;
       }
-      const int nvals = b1 - b0;
-      if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
-      v = make_double2(sx / (double)nvals, sy / (double)nvals);
+      sx = sx + u.x;
+      sy = sy + u.y;
     }
+    const int nvals = b1 - b0;
+    if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
+    const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
     if (!kM) {
       a.UV[p] = v;
     } else {
@@ -580,8 +565,8 @@ __device__ void phase_defect(const SsaArgs &a) {
   const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
   const int nw = gridDim.x * warps_per_block;
   const int lane = threadIdx.x & 31;
-  const int s1 = a.edge_first / kSlice;
-  for (int s = gw; s < s1; s += nw) {
+  for (int s = gw; s < a.nSlices; s += nw) {
+    if (a.slice_g[s] == 5) continue;
     const int p = s * kSlice + lane;
     const int n = a.deg[p];
     if (n == 0) continue;
@@ -619,33 +604,92 @@ __device__ void phase_zero_velocity(const SsaArgs &a, bool mixed) {
 // ---------------------------------------------------------------------------------------
 constexpr int kSsaBlock = 1024;
 
+// Progress of this CTA's patch: the number of colour phases it has completed in this launch.
+__device__ __forceinline__ void publish_progress(const SsaArgs &a, unsigned int value) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.prog + 32 * blockIdx.x), "r"(value) : "memory");
+  }
+}
+
+// Wait until every patch this patch synchronises with has completed `target` colour phases.
+// Bounded: after timeout_ns the CTA records UFE_TIMEOUT (the next grid barrier then fails).
+__device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSmem &ps, unsigned int target) {
+  if (threadIdx.x < ps.nsync) {
+    const unsigned int *q = a.prog + 32 * ps.sync[threadIdx.x];
+    unsigned int v = ld_acquire_u32(q);
+    if ((int)(v - target) < 0) {
+      const unsigned long long t0 = globaltimer_ns();
+      unsigned int ns = 16;
+      for (;;) {
+        __nanosleep(ns);
+        if (ns < 64) ns <<= 1;
+        v = ld_acquire_u32(q);
+        if ((int)(v - target) >= 0) break;
+        if ((long long)(globaltimer_ns() - t0) > a.timeout_ns) {
+          atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
+          atomicOr(&a.ctl->bar_count, kBarrierError);
+          break;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <int kMode>
 __global__ void __launch_bounds__(kSsaBlock, 1) ssa_persistent(SsaArgs a) {
   constexpr bool kM = kMode == kMixed;
   SsaCtl *ctl = a.ctl;
   unsigned int epoch = 0;
+  unsigned int phases = 0;   // colour phases completed by this patch in this launch
   const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  __shared__ PatchSmem ps;
+  {
+    const int b = blockIdx.x;
+    if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
+    if (threadIdx.x == 0) {
+      ps.edge0 = a.patch_edge0[b];
+      ps.edge1 = a.patch_edge0[b + 1];
+      ps.nsync = a.sync_ptr[b + 1] - a.sync_ptr[b];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < ps.nsync; i += blockDim.x) ps.sync[i] = a.sync_list[a.sync_ptr[b] + i];
+    for (int s = ps.ps[0] + threadIdx.x; s < ps.ps[kGroups]; s += blockDim.x) {
+      ps.e0[s - ps.ps[0]] = a.slice_e0[s];
+      ps.w[s - ps.ps[0]] = a.slice_w[s];
+    }
+    __syncthreads();
+  }
   double *N = a.Na, *Nprev = a.Nb;
   int did_reset_before = 0;
   int it = 0;
   bool picard_done = false;
+#define UFE_GRID_SYNC()                                   \
+  if (!grid_barrier(ctl, epoch, a.timeout_ns)) {          \
+    if (threadIdx.x == 0) a.prog[32 * blockIdx.x] = 0x7fffffffu; \
+    return;                                               \
+  }
   while (!picard_done && it < a.max_outer) {
     ++it;
     // N_prev <- N, then the new viscosity into N
     { double *t = N; N = Nprev; Nprev = t; }
     phase_viscosity(a, N, Nprev, kM && a.fp32_visc);
-    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    UFE_GRID_SYNC();
     const double RN = final_rn(a);
     if (leader) { ctl->picard_iterations = it; ctl->last_RN = RN; }
     if (RN < a.rn_tol) { picard_done = true; break; }
     phase_coefficients<kMode>(a);
     if (leader) { ctl->maxres[0] = 0ull; ctl->maxres[1] = 0ull; ctl->maxres[2] = 0ull; }
-    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    UFE_GRID_SYNC();
     if (kM) {
       phase_defect(a);
-      if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+      UFE_GRID_SYNC();
     }
-    // coloured SOR
+    // Coloured SOR. Colour phases synchronise only with the neighbouring patches; the
+    // boundary phase ends with a grid barrier, after which the sweep's maximum residual is
+    // known to every CTA.
     int sweeps = 0;
     bool lin_done = false;
     int did_reset = 0;
@@ -656,36 +700,39 @@ __global__ void __launch_bounds__(kSsaBlock, 1) ssa_persistent(SsaArgs a) {
       if (leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
       unsigned long long mx = 0ull;
       for (int g = 0; g < 5; ++g) {
+        if (g > 0) wait_neighbours(a, ps, phases);
         unsigned long long m;
-        if (kMode == kExact64) m = phase_sweep_exact(a, g);
-        else if (kMode == kFast64) m = phase_sweep_fast(a, g);
-        else m = phase_sweep32(a, g);
+        if (kMode == kExact64) m = phase_sweep_exact(a, ps, g);
+        else if (kMode == kFast64) m = phase_sweep_fast(a, ps, g);
+        else m = phase_sweep32(a, ps, g);
         mx = m > mx ? m : mx;
-        if (g == 4) block_max_to(&ctl->maxres[slot], mx);
-        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+        ++phases;
+        publish_progress(a, phases);
       }
-      phase_boundary<kM>(a);
-      if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+      block_max_to(&ctl->maxres[slot], mx);
+      wait_neighbours(a, ps, phases);
+      phase_boundary<kM>(a, ps);
+      UFE_GRID_SYNC();
       maxres = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxres[slot]);
       if (maxres < a.tol) {
         lin_done = true;
       } else if (maxres > 1e6) {
         phase_zero_velocity(a, kM);
-        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+        UFE_GRID_SYNC();
         did_reset = 1;
         lin_done = true;
       } else if (sweeps == a.max_inner) {
         if (leader) ctl->not_converged += 1;
       } else if (kM && a.refold > 0 && sweeps % a.refold == 0) {
         phase_fold(a);
-        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+        UFE_GRID_SYNC();
         phase_defect(a);
-        if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+        UFE_GRID_SYNC();
       }
     }
     if (kM && !did_reset) {
       phase_fold(a);
-      if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+      UFE_GRID_SYNC();
     }
     if (leader) {
       if (ctl->linear_solves < 64) ctl->sweeps[ctl->linear_solves] = sweeps;
@@ -706,9 +753,10 @@ __global__ void __launch_bounds__(kSsaBlock, 1) ssa_persistent(SsaArgs a) {
   if (N != a.Na) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     const int nt = gridDim.x * blockDim.x;
-    if (!grid_barrier(ctl, epoch, a.timeout_ns)) return;
+    UFE_GRID_SYNC();
     for (int p = tid; p < a.nP; p += nt) a.Na[p] = N[p];
   }
+#undef UFE_GRID_SYNC
 }
 
 // ---------------------------------------------------------------------------------------
@@ -872,6 +920,7 @@ struct SsaWork {
   float2 *dUV = nullptr, *r0 = nullptr, *rcp32 = nullptr;
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
+  unsigned int *prog = nullptr;
   SsaCtl *ctl = nullptr;
   SsaCtl *ctl_host = nullptr;    // pinned
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -886,7 +935,7 @@ struct SsaWork {
 void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
-                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->ctl};
+                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -934,10 +983,11 @@ int ensure_work(ufe_mesh_h h) {
     int per_sm = 0;
     rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], w->block, 0), "occupancy");
     if (!rc && per_sm < 1) { set_error("ssa kernel does not fit on an SM"); rc = UFE_CUDA_ERROR; }
-    w->grid[k] = h->num_sms;
+    w->grid[k] = m.n_patch;   // one CTA per patch (n_patch <= number of SMs)
     gmax = gmax > w->grid[k] ? gmax : w->grid[k];
   }
   if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)gmax * sizeof(double)), "rn_part");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->prog, 32 * (size_t)gmax * sizeof(unsigned int)), "progress counters");
   if (rc) { ssa_free(w); return rc; }
   h->ssa = w;
   return UFE_OK;
@@ -1063,16 +1113,9 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     a.col = m.col; a.cuv = m.cuv; a.nxy = m.nxy; a.cuv32 = m.cuv32; a.nxy32 = m.nxy32; a.deg = m.deg;
     a.slice_ptr = m.slice_ptr; a.h_nxy = m.h_nxy; a.h_cuv = m.h_cuv; a.sNxy = m.sNxy;
     a.s3Nxy = m.s3Nxy; a.h_nxy32 = m.h_nxy32; a.s3Nxy32 = m.s3Nxy32; a.bnd_ptr = m.bnd_ptr; a.bnd_nbr = m.bnd_nbr;
-    for (int g = 0; g <= kGroups; ++g) a.grp_off[g] = m.grp_off[g];
-    a.n_edge = m.n_edge; a.edge_first = m.edge_first; a.nP = m.nP; a.ncm = m.ncm;
-    for (int g = 0; g < kGroups; ++g) {
-      a.n_runs[g] = m.n_runs[g];
-      for (int r = 0; r < kMaxRuns; ++r) {
-        a.run_s0[g][r] = m.run_s0[g][r];
-        a.run_w[g][r] = m.run_w[g][r];
-        a.run_e0[g][r] = m.run_e0[g][r];
-      }
-    }
+    a.slice_e0 = m.slice_e0; a.slice_w = m.slice_w; a.slice_g = m.slice_g; a.patch_slice = m.patch_slice;
+    a.patch_edge0 = m.patch_edge0; a.edge_row = m.edge_row; a.sync_ptr = m.sync_ptr; a.sync_list = m.sync_list;
+    a.prog = w->prog; a.nP = m.nP; a.nSlices = m.nSlices; a.ncm = m.ncm;
     a.Hi = fl.Hi; a.Hb = fl.Hb; a.SL = fl.SL; a.hx = fl.hx; a.hy = fl.hy; a.Af = fl.Af;
     a.beta = fl.beta; a.tau = fl.tau;
     a.skip = w->gl ? w->skip : nullptr;
@@ -1095,6 +1138,7 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
                      : mode == kFast64 ? (const void *)ssa_persistent<kFast64>
                                        : (const void *)ssa_persistent<kExact64>;
     rc = cuda_status(cudaMemsetAsync(F + F_S * nP, 0, nP * sizeof(double), s), "memset S");
+    if (!rc) rc = cuda_status(cudaMemsetAsync(w->prog, 0, 32 * (size_t)w->grid[mode] * sizeof(unsigned int), s), "memset prog");
     if (!rc)
       rc = cuda_status(cudaLaunchCooperativeKernel(fn, dim3(w->grid[mode]), dim3(w->block), args, 0, s),
                        "ssa_persistent");
