@@ -17,7 +17,18 @@ namespace ufe {
 constexpr int kMaxDeg = 32;    // neighbours per AaAc row the kernels accept (nconmax <= 31)
 constexpr int kSlice = 32;     // rows per SELL slice (one warp, one row per lane)
 constexpr int kGroups = 6;     // colours 1..5 (rows swept by SOR), then the edge rows
-constexpr int kMaxPatchSlices = 1024;  // slices of 32 rows per patch (one patch per SM)
+constexpr int kMaxPatchSlices = 1024;  // slices of 32 rows per patch
+// Persistent SSA solver: CTAs of kSsaBlock threads, kCtasPerSm per SM, one spatial patch per
+// CTA. Measured on the 200k-vertex dome: 1024 x 1 beats 576 x 2, 640 x 2, 384 x 3 and
+// 320 x 4 for the mixed sweep (more CTAs per SM spill at the lower register cap).
+#ifndef UFE_SSA_BLOCK
+#define UFE_SSA_BLOCK 1024
+#endif
+#ifndef UFE_SSA_CTAS_PER_SM
+#define UFE_SSA_CTAS_PER_SM 1
+#endif
+constexpr int kSsaBlock = UFE_SSA_BLOCK;
+constexpr int kCtasPerSm = UFE_SSA_CTAS_PER_SM;
 constexpr int kMaxSync = 64;   // patches one patch may synchronise with
 
 // Physical constants, parameters_module.f90:9-21.

@@ -134,7 +134,7 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   std::vector<int> order(nA);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
-  const int n_patch = std::max(1, std::min(num_sms, nA / 1024));
+  const int n_patch = std::max(1, std::min(kCtasPerSm * num_sms, nA / (kSsaBlock / 2)));
   std::vector<int> patch_of(nA);
   std::vector<std::vector<std::vector<int>>> plist(n_patch, std::vector<std::vector<int>>(kGroups));
   for (int k = 0; k < nA; ++k) {

@@ -602,7 +602,6 @@ __device__ void phase_zero_velocity(const SsaArgs &a, bool mixed) {
 // ---------------------------------------------------------------------------------------
 // The persistent solver
 // ---------------------------------------------------------------------------------------
-constexpr int kSsaBlock = 1024;
 
 // Progress of this CTA's patch: the number of colour phases it has completed in this launch.
 __device__ __forceinline__ void publish_progress(const SsaArgs &a, unsigned int value) {
@@ -639,7 +638,7 @@ __device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSme
 }
 
 template <int kMode>
-__global__ void __launch_bounds__(kSsaBlock, 1) ssa_persistent(SsaArgs a) {
+__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(SsaArgs a) {
   constexpr bool kM = kMode == kMixed;
   SsaCtl *ctl = a.ctl;
   unsigned int epoch = 0;
@@ -982,8 +981,11 @@ int ensure_work(ufe_mesh_h h) {
   for (int k = 0; k < 3 && !rc; ++k) {
     int per_sm = 0;
     rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], w->block, 0), "occupancy");
-    if (!rc && per_sm < 1) { set_error("ssa kernel does not fit on an SM"); rc = UFE_CUDA_ERROR; }
-    w->grid[k] = m.n_patch;   // one CTA per patch (n_patch <= number of SMs)
+    if (!rc && per_sm * h->num_sms < m.n_patch) {
+      set_error("ssa kernel: not enough co-resident CTAs for one per patch");
+      rc = UFE_CUDA_ERROR;
+    }
+    w->grid[k] = m.n_patch;   // one CTA per patch (n_patch <= kCtasPerSm * number of SMs)
     gmax = gmax > w->grid[k] ? gmax : w->grid[k];
   }
   if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)gmax * sizeof(double)), "rn_part");
