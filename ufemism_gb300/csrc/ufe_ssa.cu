@@ -129,30 +129,52 @@ __device__ __forceinline__ void red_release_add_u32(unsigned int *p, unsigned in
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Grid-wide barrier for a cooperative (co-resident) launch: a monotonic arrival counter,
-// epoch k is complete when the counter reaches k * gridDim.x. The spin is bounded: after
+// A team: the CTAs of a cooperative launch that solve one problem together. GridTeam is the
+// whole grid (a single solve: rank and size come from the special registers, the counter
+// from the constant-bank argument block, so the team costs no registers); SubTeam is a
+// slice of the grid solving one ensemble member in the batched solver.
+struct GridTeam {
+  unsigned int *bar_;     // the monotonic barrier counter (bit 30: error)
+  unsigned int epoch;     // barriers passed by this CTA
+  __device__ __forceinline__ int rank() const { return (int)blockIdx.x; }
+  __device__ __forceinline__ int size() const { return (int)gridDim.x; }
+  __device__ __forceinline__ unsigned int *bar() const { return bar_; }
+};
+struct SubTeam {
+  int rank_;              // this CTA's index in the team
+  int size_;              // CTAs in the team
+  unsigned int *bar_;
+  unsigned int epoch;
+  __device__ __forceinline__ int rank() const { return rank_; }
+  __device__ __forceinline__ int size() const { return size_; }
+  __device__ __forceinline__ unsigned int *bar() const { return bar_; }
+};
+
+// Team-wide barrier (every CTA of the team is co-resident): a monotonic arrival counter,
+// epoch k is complete when the counter reaches k * size. The spin is bounded: after
 // timeout_ns the CTA records UFE_TIMEOUT and sets the error bit in the counter, which
 // releases every other waiter with a failure; callers then leave the kernel.
-__device__ __forceinline__ bool grid_barrier(SsaCtl *ctl, unsigned int &epoch, long long timeout_ns) {
+template <class Team>
+__device__ __forceinline__ bool team_barrier(Team &t, int *err, long long timeout_ns) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    epoch += 1u;
-    const unsigned int target = epoch * gridDim.x;
+    t.epoch += 1u;   // only thread 0 arrives and waits
+    const unsigned int target = t.epoch * (unsigned)t.size();
     __threadfence();
-    red_release_add_u32(&ctl->bar_count, 1u);
-    unsigned int v = ld_acquire_u32(&ctl->bar_count);
+    red_release_add_u32(t.bar(), 1u);
+    unsigned int v = ld_acquire_u32(t.bar());
     if (!(v & kBarrierError) && (int)(v - target) < 0) {
       const unsigned long long t0 = globaltimer_ns();
       unsigned int ns = 16;
       for (;;) {
         __nanosleep(ns);
         if (ns < 128) ns <<= 1;
-        v = ld_acquire_u32(&ctl->bar_count);
+        v = ld_acquire_u32(t.bar());
         if ((v & kBarrierError) || (int)((v & ~kBarrierError) - target) >= 0) break;
         if ((long long)(globaltimer_ns() - t0) > timeout_ns) {
-          atomicCAS(&ctl->err, 0, (int)UFE_TIMEOUT);
-          atomicOr(&ctl->bar_count, kBarrierError);
+          atomicCAS(err, 0, (int)UFE_TIMEOUT);
+          atomicOr(t.bar(), kBarrierError);
           v |= kBarrierError;
           break;
         }
@@ -211,10 +233,11 @@ __device__ __forceinline__ bool is_floating(double Hi, double Hb, double SL) {
 // Effective viscosity and N = eta * max(0.1, H) on every row; block partial sums of
 // (N - Nprev)^2 and N^2 for RN. FP64: reference order (home term first). FP32 variant
 // (mixed path option): FP32 arithmetic on FP64 differences u_j - u_i.
-__device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev, bool fp32) {
+template <class Team>
+__device__ void phase_viscosity(const SsaArgs &a, const Team &t, double *N, const double *Nprev, bool fp32) {
   const int warps_per_block = blockDim.x >> 5;
-  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-  const int nw = gridDim.x * warps_per_block;
+  const int gw = t.rank() * warps_per_block + (threadIdx.x >> 5);
+  const int nw = t.size() * warps_per_block;
   const int lane = threadIdx.x & 31;
   const int nslices = a.nP / kSlice;
   double sdn = 0.0, sn = 0.0;
@@ -279,17 +302,18 @@ __device__ void phase_viscosity(const SsaArgs &a, double *N, const double *Nprev
   if (threadIdx.x == 0) {
     double x = 0.0, y = 0.0;
     for (int k = 0; k < warps_per_block; ++k) { x += s_a[k]; y += s_b[k]; }
-    a.rn_part[2 * blockIdx.x] = x;
-    a.rn_part[2 * blockIdx.x + 1] = y;
+    a.rn_part[2 * t.rank()] = x;
+    a.rn_part[2 * t.rank() + 1] = y;
   }
 }
 
 // RN = sqrt(sum (N - Nprev)^2 / sum N^2), reduced in a fixed order by every CTA.
-__device__ double final_rn(const SsaArgs &a) {
+template <class Team>
+__device__ double final_rn(const SsaArgs &a, const Team &t) {
   __shared__ double s_rn;
   if (threadIdx.x < 32) {
     double x = 0.0, y = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
+    for (int b = threadIdx.x; b < t.size(); b += 32) {
       x += *(volatile double *)&a.rn_part[2 * b];
       y += *(volatile double *)&a.rn_part[2 * b + 1];
     }
@@ -302,10 +326,10 @@ __device__ double final_rn(const SsaArgs &a) {
 }
 
 // Sliding term S, centre coefficients (eu, ev), their reciprocals and the right-hand sides.
-template <int kMode>
-__device__ void phase_coefficients(const SsaArgs &a) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
+template <int kMode, class Team>
+__device__ void phase_coefficients(const SsaArgs &a, const Team &t) {
+  const int tid = t.rank() * blockDim.x + threadIdx.x;
+  const int nt = t.size() * blockDim.x;
   for (int p = tid; p < a.nP; p += nt) {
     if (a.deg[p] == 0) continue;
     double S;
@@ -544,9 +568,10 @@ __device__ void phase_boundary(const SsaArgs &a, const PatchSmem &ps) {
 }
 
 // Mixed path: u0 += d, d = 0 on every row.
-__device__ void phase_fold(const SsaArgs &a) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
+template <class Team>
+__device__ void phase_fold(const SsaArgs &a, const Team &t) {
+  const int tid = t.rank() * blockDim.x + threadIdx.x;
+  const int nt = t.size() * blockDim.x;
   for (int p = tid; p < a.nP; p += nt) {
     const float2 d = a.dUV[p];
     if (d.x != 0.0f || d.y != 0.0f) {
@@ -560,10 +585,11 @@ __device__ void phase_fold(const SsaArgs &a) {
 }
 
 // Mixed path: FP64 defect r0 = RHS - LHS(u0) on the swept rows (streamed coefficient loads).
-__device__ void phase_defect(const SsaArgs &a) {
+template <class Team>
+__device__ void phase_defect(const SsaArgs &a, const Team &t) {
   const int warps_per_block = blockDim.x >> 5;
-  const int gw = blockIdx.x * warps_per_block + (threadIdx.x >> 5);
-  const int nw = gridDim.x * warps_per_block;
+  const int gw = t.rank() * warps_per_block + (threadIdx.x >> 5);
+  const int nw = t.size() * warps_per_block;
   const int lane = threadIdx.x & 31;
   for (int s = gw; s < a.nSlices; s += nw) {
     if (a.slice_g[s] == 5) continue;
@@ -590,9 +616,10 @@ __device__ void phase_defect(const SsaArgs &a) {
   }
 }
 
-__device__ void phase_zero_velocity(const SsaArgs &a, bool mixed) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nt = gridDim.x * blockDim.x;
+template <class Team>
+__device__ void phase_zero_velocity(const SsaArgs &a, const Team &t, bool mixed) {
+  const int tid = t.rank() * blockDim.x + threadIdx.x;
+  const int nt = t.size() * blockDim.x;
   for (int p = tid; p < a.nP; p += nt) {
     a.UV[p] = make_double2(0.0, 0.0);
     if (mixed) a.dUV[p] = make_float2(0.0f, 0.0f);
@@ -604,11 +631,12 @@ __device__ void phase_zero_velocity(const SsaArgs &a, bool mixed) {
 // ---------------------------------------------------------------------------------------
 
 // Progress of this CTA's patch: the number of colour phases it has completed in this launch.
-__device__ __forceinline__ void publish_progress(const SsaArgs &a, unsigned int value) {
+template <class Team>
+__device__ __forceinline__ void publish_progress(const SsaArgs &a, const Team &t, unsigned int value) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.prog + 32 * blockIdx.x), "r"(value) : "memory");
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(a.prog + 32 * t.rank()), "r"(value) : "memory");
   }
 }
 
@@ -637,16 +665,18 @@ __device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSme
   __syncthreads();
 }
 
-template <int kMode>
-__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(SsaArgs a) {
+// The whole solve_SSA of one problem, run by the CTAs of a team (each CTA owns one patch).
+// Returns false when a bounded wait failed; the error is recorded in the problem's control
+// block and the team's barrier counter.
+template <int kMode, class Team>
+__device__ bool solve_member(const SsaArgs &a, Team &t) {
   constexpr bool kM = kMode == kMixed;
   SsaCtl *ctl = a.ctl;
-  unsigned int epoch = 0;
-  unsigned int phases = 0;   // colour phases completed by this patch in this launch
-  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  unsigned int phases = 0;   // colour phases completed by this patch
+  const bool leader = t.rank() == 0 && threadIdx.x == 0;
   __shared__ PatchSmem ps;
   {
-    const int b = blockIdx.x;
+    const int b = t.rank();
     if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
     if (threadIdx.x == 0) {
       ps.edge0 = a.patch_edge0[b];
@@ -666,24 +696,24 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(SsaArgs 
   int it = 0;
   bool picard_done = false;
 #define UFE_GRID_SYNC()                                   \
-  if (!grid_barrier(ctl, epoch, a.timeout_ns)) {          \
-    if (threadIdx.x == 0) a.prog[32 * blockIdx.x] = 0x7fffffffu; \
-    return;                                               \
+  if (!team_barrier(t, &ctl->err, a.timeout_ns)) {        \
+    if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu; \
+    return false;                                         \
   }
   while (!picard_done && it < a.max_outer) {
     ++it;
     // N_prev <- N, then the new viscosity into N
     { double *t = N; N = Nprev; Nprev = t; }
-    phase_viscosity(a, N, Nprev, kM && a.fp32_visc);
+    phase_viscosity(a, t, N, Nprev, kM && a.fp32_visc);
     UFE_GRID_SYNC();
-    const double RN = final_rn(a);
+    const double RN = final_rn(a, t);
     if (leader) { ctl->picard_iterations = it; ctl->last_RN = RN; }
     if (RN < a.rn_tol) { picard_done = true; break; }
-    phase_coefficients<kMode>(a);
+    phase_coefficients<kMode>(a, t);
     if (leader) { ctl->maxres[0] = 0ull; ctl->maxres[1] = 0ull; ctl->maxres[2] = 0ull; }
     UFE_GRID_SYNC();
     if (kM) {
-      phase_defect(a);
+      phase_defect(a, t);
       UFE_GRID_SYNC();
     }
     // Coloured SOR. Colour phases synchronise only with the neighbouring patches; the
@@ -706,7 +736,7 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(SsaArgs 
         else m = phase_sweep32(a, ps, g);
         mx = m > mx ? m : mx;
         ++phases;
-        publish_progress(a, phases);
+        publish_progress(a, t, phases);
       }
       block_max_to(&ctl->maxres[slot], mx);
       wait_neighbours(a, ps, phases);
@@ -716,21 +746,21 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(SsaArgs 
       if (maxres < a.tol) {
         lin_done = true;
       } else if (maxres > 1e6) {
-        phase_zero_velocity(a, kM);
+        phase_zero_velocity(a, t, kM);
         UFE_GRID_SYNC();
         did_reset = 1;
         lin_done = true;
       } else if (sweeps == a.max_inner) {
         if (leader) ctl->not_converged += 1;
       } else if (kM && a.refold > 0 && sweeps % a.refold == 0) {
-        phase_fold(a);
+        phase_fold(a, t);
         UFE_GRID_SYNC();
-        phase_defect(a);
+        phase_defect(a, t);
         UFE_GRID_SYNC();
       }
     }
     if (kM && !did_reset) {
-      phase_fold(a);
+      phase_fold(a, t);
       UFE_GRID_SYNC();
     }
     if (leader) {
@@ -750,12 +780,66 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(SsaArgs 
   }
   // Final N lives in N; make Na hold it for the scatter.
   if (N != a.Na) {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nt = gridDim.x * blockDim.x;
+    const int tid = t.rank() * blockDim.x + threadIdx.x;
+    const int nt = t.size() * blockDim.x;
     UFE_GRID_SYNC();
     for (int p = tid; p < a.nP; p += nt) a.Na[p] = N[p];
   }
+  UFE_GRID_SYNC();
+  return true;
 #undef UFE_GRID_SYNC
+}
+
+// Stage the argument block in shared memory (it is read on every phase by every thread).
+__device__ __forceinline__ void stage_args(SsaArgs &dst, const SsaArgs *src) {
+  const int n = (int)(sizeof(SsaArgs) / sizeof(int));
+  int *d = reinterpret_cast<int *>(&dst);
+  const int *q = reinterpret_cast<const int *>(src);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) d[i] = q[i];
+  __syncthreads();
+}
+
+// Single solve: the whole grid is one team; the argument block stays in the kernel's
+// parameter space (constant bank operands cost no registers).
+template <int kMode>
+__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(const SsaArgs a) {
+  GridTeam t{&a.ctl->bar_count, 0u};
+  solve_member<kMode>(a, t);
+}
+
+// Ensemble of independent solves in one launch: the grid is cut into teams of team_size
+// CTAs; each team takes the next member from a queue (members sorted by expected cost,
+// largest first) and solves it with its own barriers, until the queue is empty.
+struct BatchArgs {
+  const SsaArgs *members;        // [n_members], device
+  int n_members;
+  int team_size;
+  unsigned int *queue;           // next member index
+  unsigned int *team_bar;        // [n_teams * 32] barrier counters
+  unsigned int *team_member;     // [n_teams * 32] member being solved
+  unsigned long long *times;     // [n_members * 2] start / end (ns, globaltimer)
+  int *err;
+  long long timeout_ns;
+};
+
+template <int kMode>
+__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_batched(const BatchArgs b) {
+  __shared__ SsaArgs a;
+  const int team = blockIdx.x / b.team_size;
+  SubTeam t{(int)(blockIdx.x % b.team_size), b.team_size, b.team_bar + 32 * team, 0u};
+  for (;;) {
+    if (t.rank() == 0 && threadIdx.x == 0) {
+      const unsigned int m = atomicAdd(b.queue, 1u);
+      b.team_member[32 * team] = m;
+      if (m < (unsigned)b.n_members) b.times[2 * m] = globaltimer_ns();
+    }
+    if (!team_barrier(t, b.err, b.timeout_ns)) return;
+    const unsigned int m = *(volatile unsigned int *)&b.team_member[32 * team];
+    if (m >= (unsigned)b.n_members) return;
+    stage_args(a, b.members + m);
+    if (!solve_member<kMode>(a, t)) return;
+    if (t.rank() == 0 && threadIdx.x == 0) b.times[2 * m + 1] = globaltimer_ns();
+  }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -1061,28 +1145,46 @@ extern "C" int ufe_ssa_upload(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_i
   return rc;
 }
 
-extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *stats) {
-  if (!h || !p) { set_error("ufe_ssa_run: null argument"); return UFE_BAD_ARG; }
-  SsaWork *w = h->ssa;
-  if (!w || !w->uploaded) { set_error("ufe_ssa_run: no inputs uploaded"); return UFE_BAD_ARG; }
-  if (p->precision != UFE_FP64 && p->precision != UFE_MIXED) { set_error("ufe_ssa_run: unknown precision"); return UFE_BAD_ARG; }
+namespace ufe {
+namespace {
+
+int check_params(const ufe_params *p, const char *who) {
+  if (p->precision != UFE_FP64 && p->precision != UFE_MIXED) { set_error(std::string(who) + ": unknown precision"); return UFE_BAD_ARG; }
   if (p->sliding_law != UFE_SLIDING_COULOMB_REGULARISED && p->sliding_law != UFE_SLIDING_LINEAR) {
-    set_error("ufe_ssa_run: sliding law not implemented");
+    set_error(std::string(who) + ": sliding law not implemented");
     return UFE_BAD_ARG;
   }
-  if (p->SSA_max_inner_loops < 1 || p->SSA_max_outer_loops < 1) { set_error("ufe_ssa_run: loop limits must be >= 1"); return UFE_BAD_ARG; }
-  const DevMesh &m = h->m;
-  cudaStream_t s = h->stream;
-  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA, nP = w->nP;
-  int rc = UFE_OK;
-  const bool mixed = p->precision == UFE_MIXED;
+  if (p->SSA_max_inner_loops < 1 || p->SSA_max_outer_loops < 1) {
+    set_error(std::string(who) + ": loop limits must be >= 1");
+    return UFE_BAD_ARG;
+  }
+  return UFE_OK;
+}
 
+int sweep_mode(const ufe_params *p) {
+  return p->precision == UFE_MIXED ? kMixed : (p->fp64_exact ? kExact64 : kFast64);
+}
+
+Fields fields_of(SsaWork *w) {
+  const size_t nP = w->nP;
   double *F = w->f;
   Fields fl;
   fl.Hi = F + F_HI * nP; fl.Hb = F + F_HB * nP; fl.SL = F + F_SL * nP; fl.hx = F + F_HX * nP;
   fl.hy = F + F_HY * nP; fl.Af = F + F_AF * nP; fl.beta = w->has_beta ? F + F_BETA * nP : nullptr;
   fl.tau = F + F_TAU * nP; fl.phi = F + F_PHI * nP; fl.UV = w->UV; fl.dUV = w->dUV;
   fl.Na = F + F_NA * nP; fl.Nb = F + F_NB * nP;
+  return fl;
+}
+
+// Gather the uploaded inputs into device order (and the GL flux rows), clear the control
+// block, and fill the argument block of the persistent solver. Returns *solve = false when
+// the reference's early-out applies (no solve to run).
+int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a, bool *solve) {
+  SsaWork *w = h->ssa;
+  const DevMesh &m = h->m;
+  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA, nP = w->nP;
+  Fields fl = fields_of(w);
+  double *F = w->f;
   double *st = w->stage_in;
   StageIn si;
   si.Hi = st; si.Hb = st + nV; si.SL = st + 2 * nV; si.hx = st + 3 * nV; si.hy = st + 4 * nV; si.Af = st + 5 * nV;
@@ -1092,10 +1194,7 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
   si.beta = w->has_beta ? acb + 6 * nAc : nullptr;
   si.U = acb + 6 * nAc + nA; si.V = si.U + nV; si.Ux = si.V + nV; si.Uy = si.Ux + nAc;
   si.N = w->has_N ? si.Uy + nAc : nullptr;
-
-  std::memset(w->ctl_host, 0, sizeof(SsaCtl));
-  rc = cuda_status(cudaEventRecord(w->ev0, s), "event");
-  if (!rc) rc = cuda_status(cudaMemsetAsync(w->ctl, 0, sizeof(SsaCtl), s), "memset ctl");
+  int rc = cuda_status(cudaMemsetAsync(w->ctl, 0, sizeof(SsaCtl), s), "memset ctl");
   if (!rc) {
     k_gather<<<(unsigned)((nP + 255) / 256), 256, 0, s>>>((int)nP, (int)nV, m.orig_of_dev, si, fl);
     rc = cuda_status(cudaGetLastError(), "k_gather");
@@ -1109,66 +1208,62 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     k_gl_flux<<<(unsigned)((nAc + 255) / 256), 256, 0, s>>>((int)nAc, (int)nV, m.dev_of_orig, m.Aci12, g, fl.phi, w->UV, w->skip, 8.0 * 0.61);
     rc = cuda_status(cudaGetLastError(), "k_gl_flux");
   }
-  if (!rc && !w->zero) {
-    SsaArgs a;
-    std::memset(&a, 0, sizeof(a));
-    a.col = m.col; a.cuv = m.cuv; a.nxy = m.nxy; a.cuv32 = m.cuv32; a.nxy32 = m.nxy32; a.deg = m.deg;
-    a.slice_ptr = m.slice_ptr; a.h_nxy = m.h_nxy; a.h_cuv = m.h_cuv; a.sNxy = m.sNxy;
-    a.s3Nxy = m.s3Nxy; a.h_nxy32 = m.h_nxy32; a.s3Nxy32 = m.s3Nxy32; a.bnd_ptr = m.bnd_ptr; a.bnd_nbr = m.bnd_nbr;
-    a.slice_e0 = m.slice_e0; a.slice_w = m.slice_w; a.slice_g = m.slice_g; a.patch_slice = m.patch_slice;
-    a.patch_edge0 = m.patch_edge0; a.edge_row = m.edge_row; a.sync_ptr = m.sync_ptr; a.sync_list = m.sync_list;
-    a.prog = w->prog; a.nP = m.nP; a.nSlices = m.nSlices; a.ncm = m.ncm;
-    a.Hi = fl.Hi; a.Hb = fl.Hb; a.SL = fl.SL; a.hx = fl.hx; a.hy = fl.hy; a.Af = fl.Af;
-    a.beta = fl.beta; a.tau = fl.tau;
-    a.skip = w->gl ? w->skip : nullptr;
-    a.UV = w->UV; a.dUV = w->dUV; a.r0 = w->r0; a.rcp32 = w->rcp32; a.rcp = w->rcp;
-    a.eta = F + F_ETA * nP; a.Na = fl.Na; a.Nb = fl.Nb; a.S = F + F_S * nP;
-    a.rhs = w->rhs; a.euv = w->euv; a.rn_part = w->rn_part; a.ctl = w->ctl;
-    a.omega = p->SSA_SOR_omega; a.tol = p->SSA_max_residual_UV; a.rn_tol = p->SSA_RN_tol;
-    a.m_enh = p->m_enh_ssa;
-    a.uq = std::pow(100.0, 0.30);          // u_threshold**q_plastic
-    a.expo = 0.5 * (0.30 - 1.0);           // 0.5*(q_plastic-1)
-    a.beta_const = p->beta_sq;
-    a.max_inner = p->SSA_max_inner_loops; a.max_outer = p->SSA_max_outer_loops;
-    a.sliding_law = p->sliding_law; a.has_beta = w->has_beta;
-    a.refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 32;
-    a.fp32_visc = p->mixed_fp32_viscosity != 0;
-    a.timeout_ns = 20LL * 1000 * 1000 * 1000;
-    void *args[] = {&a};
-    const int mode = mixed ? kMixed : (p->fp64_exact ? kExact64 : kFast64);
-    const void *fn = mode == kMixed ? (const void *)ssa_persistent<kMixed>
-                     : mode == kFast64 ? (const void *)ssa_persistent<kFast64>
-                                       : (const void *)ssa_persistent<kExact64>;
-    rc = cuda_status(cudaMemsetAsync(F + F_S * nP, 0, nP * sizeof(double), s), "memset S");
-    if (!rc) rc = cuda_status(cudaMemsetAsync(w->prog, 0, 32 * (size_t)w->grid[mode] * sizeof(unsigned int), s), "memset prog");
-    if (!rc)
-      rc = cuda_status(cudaLaunchCooperativeKernel(fn, dim3(w->grid[mode]), dim3(w->block), args, 0, s),
-                       "ssa_persistent");
-  }
+  if (!rc) rc = cuda_status(cudaMemsetAsync(F + F_S * nP, 0, nP * sizeof(double), s), "memset S");
+  if (!rc) rc = cuda_status(cudaMemsetAsync(w->prog, 0, 32 * (size_t)m.n_patch * sizeof(unsigned int), s), "memset prog");
+  *solve = !w->zero;
+  std::memset(a, 0, sizeof(*a));
+  a->col = m.col; a->cuv = m.cuv; a->nxy = m.nxy; a->cuv32 = m.cuv32; a->nxy32 = m.nxy32; a->deg = m.deg;
+  a->slice_ptr = m.slice_ptr; a->h_nxy = m.h_nxy; a->h_cuv = m.h_cuv; a->sNxy = m.sNxy;
+  a->s3Nxy = m.s3Nxy; a->h_nxy32 = m.h_nxy32; a->s3Nxy32 = m.s3Nxy32; a->bnd_ptr = m.bnd_ptr; a->bnd_nbr = m.bnd_nbr;
+  a->slice_e0 = m.slice_e0; a->slice_w = m.slice_w; a->slice_g = m.slice_g; a->patch_slice = m.patch_slice;
+  a->patch_edge0 = m.patch_edge0; a->edge_row = m.edge_row; a->sync_ptr = m.sync_ptr; a->sync_list = m.sync_list;
+  a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
+  a->Hi = fl.Hi; a->Hb = fl.Hb; a->SL = fl.SL; a->hx = fl.hx; a->hy = fl.hy; a->Af = fl.Af;
+  a->beta = fl.beta; a->tau = fl.tau;
+  a->skip = w->gl ? w->skip : nullptr;
+  a->UV = w->UV; a->dUV = w->dUV; a->r0 = w->r0; a->rcp32 = w->rcp32; a->rcp = w->rcp;
+  a->eta = F + F_ETA * nP; a->Na = fl.Na; a->Nb = fl.Nb; a->S = F + F_S * nP;
+  a->rhs = w->rhs; a->euv = w->euv; a->rn_part = w->rn_part; a->ctl = w->ctl;
+  a->omega = p->SSA_SOR_omega; a->tol = p->SSA_max_residual_UV; a->rn_tol = p->SSA_RN_tol;
+  a->m_enh = p->m_enh_ssa;
+  a->uq = std::pow(100.0, 0.30);          // u_threshold**q_plastic
+  a->expo = 0.5 * (0.30 - 1.0);           // 0.5*(q_plastic-1)
+  a->beta_const = p->beta_sq;
+  a->max_inner = p->SSA_max_inner_loops; a->max_outer = p->SSA_max_outer_loops;
+  a->sliding_law = p->sliding_law; a->has_beta = w->has_beta;
+  a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 32;
+  a->fp32_visc = p->mixed_fp32_viscosity != 0;
+  a->timeout_ns = 20LL * 1000 * 1000 * 1000;
+  return rc;
+}
+
+// Scatter the results back to the caller's order and fetch the control block.
+int launch_finish(ufe_mesh_h h, cudaStream_t s) {
+  SsaWork *w = h->ssa;
+  const DevMesh &m = h->m;
+  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA, nP = w->nP;
+  Fields fl = fields_of(w);
+  double *F = w->f;
+  StageOut o;
+  double *so = w->stage_out;
+  o.U = so; o.V = so + nV; o.Ux = so + 2 * nV; o.Uy = o.Ux + nAc; o.Up = o.Uy + nAc; o.Uo = o.Up + nAc;
+  o.N = o.Uo + nAc; o.eta = o.N + nA; o.S = o.eta + nA; o.tau = o.S + nA; o.phi = o.tau + nA;
+  int rc = UFE_OK;
+  if (w->zero) rc = cuda_status(cudaMemsetAsync(w->UV, 0, nP * sizeof(double2), s), "memset UV");
   if (!rc) {
-    StageOut o;
-    double *so = w->stage_out;
-    o.U = so; o.V = so + nV; o.Ux = so + 2 * nV; o.Uy = o.Ux + nAc; o.Up = o.Uy + nAc; o.Uo = o.Up + nAc;
-    o.N = o.Uo + nAc; o.eta = o.N + nA; o.S = o.eta + nA; o.tau = o.S + nA; o.phi = o.tau + nA;
-    if (w->zero) {
-      // velocities zero, Picard state untouched
-      rc = cuda_status(cudaMemsetAsync(w->UV, 0, nP * sizeof(double2), s), "memset UV");
-    }
-    if (!rc) {
-      k_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>((int)nA, (int)nV, m.dev_of_orig, m.V, m.Aci12, w->UV,
-                                                            fl.Na, F + F_ETA * nP, F + F_S * nP, fl.tau, fl.phi, o);
-      rc = cuda_status(cudaGetLastError(), "k_scatter");
-    }
+    k_scatter<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>((int)nA, (int)nV, m.dev_of_orig, m.V, m.Aci12, w->UV,
+                                                          fl.Na, F + F_ETA * nP, F + F_S * nP, fl.tau, fl.phi, o);
+    rc = cuda_status(cudaGetLastError(), "k_scatter");
   }
   if (!rc) rc = cuda_status(cudaMemcpyAsync(w->ctl_host, w->ctl, sizeof(SsaCtl), cudaMemcpyDeviceToHost, s), "ctl D2H");
-  if (!rc) rc = cuda_status(cudaEventRecord(w->ev1, s), "event");
-  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa solve");
-  if (rc) return rc;
-  const SsaCtl &c = *w->ctl_host;
+  return rc;
+}
+
+int stats_of(const SsaCtl &c, ufe_ssa_stats *stats, double ms) {
   int status = UFE_OK;
   if (c.err) {
     status = c.err;
-    set_error("ufe_ssa_run: a device-side barrier wait timed out");
+    set_error("solve_SSA: a device-side bounded wait timed out");
   } else if (c.status == UFE_DIVERGED) {
     status = UFE_DIVERGED;
     set_error("solve_SSA: SSA remains unstable after resetting velocities to zero");
@@ -1188,11 +1283,45 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     stats->last_RN = c.last_RN;
     stats->last_max_residual = c.last_max_residual;
     for (int k = 0; k < 64; ++k) stats->sweeps[k] = c.sweeps[k];
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, w->ev0, w->ev1);
     stats->device_ms = ms;
   }
   return status;
+}
+
+const void *persistent_kernel(int mode) {
+  return mode == kMixed ? (const void *)ssa_persistent<kMixed>
+         : mode == kFast64 ? (const void *)ssa_persistent<kFast64>
+                           : (const void *)ssa_persistent<kExact64>;
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *stats) {
+  if (!h || !p) { set_error("ufe_ssa_run: null argument"); return UFE_BAD_ARG; }
+  SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) { set_error("ufe_ssa_run: no inputs uploaded"); return UFE_BAD_ARG; }
+  int rc = check_params(p, "ufe_ssa_run");
+  if (rc) return rc;
+  cudaStream_t s = h->stream;
+  std::memset(w->ctl_host, 0, sizeof(SsaCtl));
+  rc = cuda_status(cudaEventRecord(w->ev0, s), "event");
+  bool solve = false;
+  SsaArgs a;
+  if (!rc) rc = launch_prepare(h, p, s, &a, &solve);
+  if (!rc && solve) {
+    const int mode = sweep_mode(p);
+    void *args[] = {(void *)&a};
+    rc = cuda_status(cudaLaunchCooperativeKernel(persistent_kernel(mode), dim3(w->grid[mode]), dim3(w->block), args, 0, s),
+                       "ssa_persistent");
+  }
+  if (!rc) rc = launch_finish(h, s);
+  if (!rc) rc = cuda_status(cudaEventRecord(w->ev1, s), "event");
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa solve");
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+  return stats_of(*w->ctl_host, stats, ms);
 }
 
 extern "C" int ufe_ssa_download(ufe_mesh_h h, ufe_ssa_inout *io, ufe_ssa_out *out) {
