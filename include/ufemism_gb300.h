@@ -184,6 +184,20 @@ int ufe_ssa_download(ufe_mesh_h mesh, ufe_ssa_inout *inout, ufe_ssa_out *out);
 int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
                   ufe_sia_out *out);
 
+/* No counterpart in the reference. ufe_sia_solve for callers that cannot allocate device
+ * memory (a model that reserves the device's memory for its own pool; a time loop that cannot
+ * afford the device-wide synchronisation of cudaMalloc/cudaFree): every array of `in` and `out`
+ * is DEVICE memory of the mesh's device (the mesh's device must be current), nothing is
+ * allocated, and the Ac intermediates the caller leaves NULL live in a fixed scratch array of
+ * the library (at most UFE_SIA_NOALLOC_MAX_AC Ac edges; larger meshes return UFE_BAD_ARG).
+ * Up to 64 devices. The first call on a device looks up the scratch address: make it before
+ * any stream capture. The scratch is shared by every call on a device: calls that overlap in
+ * time (several threads, or several meshes of the same device) race on it and must be
+ * serialised by the caller. Synchronous like ufe_sia_solve. */
+#define UFE_SIA_NOALLOC_MAX_AC 262144
+int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
+                          ufe_sia_out *out);
+
 /* Host-side mesh substrate: builds the Ac and combined AaAc mesh, the AaAc and Aa
  * neighbour functions and the five-colouring from a base triangulation, exactly as
  * make_Ac_mesh (mesh_ArakawaC_module.f90:24-540), get_neighbour_functions

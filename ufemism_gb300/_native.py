@@ -19,6 +19,7 @@ UFE_OK, UFE_NOT_CONVERGED, UFE_RESET_ONCE = 0, 1, 2
 UFE_DIVERGED, UFE_BAD_MESH, UFE_COLOUR_IDENTIFY, UFE_TIMEOUT = -1, -2, -3, -4
 UFE_CUDA_ERROR, UFE_BAD_ARG, UFE_NO_DEVICE, UFE_OUT_OF_MEMORY = -5, -6, -7, -8
 UFE_FP64, UFE_MIXED = 0, 1
+UFE_SIA_NOALLOC_MAX_AC = 262144   # scratch limit of ufe_sia_solve_noalloc (Ac edges)
 UFE_SLIDING_COULOMB_REGULARISED, UFE_SLIDING_LINEAR = 0, 1
 
 STATUS_NAMES = {0: "UFE_OK", 1: "UFE_NOT_CONVERGED", 2: "UFE_RESET_ONCE", -1: "UFE_DIVERGED",
@@ -101,6 +102,7 @@ PROTOTYPES = {
     "ufe_ssa_run": (I32, [P, ct.POINTER(Params), ct.POINTER(SsaStats)]),
     "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_aaac_build": (I32, [ct.POINTER(BaseMeshC), ct.POINTER(AaAcMeshC)]),
 }
 

@@ -8,7 +8,9 @@
 // a small gather over iAci. Built with --fmad=false: every product and sum rounds as in the
 // reference.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "ufe_internal.h"
@@ -177,5 +179,130 @@ extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in
   back(out->V_SIA, Va, nV);
   back(out->D_SIA, Da, nV);
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "sia solve");
+  return rc;
+}
+
+// ---------------------------------------------------------------------------------------
+// solve_SIA without allocation: device-resident inputs and outputs, intermediates in a
+// fixed scratch array of this translation unit.
+//
+// Who needs it: a model that keeps its ice state on the device and reserves its device
+// memory up front (its own pool sized to the HBM it wants), and a time loop that must not
+// stall: cudaMalloc and cudaFree synchronise the whole device, and the per-handle buffers of
+// ufe_sia_solve are (re)allocated on the first call and whenever nZ changes. This entry
+// point calls neither; its only device memory beyond the caller's arrays is the scratch
+// below, which exists from the moment the module is loaded.
+// ---------------------------------------------------------------------------------------
+namespace ufe {
+namespace {
+
+constexpr int kNoAllocMaxAc = UFE_SIA_NOALLOC_MAX_AC;
+constexpr int kNoAllocMaxDevices = 64;
+// Layout: zeta (kMaxZ), zeta^3 (kMaxZ), then D, Ux, Uy, Up, Uo on the Ac edges (kNoAllocMaxAc
+// each): 2 * 64 + 5 * 262,144 doubles = 10 MiB + 1 KiB.
+constexpr size_t kNoAllocScratch = 2 * (size_t)kMaxZ + 5 * (size_t)kNoAllocMaxAc;
+static __device__ __align__(256) double g_sia_scratch[kNoAllocScratch];
+
+std::mutex g_scratch_mutex;
+double *g_scratch_ptr[kNoAllocMaxDevices] = {};
+
+// Address of the scratch on the current device, looked up once per device.
+int scratch_address(int device, double **out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[device]) {
+    double *p = nullptr;
+    const int rc = cuda_status(cudaGetSymbolAddress((void **)&p, g_sia_scratch), "cudaGetSymbolAddress(scratch)");
+    if (rc) return rc;
+    g_scratch_ptr[device] = p;
+  }
+  *out = g_scratch_ptr[device];
+  return UFE_OK;
+}
+
+// The kernels dereference every array given, so each must be device memory of this device
+// (or managed memory); a host pointer is rejected here instead of faulting there.
+bool on_device(const void *ptr, int device) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) { cudaGetLastError(); return false; }
+  if (at.type == cudaMemoryTypeManaged) return true;
+  return at.type == cudaMemoryTypeDevice && at.device == device;
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_sia_solve_noalloc(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out) {
+  if (!h || !p || !in || !out) { set_error("ufe_sia_solve_noalloc: null argument"); return UFE_BAD_ARG; }
+  const char *who = "ufe_sia_solve_noalloc";
+  if (!in->mask_sheet_Ac || !in->Hi_Ac || !in->dHs_dx_Ac || !in->dHs_dy_Ac || !in->dHs_dp_Ac ||
+      !in->dHs_do_Ac || !in->A_flow_Ac || !p->zeta) {
+    set_error(std::string(who) + ": missing input array");
+    return UFE_BAD_ARG;
+  }
+  if (p->nZ < 2 || p->nZ > kMaxZ) { set_error(std::string(who) + ": nZ must be in [2, 64]"); return UFE_BAD_ARG; }
+  const DevMesh &m = h->m;
+  const int nV = m.nV, nAc = m.nAc, nZ = p->nZ;
+  if (nAc > kNoAllocMaxAc) {
+    char buf[192];
+    std::snprintf(buf, sizeof buf, "%s: the mesh has %d Ac edges; the fixed scratch holds at most %d", who, nAc,
+                  kNoAllocMaxAc);
+    set_error(buf);
+    return UFE_BAD_ARG;
+  }
+  if (!out->U_SIA != !out->V_SIA || !out->U_SIA != !out->D_SIA) {
+    set_error(std::string(who) + ": U_SIA, V_SIA and D_SIA are given together or not at all");
+    return UFE_BAD_ARG;
+  }
+  int dev = -1;
+  int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  if (dev != h->device || dev < 0 || dev >= kNoAllocMaxDevices) {
+    set_error(std::string(who) + ": the mesh's device must be the current device");
+    return UFE_BAD_ARG;
+  }
+  const void *ins[7] = {in->mask_sheet_Ac, in->Hi_Ac, in->dHs_dx_Ac, in->dHs_dy_Ac, in->dHs_dp_Ac, in->dHs_do_Ac,
+                        in->A_flow_Ac};
+  const void *outs[9] = {out->D_SIA_3D_Ac, out->D_SIA_Ac, out->Ux_SIA_Ac, out->Uy_SIA_Ac, out->Up_SIA_Ac,
+                         out->Uo_SIA_Ac, out->U_SIA, out->V_SIA, out->D_SIA};
+  for (const void *q : ins)
+    if (!on_device(q, dev)) { set_error(std::string(who) + ": an input array is not device memory of the mesh's device"); return UFE_BAD_ARG; }
+  for (const void *q : outs)
+    if (q && !on_device(q, dev)) { set_error(std::string(who) + ": an output array is not device memory of the mesh's device"); return UFE_BAD_ARG; }
+  double *scratch = nullptr;
+  rc = scratch_address(dev, &scratch);
+  if (rc) return rc;
+  cudaStream_t s = h->stream;
+  // zeta and zeta**n_flow (n = 3) as in ufe_sia_solve, staged from the stack.
+  double zc[2 * kMaxZ];
+  for (int k = 0; k < nZ; ++k) { zc[k] = p->zeta[k]; zc[nZ + k] = std::pow(p->zeta[k], 3.0); }
+  double *zeta = scratch, *zeta3 = scratch + nZ;
+  // Ac intermediates the caller did not ask for go to the scratch. Every scratch word a
+  // kernel reads is written earlier in the same call, so nothing needs clearing.
+  double *edge = scratch + 2 * kMaxZ;
+  const size_t na = nAc;
+  double *D = out->D_SIA_Ac ? out->D_SIA_Ac : edge;
+  double *Ux = out->Ux_SIA_Ac ? out->Ux_SIA_Ac : edge + na;
+  double *Uy = out->Uy_SIA_Ac ? out->Uy_SIA_Ac : edge + 2 * na;
+  double *Up = out->Up_SIA_Ac ? out->Up_SIA_Ac : edge + 3 * na;
+  double *Uo = out->Uo_SIA_Ac ? out->Uo_SIA_Ac : edge + 4 * na;
+  rc = cuda_status(cudaMemcpyAsync(zeta, zc, 2 * (size_t)nZ * sizeof(double), cudaMemcpyHostToDevice, s), "H2D zeta");
+  if (!rc) {
+    const unsigned g = (unsigned)((nAc + 255) / 256);
+    if (nZ == 15)
+      k_sia_edges<15><<<g, 256, 0, s>>>(nAc, nZ, in->mask_sheet_Ac, in->Hi_Ac, in->dHs_dx_Ac, in->dHs_dy_Ac,
+                                        in->dHs_dp_Ac, in->dHs_do_Ac, in->A_flow_Ac, zeta, zeta3, p->m_enh_sia,
+                                        out->D_SIA_3D_Ac, D, Ux, Uy, Up, Uo);
+    else
+      k_sia_edges<0><<<g, 256, 0, s>>>(nAc, nZ, in->mask_sheet_Ac, in->Hi_Ac, in->dHs_dx_Ac, in->dHs_dy_Ac,
+                                       in->dHs_dp_Ac, in->dHs_do_Ac, in->A_flow_Ac, zeta, zeta3, p->m_enh_sia,
+                                       out->D_SIA_3D_Ac, D, Ux, Uy, Up, Uo);
+    rc = cuda_status(cudaGetLastError(), "k_sia_edges");
+  }
+  if (!rc && out->U_SIA) {
+    k_ac_to_aa3<<<(unsigned)((nV + 255) / 256), 256, 0, s>>>(nV, m.nC, m.iAci, Ux, Uy, D, out->U_SIA, out->V_SIA,
+                                                            out->D_SIA);
+    rc = cuda_status(cudaGetLastError(), "k_ac_to_aa3");
+  }
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "sia solve (no allocation)");
   return rc;
 }
