@@ -198,6 +198,36 @@ int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *i
 int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
                           ufe_sia_out *out);
 
+/* Batched ensemble (no counterpart in the reference, whose model runs one solve_SSA per
+ * time step): many independent solves on meshes of uneven size (friction or rheology
+ * ensembles) in one persistent cooperative launch. The grid is cut into teams of
+ * team_ctas CTAs; every member mesh is laid out in exactly team_ctas spatial patches, and
+ * each team takes the next member (largest expected cost first) from a device queue until
+ * none is left. With use_graph the whole batch (gathers, the persistent solve, scatters)
+ * is captured once per parameter set and replayed as a CUDA graph. Members share one
+ * ufe_params; their inputs are uploaded one by one (the arrays of ufe_ssa_upload). */
+typedef struct ufe_batch_s *ufe_batch_h;
+typedef struct ufe_batch_config {
+  int32_t team_ctas;   /* CTAs per member (0: the fewest that fit the largest member) */
+  int32_t block;       /* threads per CTA: 1024, 512 or 256 (0: 1024); 512 and 256 run 2 and 4 CTAs per SM */
+  int32_t use_graph;   /* 1: capture and replay the batch as a CUDA graph */
+} ufe_batch_config;
+typedef struct ufe_batch_timing {
+  double device_ms;      /* the whole batch on the device (CUDA events) */
+  double solve_ms;       /* first member start to last member end inside the persistent kernel */
+  double member_p50_ms, member_p99_ms, member_max_ms;  /* per-member solve time (team start to end) */
+  double *member_ms;     /* (n_members) per-member solve time, or NULL */
+  int32_t n_active, n_teams, team_ctas, block;
+} ufe_batch_timing;
+int ufe_batch_create(const ufe_mesh_desc *descs, int32_t n_members, const ufe_batch_config *config,
+                     ufe_batch_h *out);
+int ufe_batch_destroy(ufe_batch_h batch);
+int ufe_batch_upload(ufe_batch_h batch, int32_t member, const ufe_params *params, const ufe_ssa_in *in,
+                     const ufe_ssa_inout *inout);
+/* stats: (n_members) or NULL. Returns the most severe member status. */
+int ufe_batch_run(ufe_batch_h batch, const ufe_params *params, ufe_ssa_stats *stats, ufe_batch_timing *timing);
+int ufe_batch_download(ufe_batch_h batch, int32_t member, ufe_ssa_inout *inout, ufe_ssa_out *out);
+
 /* Host-side mesh substrate: builds the Ac and combined AaAc mesh, the AaAc and Aa
  * neighbour functions and the five-colouring from a base triangulation, exactly as
  * make_Ac_mesh (mesh_ArakawaC_module.f90:24-540), get_neighbour_functions

@@ -33,7 +33,8 @@ def test_library_exports_every_declared_symbol():
 def test_struct_layouts_match_header():
     # field counts of the POD structs (a cheap guard against header/binding drift)
     text = open(HEADER).read()
-    for cname, py in (("ufe_params", nat.Params), ("ufe_ssa_stats", nat.SsaStats)):
+    for cname, py in (("ufe_params", nat.Params), ("ufe_ssa_stats", nat.SsaStats),
+                      ("ufe_batch_config", nat.BatchConfig), ("ufe_batch_timing", nat.BatchTiming)):
         body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), text, re.S).group(1)
         body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
         names = re.findall(r"(\w+)(?:\[\d+\])?\s*[,;]", body)
@@ -90,3 +91,18 @@ def test_ssa_entry_points_validate_arguments():
     ps, _z = api._params_struct(api.default_params())
     assert L.ufe_ssa_run(None, ct.byref(ps), None) == nat.UFE_BAD_ARG
     assert L.ufe_ssa_solve(None, ct.byref(ps), None, None, None, None) == nat.UFE_BAD_ARG
+
+
+def test_batch_entry_points_validate_arguments():
+    L = nat.load()
+    ps, _z = api._params_struct(api.default_params())
+    h = ct.c_void_p()
+    assert L.ufe_batch_create(None, 4, None, ct.byref(h)) == nat.UFE_BAD_ARG
+    m = oracle_aaac("tiny")
+    d, keep = _desc(m)
+    cfg = nat.BatchConfig(0, 300, 1)     # not a supported CTA size
+    assert L.ufe_batch_create(ct.byref(d), 1, ct.byref(cfg), ct.byref(h)) == nat.UFE_BAD_ARG
+    assert "block" in nat.last_error()
+    assert L.ufe_batch_run(None, ct.byref(ps), None, None) == nat.UFE_BAD_ARG
+    assert L.ufe_batch_upload(None, 0, ct.byref(ps), None, None) == nat.UFE_BAD_ARG
+    assert L.ufe_batch_destroy(None) == nat.UFE_BAD_ARG

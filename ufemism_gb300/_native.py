@@ -75,6 +75,16 @@ class SiaOut(ct.Structure):
                                  "U_SIA", "V_SIA", "D_SIA")]
 
 
+class BatchConfig(ct.Structure):
+    _fields_ = [("team_ctas", I32), ("block", I32), ("use_graph", I32)]
+
+
+class BatchTiming(ct.Structure):
+    _fields_ = [("device_ms", F64), ("solve_ms", F64), ("member_p50_ms", F64), ("member_p99_ms", F64),
+                ("member_max_ms", F64), ("member_ms", P), ("n_active", I32), ("n_teams", I32),
+                ("team_ctas", I32), ("block", I32)]
+
+
 class BaseMeshC(ct.Structure):
     _fields_ = [("nV", I32), ("nTri", I32), ("nC_mem", I32)] + \
                [(n, P) for n in ("V", "nC", "C", "niTri", "iTri", "Tri", "edge_index")]
@@ -103,6 +113,11 @@ PROTOTYPES = {
     "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_batch_create": (I32, [ct.POINTER(MeshDesc), I32, ct.POINTER(BatchConfig), ct.POINTER(P)]),
+    "ufe_batch_destroy": (I32, [P]),
+    "ufe_batch_upload": (I32, [P, I32, ct.POINTER(Params), ct.POINTER(SsaIn), ct.POINTER(SsaInout)]),
+    "ufe_batch_run": (I32, [P, ct.POINTER(Params), ct.POINTER(SsaStats), ct.POINTER(BatchTiming)]),
+    "ufe_batch_download": (I32, [P, I32, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_aaac_build": (I32, [ct.POINTER(BaseMeshC), ct.POINTER(AaAcMeshC)]),
 }
 

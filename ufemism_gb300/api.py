@@ -101,31 +101,68 @@ def init(device: int = 0) -> None:
         raise nat.UfeError(rc, "ufe_init")
 
 
+def _mesh_desc(mesh):
+    """ufe_mesh_desc of a mesh, with the arrays it points to (keep them alive until the
+    library has copied them)."""
+    base = mesh.base
+    k = dict(V=_f64(base.V), nC=_i32(base.nC), iAci=_i32(mesh.iAci), Aci=_i32(mesh.Aci),
+             edge_index=_i32(base.edge_index), edge_index_Ac=_i32(mesh.edge_index_Ac),
+             nCAaAc=_i32(mesh.nCAaAc), CAaAc=_i32(mesh.CAaAc), Nx_AaAc=_f64(mesh.Nx_AaAc),
+             Ny_AaAc=_f64(mesh.Ny_AaAc), Nxx_AaAc=_f64(mesh.Nxx_AaAc), Nxy_AaAc=_f64(mesh.Nxy_AaAc),
+             Nyy_AaAc=_f64(mesh.Nyy_AaAc), colour=_i32(mesh.colour), colour_vi=_i32(mesh.colour_vi),
+             colour_nV=_i32(mesh.colour_nV))
+    d = nat.MeshDesc(base.nV, mesh.nAc, mesh.nVAaAc, k["CAaAc"].shape[1],
+                     *(_ptr(k[n]) for n in ("V", "nC", "iAci", "Aci", "edge_index", "edge_index_Ac", "nCAaAc",
+                                            "CAaAc", "Nx_AaAc", "Ny_AaAc", "Nxx_AaAc", "Nxy_AaAc", "Nyy_AaAc",
+                                            "colour", "colour_vi", "colour_nV")))
+    return d, k
+
+
+def _ssa_structs(nV, nAc, nA, fields: dict, warm: dict | None):
+    keep = {}
+
+    def g(k, dt=np.float64):
+        v = fields.get(k)
+        if v is None:
+            return None
+        a = np.ascontiguousarray(v, dtype=dt)
+        keep[k] = a
+        return a.ctypes.data
+
+    ints = ("mask_sheet", "mask_gl_Ac")
+    si = nat.SsaIn(*(g(k, np.int32 if k in ints else np.float64) for k in nat.SSA_IN_FIELDS))
+    warm = warm or {}
+    io = {}
+    for k, n in (("U_SSA", nV), ("V_SSA", nV), ("Ux_SSA_Ac", nAc), ("Uy_SSA_Ac", nAc)):
+        io[k] = np.array(warm.get(k, np.zeros(n)), dtype=np.float64, copy=True)
+    io["N_AaAc"] = np.array(warm.get("N_AaAc", np.zeros(nA)), dtype=np.float64, copy=True)
+    sio = nat.SsaInout(*(io[k].ctypes.data for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")))
+    return si, sio, io, keep
+
+
+def _download_structs(nV, nAc, nA):
+    io = {k: np.zeros(nV) for k in ("U_SSA", "V_SSA")}
+    io.update({k: np.zeros(nAc) for k in ("Ux_SSA_Ac", "Uy_SSA_Ac", "Up_SSA_Ac", "Uo_SSA_Ac")})
+    io.update({k: np.zeros(nA) for k in ("N_AaAc", "eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")})
+    sio = nat.SsaInout(*(io[k].ctypes.data for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")))
+    so = nat.SsaOut(*(io[k].ctypes.data for k in ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc", "tau_c_AaAc",
+                                                   "phi_fric_AaAc")))
+    return io, sio, so
+
+
 class DeviceMesh:
     """An uploaded mesh (ufe_mesh_create). ``mesh`` is any object with the type_mesh
     attributes: base (V, nC, edge_index) and the AaAc arrays."""
 
     def __init__(self, mesh):
         L = nat.load()
-        base = mesh.base
-        self.nV, self.nAc, self.nVAaAc = base.nV, mesh.nAc, mesh.nVAaAc
-        self._keep = dict(V=_f64(base.V), nC=_i32(base.nC), iAci=_i32(mesh.iAci), Aci=_i32(mesh.Aci),
-                          edge_index=_i32(base.edge_index), edge_index_Ac=_i32(mesh.edge_index_Ac),
-                          nCAaAc=_i32(mesh.nCAaAc), CAaAc=_i32(mesh.CAaAc), Nx_AaAc=_f64(mesh.Nx_AaAc),
-                          Ny_AaAc=_f64(mesh.Ny_AaAc), Nxx_AaAc=_f64(mesh.Nxx_AaAc), Nxy_AaAc=_f64(mesh.Nxy_AaAc),
-                          Nyy_AaAc=_f64(mesh.Nyy_AaAc), colour=_i32(mesh.colour), colour_vi=_i32(mesh.colour_vi),
-                          colour_nV=_i32(mesh.colour_nV))
-        k = self._keep
-        d = nat.MeshDesc(self.nV, self.nAc, self.nVAaAc, k["CAaAc"].shape[1],
-                         *(_ptr(k[n]) for n in ("V", "nC", "iAci", "Aci", "edge_index", "edge_index_Ac", "nCAaAc",
-                                                "CAaAc", "Nx_AaAc", "Ny_AaAc", "Nxx_AaAc", "Nxy_AaAc", "Nyy_AaAc",
-                                                "colour", "colour_vi", "colour_nV")))
+        self.nV, self.nAc, self.nVAaAc = mesh.base.nV, mesh.nAc, mesh.nVAaAc
+        d, keep = _mesh_desc(mesh)
         h = ct.c_void_p()
         rc = L.ufe_mesh_create(ct.byref(d), ct.byref(h))
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_mesh_create")
-        self._h = h
-        self._keep = None  # the library copied everything it needs
+        self._h = h   # the library copied everything it needs from ``keep``
 
     @property
     def handle(self):
@@ -148,25 +185,7 @@ class DeviceMesh:
 
     # ---------------------------------------------------------------- SSA
     def _ssa_structs(self, fields: dict, warm: dict | None):
-        keep = {}
-
-        def g(k, dt=np.float64):
-            v = fields.get(k)
-            if v is None:
-                return None
-            a = np.ascontiguousarray(v, dtype=dt)
-            keep[k] = a
-            return a.ctypes.data
-
-        ints = ("mask_sheet", "mask_gl_Ac")
-        si = nat.SsaIn(*(g(k, np.int32 if k in ints else np.float64) for k in nat.SSA_IN_FIELDS))
-        warm = warm or {}
-        io = {}
-        for k, n in (("U_SSA", self.nV), ("V_SSA", self.nV), ("Ux_SSA_Ac", self.nAc), ("Uy_SSA_Ac", self.nAc)):
-            io[k] = np.array(warm.get(k, np.zeros(n)), dtype=np.float64, copy=True)
-        io["N_AaAc"] = np.array(warm.get("N_AaAc", np.zeros(self.nVAaAc)), dtype=np.float64, copy=True)
-        sio = nat.SsaInout(*(io[k].ctypes.data for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")))
-        return si, sio, io, keep
+        return _ssa_structs(self.nV, self.nAc, self.nVAaAc, fields, warm)
 
     def solve_ssa(self, fields: dict, params: dict, warm: dict | None = None, check: bool = True):
         """solve_SSA. Returns (status, outputs, stats). Outputs hold the solution U_SSA, V_SSA,
@@ -205,12 +224,7 @@ class DeviceMesh:
 
     def ssa_download(self):
         L = nat.load()
-        io = {k: np.zeros(self.nV) for k in ("U_SSA", "V_SSA")}
-        io.update({k: np.zeros(self.nAc) for k in ("Ux_SSA_Ac", "Uy_SSA_Ac", "Up_SSA_Ac", "Uo_SSA_Ac")})
-        io.update({k: np.zeros(self.nVAaAc) for k in ("N_AaAc", "eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")})
-        sio = nat.SsaInout(*(io[k].ctypes.data for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")))
-        so = nat.SsaOut(*(io[k].ctypes.data for k in ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc", "tau_c_AaAc",
-                                                       "phi_fric_AaAc")))
+        io, sio, so = _download_structs(self.nV, self.nAc, self.nVAaAc)
         rc = L.ufe_ssa_download(self._h, ct.byref(sio), ct.byref(so))
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_ssa_download")
@@ -246,3 +260,69 @@ def stats_dict(st) -> dict:
                 resets=st.resets, not_converged=st.not_converged, total_sweeps=st.total_sweeps,
                 last_RN=st.last_RN, last_max_residual=st.last_max_residual, sweeps=list(st.sweeps)[:n],
                 device_ms=st.device_ms)
+
+
+class Batch:
+    """A batched ensemble (ufe_batch_create): independent SSA solves on meshes of uneven
+    size, solved together in one persistent launch (replayed as a CUDA graph)."""
+
+    def __init__(self, meshes, team_ctas: int = 0, block: int = 0, use_graph: bool = True):
+        L = nat.load()
+        n = len(meshes)
+        descs = (nat.MeshDesc * n)()
+        keep = []
+        self.sizes = []
+        for i, m in enumerate(meshes):
+            d, k = _mesh_desc(m)
+            descs[i] = d
+            keep.append(k)
+            self.sizes.append((m.base.nV, m.nAc, m.nVAaAc))
+        cfg = nat.BatchConfig(team_ctas, block, 1 if use_graph else 0)
+        h = ct.c_void_p()
+        rc = L.ufe_batch_create(descs, n, ct.byref(cfg), ct.byref(h))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_batch_create")
+        self._h = h
+        self.n = n
+
+    def upload(self, i: int, fields: dict, params: dict, warm: dict | None = None):
+        L = nat.load()
+        si, sio, io, keep = _ssa_structs(*self.sizes[i], fields, warm)
+        ps, _z = _params_struct(params)
+        rc = L.ufe_batch_upload(self._h, i, ct.byref(ps), ct.byref(si), ct.byref(sio))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_batch_upload")
+
+    def run(self, params: dict, check: bool = True):
+        """Solve every member. Returns (status, [stats per member], timing dict)."""
+        L = nat.load()
+        ps, _z = _params_struct(params)
+        st = (nat.SsaStats * self.n)()
+        member_ms = np.zeros(self.n)
+        tm = nat.BatchTiming()
+        tm.member_ms = member_ms.ctypes.data
+        rc = L.ufe_batch_run(self._h, ct.byref(ps), st, ct.byref(tm))
+        if check and rc < 0:
+            raise nat.UfeError(rc, "ufe_batch_run")
+        timing = {k: getattr(tm, k) for k, _ in nat.BatchTiming._fields_ if k != "member_ms"}
+        timing["member_ms"] = member_ms
+        return rc, [stats_dict(s) for s in st], timing
+
+    def download(self, i: int) -> dict:
+        L = nat.load()
+        io, sio, so = _download_structs(*self.sizes[i])
+        rc = L.ufe_batch_download(self._h, i, ct.byref(sio), ct.byref(so))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_batch_download")
+        return io
+
+    def close(self):
+        if getattr(self, "_h", None):
+            nat.load().ufe_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

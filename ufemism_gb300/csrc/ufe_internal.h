@@ -44,6 +44,8 @@ void neighbour_functions(double px, double py, int n, const double *qx, const do
                          bool edge, double *Nx, double *Ny, double *Nxx, double *Nxy,
                          double *Nyy);
 int aaac_build(const ufe_base_mesh *b, ufe_aaac_mesh *o, std::string *msg);
+// ufe_mesh_create with a chosen number of spatial patches (0: the single-solve default).
+int mesh_create(const ufe_mesh_desc *d, int n_patch, ufe_mesh_h *out);
 
 // Device re-layout of the combined AaAc mesh.
 //

@@ -44,7 +44,9 @@ void free_mesh(DevMesh &m) {
 
 using namespace ufe;
 
-extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
+namespace ufe {
+
+int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
   if (!d || !out) { set_error("ufe_mesh_create: null argument"); return UFE_BAD_ARG; }
   *out = nullptr;
   const int nV = d->nV, nAc = d->nAc, nA = d->nVAaAc, ncm = d->nC_mem;
@@ -134,7 +136,10 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   std::vector<int> order(nA);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
-  const int n_patch = std::max(1, std::min(kCtasPerSm * num_sms, nA / (kSsaBlock / 2)));
+  // Default: one patch per CTA of the single-solve grid, at least kSsaBlock / 2 rows each. A
+  // batched solve asks for its team size instead.
+  const int n_patch = n_patch_request > 0 ? std::min(n_patch_request, std::max(1, nA / kSlice))
+                                          : std::max(1, std::min(kCtasPerSm * num_sms, nA / (kSsaBlock / 2)));
   std::vector<int> patch_of(nA);
   std::vector<std::vector<std::vector<int>>> plist(n_patch, std::vector<std::vector<int>>(kGroups));
   for (int k = 0; k < nA; ++k) {
@@ -192,7 +197,7 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   m.max_patch_slices = max_patch_slices;
   m.n_edge_total = (int)edge_row.size();
   if (max_patch_slices > kMaxPatchSlices) {
-    set_error("ufe_mesh_create: mesh too large for one patch per SM (more than 1024 slices of 32 rows per patch)");
+    set_error("ufe_mesh_create: a patch would hold more than 1024 slices of 32 rows (too few patches for this mesh)");
     return UFE_BAD_ARG;
   }
 
@@ -366,6 +371,10 @@ extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) {
   *out = h;
   return UFE_OK;
 }
+
+}  // namespace ufe
+
+extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) { return mesh_create(d, 0, out); }
 
 extern "C" int ufe_mesh_destroy(ufe_mesh_h h) {
   if (!h) return UFE_OK;

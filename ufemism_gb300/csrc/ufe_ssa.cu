@@ -29,8 +29,11 @@
 // on FP64 differences u_j - u_i. Convergence norms (RN, max residual) are FP64.
 #include <cooperative_groups.h>
 
+#include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <numeric>
 #include <vector>
 
 #include "ufe_internal.h"
@@ -642,7 +645,8 @@ __device__ __forceinline__ void publish_progress(const SsaArgs &a, const Team &t
 
 // Wait until every patch this patch synchronises with has completed `target` colour phases.
 // Bounded: after timeout_ns the CTA records UFE_TIMEOUT (the next grid barrier then fails).
-__device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSmem &ps, unsigned int target) {
+__device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSmem &ps, unsigned int target,
+                                                unsigned int *team_bar) {
   if (threadIdx.x < ps.nsync) {
     const unsigned int *q = a.prog + 32 * ps.sync[threadIdx.x];
     unsigned int v = ld_acquire_u32(q);
@@ -656,7 +660,7 @@ __device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSme
         if ((int)(v - target) >= 0) break;
         if ((long long)(globaltimer_ns() - t0) > a.timeout_ns) {
           atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
-          atomicOr(&a.ctl->bar_count, kBarrierError);
+          atomicOr(team_bar, kBarrierError);
           break;
         }
       }
@@ -729,7 +733,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
       if (leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
       unsigned long long mx = 0ull;
       for (int g = 0; g < 5; ++g) {
-        if (g > 0) wait_neighbours(a, ps, phases);
+        if (g > 0) wait_neighbours(a, ps, phases, t.bar());
         unsigned long long m;
         if (kMode == kExact64) m = phase_sweep_exact(a, ps, g);
         else if (kMode == kFast64) m = phase_sweep_fast(a, ps, g);
@@ -739,7 +743,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         publish_progress(a, t, phases);
       }
       block_max_to(&ctl->maxres[slot], mx);
-      wait_neighbours(a, ps, phases);
+      wait_neighbours(a, ps, phases, t.bar());
       phase_boundary<kM>(a, ps);
       UFE_GRID_SYNC();
       maxres = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxres[slot]);
@@ -808,22 +812,23 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(const Ss
 }
 
 // Ensemble of independent solves in one launch: the grid is cut into teams of team_size
-// CTAs; each team takes the next member from a queue (members sorted by expected cost,
-// largest first) and solves it with its own barriers, until the queue is empty.
+// CTAs; each team takes the next member from a queue (members ordered by expected cost,
+// largest first) and solves it with its own barriers, until the queue is empty. Every
+// member's mesh has exactly team_size patches.
 struct BatchArgs {
-  const SsaArgs *members;        // [n_members], device
+  const SsaArgs *members;        // [n_members] in queue order, device
   int n_members;
   int team_size;
-  unsigned int *queue;           // next member index
+  unsigned int *queue;           // next queue position
   unsigned int *team_bar;        // [n_teams * 32] barrier counters
-  unsigned int *team_member;     // [n_teams * 32] member being solved
-  unsigned long long *times;     // [n_members * 2] start / end (ns, globaltimer)
-  int *err;
+  unsigned int *team_member;     // [n_teams * 32] queue position being solved
+  unsigned long long *times;     // [n_members * 2] start / end (globaltimer ns) by queue position
+  int *err;                      // first failure of any team
   long long timeout_ns;
 };
 
-template <int kMode>
-__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_batched(const BatchArgs b) {
+template <int kMode, int kBlock, int kPerSm>
+__global__ void __launch_bounds__(kBlock, kPerSm) ssa_batched(const BatchArgs b) {
   __shared__ SsaArgs a;
   const int team = blockIdx.x / b.team_size;
   SubTeam t{(int)(blockIdx.x % b.team_size), b.team_size, b.team_bar + 32 * team, 0u};
@@ -837,7 +842,10 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_batched(const Batch
     const unsigned int m = *(volatile unsigned int *)&b.team_member[32 * team];
     if (m >= (unsigned)b.n_members) return;
     stage_args(a, b.members + m);
-    if (!solve_member<kMode>(a, t)) return;
+    if (!solve_member<kMode>(a, t)) {
+      if (threadIdx.x == 0) atomicCAS(b.err, 0, (int)UFE_TIMEOUT);
+      return;
+    }
     if (t.rank() == 0 && threadIdx.x == 0) b.times[2 * m + 1] = globaltimer_ns();
   }
 }
@@ -1361,4 +1369,320 @@ extern "C" int ufe_ssa_solve(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in
   rc = ufe_ssa_download(h, io, out);
   if (rc < 0) return rc;
   return status;
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched ensemble: many independent solves in one persistent launch (no counterpart in
+// the reference, whose model runs one solve_SSA per time step).
+// ---------------------------------------------------------------------------------------
+struct ufe_batch_s {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int n = 0;                          // members
+  int team = 0;                       // CTAs per member (= patches of every member mesh)
+  int block = 0;                      // threads per CTA of the batched kernel
+  bool use_graph = true;
+  std::vector<ufe_mesh_h> members;    // owned
+  std::vector<double> cost;           // expected relative cost of each member
+  std::vector<int> order;             // queue position -> member (active members only)
+  SsaArgs *args_host = nullptr;       // pinned, [n] by queue position
+  SsaArgs *args_dev = nullptr;
+  unsigned int *sched = nullptr;      // queue (32 words), team_bar, team_member
+  int max_teams = 0;
+  unsigned long long *times_dev = nullptr, *times_host = nullptr;   // [2n]
+  int *err_dev = nullptr, *err_host = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ufe_params graph_params{};          // what the graph was captured for
+  std::vector<uint8_t> graph_flags;   // per member: uploaded state the graph depends on
+};
+
+namespace ufe {
+namespace {
+
+void batch_free(ufe_batch_s *b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (ufe_mesh_h h : b->members)
+    if (h) ufe_mesh_destroy(h);
+  if (b->args_host) cudaFreeHost(b->args_host);
+  if (b->times_host) cudaFreeHost(b->times_host);
+  if (b->err_host) cudaFreeHost(b->err_host);
+  void *ptrs[] = {b->args_dev, b->sched, b->times_dev, b->err_dev};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+// The batched kernel for a sweep mode and CTA shape (nullptr: not built).
+const void *batched_kernel(int mode, int block) {
+  switch (mode * 10000 + block) {
+    case kExact64 * 10000 + 1024: return (const void *)ssa_batched<kExact64, 1024, 1>;
+    case kFast64 * 10000 + 1024: return (const void *)ssa_batched<kFast64, 1024, 1>;
+    case kFast64 * 10000 + 512: return (const void *)ssa_batched<kFast64, 512, 2>;
+    case kFast64 * 10000 + 256: return (const void *)ssa_batched<kFast64, 256, 4>;
+    case kMixed * 10000 + 1024: return (const void *)ssa_batched<kMixed, 1024, 1>;
+    case kMixed * 10000 + 512: return (const void *)ssa_batched<kMixed, 512, 2>;
+    case kMixed * 10000 + 256: return (const void *)ssa_batched<kMixed, 256, 4>;
+    default: return nullptr;
+  }
+}
+
+uint8_t member_flags(ufe_mesh_h h) {
+  const SsaWork *w = h->ssa;
+  if (!w) return 0;
+  return (uint8_t)(1 | (w->has_beta << 1) | (w->has_N << 2) | (w->gl << 3) | (w->zero << 4) | (w->uploaded << 5));
+}
+
+bool same_params(const ufe_params &a, const ufe_params &b) {
+  return a.SSA_RN_tol == b.SSA_RN_tol && a.SSA_max_outer_loops == b.SSA_max_outer_loops &&
+         a.SSA_max_residual_UV == b.SSA_max_residual_UV && a.SSA_SOR_omega == b.SSA_SOR_omega &&
+         a.SSA_max_inner_loops == b.SSA_max_inner_loops && a.m_enh_ssa == b.m_enh_ssa &&
+         a.sliding_law == b.sliding_law && a.beta_sq == b.beta_sq &&
+         a.use_analytical_GL_flux == b.use_analytical_GL_flux && a.zero_velocities == b.zero_velocities &&
+         a.precision == b.precision && a.mixed_refold_sweeps == b.mixed_refold_sweeps &&
+         a.fp64_exact == b.fp64_exact && a.mixed_fp32_viscosity == b.mixed_fp32_viscosity;
+}
+
+// Enqueue one whole batch on b->stream: per member gather (and GL flux), the persistent
+// batched solve over the active members, per member scatter and control-block read-back.
+int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
+  cudaStream_t s = b->stream;
+  b->order.clear();
+  int rc = UFE_OK;
+  std::vector<int> by_cost(b->n);
+  std::iota(by_cost.begin(), by_cost.end(), 0);
+  std::stable_sort(by_cost.begin(), by_cost.end(), [&](int x, int y) { return b->cost[x] > b->cost[y]; });
+  for (int k = 0; k < b->n && !rc; ++k) {
+    const int m = by_cost[k];
+    bool solve = false;
+    SsaArgs a;
+    rc = launch_prepare(b->members[m], p, s, &a, &solve);
+    if (!rc && solve) {
+      b->args_host[b->order.size()] = a;
+      b->order.push_back(m);
+    }
+  }
+  const int n_active = (int)b->order.size();
+  const void *fn = batched_kernel(mode, b->block);
+  if (!rc && n_active > 0) {
+    const int n_teams = std::min(n_active, b->max_teams);
+    unsigned int *queue = b->sched, *team_bar = b->sched + 32, *team_member = team_bar + 32 * (size_t)b->max_teams;
+    rc = cuda_status(cudaMemsetAsync(b->sched, 0, (32 + 64 * (size_t)b->max_teams) * sizeof(unsigned int), s), "memset sched");
+    if (!rc) rc = cuda_status(cudaMemsetAsync(b->err_dev, 0, sizeof(int), s), "memset err");
+    if (!rc) rc = cuda_status(cudaMemsetAsync(b->times_dev, 0, 2 * (size_t)b->n * sizeof(unsigned long long), s), "memset times");
+    if (!rc)
+      rc = cuda_status(cudaMemcpyAsync(b->args_dev, b->args_host, (size_t)n_active * sizeof(SsaArgs),
+                                       cudaMemcpyHostToDevice, s), "args H2D");
+    BatchArgs ba;
+    ba.members = b->args_dev; ba.n_members = n_active; ba.team_size = b->team;
+    ba.queue = queue; ba.team_bar = team_bar; ba.team_member = team_member;
+    ba.times = b->times_dev; ba.err = b->err_dev; ba.timeout_ns = 20LL * 1000 * 1000 * 1000;
+    if (!rc) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)(n_teams * b->team));
+      cfg.blockDim = dim3((unsigned)b->block);
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeCooperative;
+      attr[0].val.cooperative = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      void *kargs[] = {(void *)&ba};
+      rc = cuda_status(cudaLaunchKernelExC(&cfg, fn, kargs), "ssa_batched");
+    }
+  }
+  for (int m = 0; m < b->n && !rc; ++m) rc = launch_finish(b->members[m], s);
+  if (!rc)
+    rc = cuda_status(cudaMemcpyAsync(b->times_host, b->times_dev, 2 * (size_t)b->n * sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToHost, s), "times D2H");
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(b->err_host, b->err_dev, sizeof(int), cudaMemcpyDeviceToHost, s), "err D2H");
+  return rc;
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_batch_create(const ufe_mesh_desc *descs, int32_t n, const ufe_batch_config *cfg,
+                                ufe_batch_h *out) {
+  if (!descs || !out || n < 1) { set_error("ufe_batch_create: null argument or no members"); return UFE_BAD_ARG; }
+  *out = nullptr;
+  int team = cfg ? cfg->team_ctas : 0;
+  const int block = cfg && cfg->block ? cfg->block : 1024;
+  if (block != 1024 && block != 512 && block != 256) {
+    set_error("ufe_batch_create: block must be 1024, 512 or 256 threads");
+    return UFE_BAD_ARG;
+  }
+  if (team < 0) { set_error("ufe_batch_create: team_ctas must be >= 0"); return UFE_BAD_ARG; }
+  int max_nA = 0;
+  for (int k = 0; k < n; ++k) max_nA = std::max(max_nA, descs[k].nVAaAc);
+  // Default team: the fewest CTAs per member that keep every patch at <= 3/4 of the
+  // per-CTA slice table (the rest is padding headroom).
+  if (team == 0) team = std::max(1, (max_nA + (kMaxPatchSlices * kSlice * 3 / 4) - 1) / (kMaxPatchSlices * kSlice * 3 / 4));
+  ufe_batch_s *b = new ufe_batch_s();
+  b->n = n; b->team = team; b->block = block; b->use_graph = !cfg || cfg->use_graph != 0;
+  int rc = cuda_status(cudaGetDevice(&b->device), "cudaGetDevice");
+  if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device), "SM count");
+  if (!rc) rc = cuda_status(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  b->members.assign(n, nullptr);
+  b->cost.assign(n, 0.0);
+  for (int k = 0; k < n && !rc; ++k) {
+    rc = mesh_create(descs + k, team, &b->members[k]);
+    if (!rc && b->members[k]->m.n_patch != team) {
+      char buf[160];
+      std::snprintf(buf, sizeof buf, "ufe_batch_create: member %d has too few rows for %d patches", k, team);
+      set_error(buf);
+      rc = UFE_BAD_ARG;
+    }
+    if (rc == UFE_BAD_MESH) {
+      const std::string e = ufe_last_error_string();
+      set_error("ufe_batch_create: member " + std::to_string(k) + ": " + e);
+    }
+    // Expected cost: rows x sweeps, the sweep count of SOR growing like the square root of the rows.
+    if (!rc) b->cost[k] = (double)descs[k].nVAaAc * std::sqrt((double)descs[k].nVAaAc);
+  }
+  // Co-resident CTAs of the batched kernel: every mode's variant of this block size.
+  int per_sm = 1 << 30;
+  for (int mode = 0; mode < 3 && !rc; ++mode) {
+    const void *fn = batched_kernel(mode, block);
+    if (!fn) continue;
+    int q = 0;
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, fn, block, 0), "occupancy");
+    per_sm = std::min(per_sm, q);
+  }
+  if (!rc) {
+    b->max_teams = per_sm * b->num_sms / team;
+    if (b->max_teams < 1) {
+      set_error("ufe_batch_create: team_ctas exceeds the co-resident CTAs of the device");
+      rc = UFE_BAD_ARG;
+    }
+  }
+  if (!rc) rc = cuda_status(cudaMallocHost(&b->args_host, (size_t)n * sizeof(SsaArgs)), "batch args host");
+  if (!rc) rc = cuda_status(cudaMalloc(&b->args_dev, (size_t)n * sizeof(SsaArgs)), "batch args");
+  if (!rc) rc = cuda_status(cudaMalloc(&b->sched, (32 + 64 * (size_t)b->max_teams) * sizeof(unsigned int)), "batch sched");
+  if (!rc) rc = cuda_status(cudaMalloc(&b->times_dev, 2 * (size_t)n * sizeof(unsigned long long)), "batch times");
+  if (!rc) rc = cuda_status(cudaMallocHost(&b->times_host, 2 * (size_t)n * sizeof(unsigned long long)), "batch times host");
+  if (!rc) rc = cuda_status(cudaMalloc(&b->err_dev, sizeof(int)), "batch err");
+  if (!rc) rc = cuda_status(cudaMallocHost(&b->err_host, sizeof(int)), "batch err host");
+  if (!rc) rc = cuda_status(cudaEventCreate(&b->ev0), "event");
+  if (!rc) rc = cuda_status(cudaEventCreate(&b->ev1), "event");
+  if (rc) { batch_free(b); return rc; }
+  *out = b;
+  return UFE_OK;
+}
+
+extern "C" int ufe_batch_destroy(ufe_batch_h b) {
+  if (!b) return UFE_BAD_ARG;
+  cudaStreamSynchronize(b->stream);
+  batch_free(b);
+  return UFE_OK;
+}
+
+extern "C" int ufe_batch_upload(ufe_batch_h b, int32_t member, const ufe_params *p, const ufe_ssa_in *in,
+                                const ufe_ssa_inout *io) {
+  if (!b || member < 0 || member >= b->n) { set_error("ufe_batch_upload: bad batch or member index"); return UFE_BAD_ARG; }
+  ufe_mesh_h h = b->members[member];
+  int rc = ufe_ssa_upload(h, p, in, io);
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(h->stream), "batch upload");
+  return rc;
+}
+
+extern "C" int ufe_batch_download(ufe_batch_h b, int32_t member, ufe_ssa_inout *io, ufe_ssa_out *out) {
+  if (!b || member < 0 || member >= b->n) { set_error("ufe_batch_download: bad batch or member index"); return UFE_BAD_ARG; }
+  return ufe_ssa_download(b->members[member], io, out);
+}
+
+extern "C" int ufe_batch_run(ufe_batch_h b, const ufe_params *p, ufe_ssa_stats *stats, ufe_batch_timing *timing) {
+  if (!b || !p) { set_error("ufe_batch_run: null argument"); return UFE_BAD_ARG; }
+  int rc = check_params(p, "ufe_batch_run");
+  if (rc) return rc;
+  for (int m = 0; m < b->n; ++m)
+    if (!b->members[m]->ssa || !b->members[m]->ssa->uploaded) {
+      set_error("ufe_batch_run: member " + std::to_string(m) + " has no uploaded inputs");
+      return UFE_BAD_ARG;
+    }
+  const int mode = sweep_mode(p);
+  if (!batched_kernel(mode, b->block)) {
+    set_error("ufe_batch_run: the exact FP64 mode is built for 1024-thread CTAs only");
+    return UFE_BAD_ARG;
+  }
+  cudaStream_t s = b->stream;
+  for (int m = 0; m < b->n; ++m) std::memset(b->members[m]->ssa->ctl_host, 0, sizeof(SsaCtl));
+  *b->err_host = 0;
+  if (b->use_graph) {
+    // Capture once per parameter set and upload state; replays re-run every step, including
+    // the gathers of the current uploaded inputs.
+    std::vector<uint8_t> flags(b->n);
+    for (int m = 0; m < b->n; ++m) flags[m] = member_flags(b->members[m]);
+    if (!b->exec || !same_params(b->graph_params, *p) || flags != b->graph_flags) {
+      if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+      if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+      rc = cuda_status(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+      if (!rc) {
+        const int rc_enq = batch_enqueue(b, p, mode);
+        const int rc_end = cuda_status(cudaStreamEndCapture(s, &b->graph), "end capture");
+        rc = rc_enq ? rc_enq : rc_end;
+      }
+      if (!rc) rc = cuda_status(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+      if (rc) return rc;
+      b->graph_params = *p;
+      b->graph_flags = flags;
+    }
+    rc = cuda_status(cudaEventRecord(b->ev0, s), "event");
+    if (!rc) rc = cuda_status(cudaGraphLaunch(b->exec, s), "graph launch");
+  } else {
+    rc = cuda_status(cudaEventRecord(b->ev0, s), "event");
+    if (!rc) rc = batch_enqueue(b, p, mode);
+  }
+  if (!rc) rc = cuda_status(cudaEventRecord(b->ev1, s), "event");
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "batch solve");
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  int worst = UFE_OK;
+  for (int m = 0; m < b->n; ++m) {
+    const int st = stats_of(*b->members[m]->ssa->ctl_host, stats ? stats + m : nullptr, ms);
+    if (st < 0 && (worst >= 0 || st < worst)) worst = st;
+    else if (worst >= 0 && st > worst) worst = st;
+  }
+  if (*b->err_host && worst >= 0) {
+    worst = *b->err_host;
+    set_error("ufe_batch_run: a device-side bounded wait timed out");
+  }
+  if (timing) {
+    const int n_active = (int)b->order.size();
+    std::vector<double> dur;
+    unsigned long long t0 = ~0ull, t1 = 0ull;
+    for (int q = 0; q < n_active; ++q) {
+      const unsigned long long a = b->times_host[2 * q], e = b->times_host[2 * q + 1];
+      if (e > a) {
+        dur.push_back(1e-6 * (double)(e - a));
+        t0 = std::min(t0, a);
+        t1 = std::max(t1, e);
+      }
+      if (timing->member_ms && e > a) timing->member_ms[b->order[q]] = 1e-6 * (double)(e - a);
+    }
+    std::sort(dur.begin(), dur.end());
+    auto pct = [&](double f) {   // nearest-rank percentile
+      if (dur.empty()) return 0.0;
+      const long r = (long)std::ceil(f * (double)dur.size()) - 1;
+      return dur[(size_t)std::min<long>((long)dur.size() - 1, std::max<long>(0, r))];
+    };
+    timing->device_ms = ms;
+    timing->solve_ms = t1 > t0 ? 1e-6 * (double)(t1 - t0) : 0.0;
+    timing->member_p50_ms = pct(0.5);
+    timing->member_p99_ms = pct(0.99);
+    timing->member_max_ms = dur.empty() ? 0.0 : dur.back();
+    timing->n_active = n_active;
+    timing->n_teams = std::min(n_active, b->max_teams);
+    timing->team_ctas = b->team;
+    timing->block = b->block;
+  }
+  return worst;
 }

@@ -131,3 +131,24 @@ def prepare_inputs(mesh, Hi, Hb, SL, A=A_FLOW, nZ=15):
     sia = dict(mask_sheet_Ac=sheet_Ac.astype(np.int32), Hi_Ac=Hi_Ac, dHs_dx_Ac=dHs_dx_Ac, dHs_dy_Ac=dHs_dy_Ac,
                dHs_dp_Ac=dHs_dp_Ac, dHs_do_Ac=dHs_do_Ac, A_flow_Ac=np.full((mesh.nAc, nZ), A, order="F"))
     return ssa, sia
+
+
+def ensemble_sizes(n_members, seed=20261210, lo=2000, hi=50000):
+    """Vertex counts drawn log-uniformly from [lo, hi]."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_members)).astype(np.int64)
+
+
+def ensemble_member(n_vertices, seed):
+    """One member of a friction/geometry ensemble: a mesh of about ``n_vertices`` vertices,
+    a dome with H0 drawn uniformly from [2000, 4000] m, and log(beta^2) a Gaussian random
+    field (mean ln 1e3, std 1.0, correlation length 100 km). Returns (base, mesh, ssa)."""
+    from . import api
+    from .meshgen import sized_mesh
+    base = sized_mesh(int(n_vertices), int(seed))
+    mesh = api.build_aaac(base)
+    H0 = np.random.default_rng(int(seed)).uniform(2000.0, 4000.0)
+    Hi, Hb, SL = dome_geometry(base, H0=H0)
+    ssa, _ = prepare_inputs(mesh, Hi, Hb, SL)
+    ssa["beta_sq_AaAc"] = np.exp(log_beta_field(mesh, std=1.0, ell=100e3, seed=int(seed) + 1))
+    return base, mesh, ssa
