@@ -276,6 +276,126 @@ def profile_case(args):
     return 0
 
 
+def ensemble_bench(args):
+    """Batched ensemble: ``--members`` independent mixed-precision SSA solves on meshes of
+    2k-50k vertices (log-uniform), dome thickness with H0 in [2000, 4000] m and a log-normal
+    friction field per member, solved in one persistent launch (CUDA graph replay) and
+    compared with a loop of single solves of the same members. Under torchrun every rank
+    solves its share of the members (greedy cost partition); value = all members / the
+    slowest rank's time."""
+    from ufemism_gb300 import ensemble as ens
+    from ufemism_gb300 import workloads as wl
+    rank, world, local = dist_info()
+    sizes = wl.ensemble_sizes(args.members)
+    parts = ens.partition(ens.member_cost(4 * sizes), world)
+    mine = parts[rank]
+    t_build = time.time()
+    members = ens.build_members(sizes[mine], [ens.member_seed(i) for i in mine])
+    t_build = time.time() - t_build
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api
+    api.init(local)
+    p = api.default_params(precision=nat.UFE_MIXED)
+    tuned = None
+    if args.autotune:
+        cfg, tried = api.batch_autotune(members, p)
+        tuned = {"best": cfg, "tried": tried}
+    else:
+        cfg = dict(team_ctas=0, rows_per_cta=args.rows_per_cta, block=args.block, use_graph=1)
+    b = api.Batch([m for _, m, _ in members], team_ctas=cfg["team_ctas"], rows_per_cta=cfg["rows_per_cta"],
+                  block=cfg["block"], use_graph=True)
+    for i, (_, _, f) in enumerate(members):
+        b.upload(i, f, p)
+    for _ in range(args.warmup):
+        b.run(p)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = []
+        for _ in range(args.steps):
+            rc, stats, tm = b.run(p)
+            ms.append(tm["device_ms"])
+    clocks = clk.summary()
+    batch_ms = float(np.mean(ms))
+    # e2e: every step uploads each member's inputs from host arrays, solves the batch and
+    # downloads each member's results
+    h2d = d2h = 0
+    for base, mesh, f in members:
+        h2d += sum(np.asarray(v).nbytes for k, v in f.items() if v is not None and k in nat.SSA_IN_FIELDS)
+        h2d += 8 * (2 * base.nV + 2 * mesh.nAc + mesh.nVAaAc)
+        d2h += 8 * (2 * base.nV + 4 * mesh.nAc + 5 * mesh.nVAaAc)
+    e2e = []
+    for i in range(1 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, (_, _, f) in enumerate(members):
+            b.upload(k, f, p)
+        b.run(p)
+        for k in range(len(members)):
+            b.download(k)
+        if i >= 1:
+            e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = float(np.mean(e2e))
+    # the same members as a loop of single solves (each on its own default layout)
+    single_ms = []
+    single_sweeps = []
+    for base, mesh, f in members:
+        dm = api.DeviceMesh(mesh)
+        dm.ssa_upload(f, p)
+        dm.ssa_run(p)
+        rc1, st1 = dm.ssa_run(p)
+        single_ms.append(st1["device_ms"])
+        single_sweeps.append(st1["total_sweeps"])
+        dm.close()
+    loop_ms = float(np.sum(single_ms))
+    same = all(s["total_sweeps"] == q for s, q in zip(stats, single_sweeps))
+    b.close()
+    vals = torch.tensor([batch_ms, loop_ms, e2e_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(vals, op=torch.distributed.ReduceOp.MAX)
+    batch_ms, loop_ms, e2e_ms = (float(x) for x in vals.tolist())
+    n_total = int(args.members)
+    sm = np.sort(single_ms)
+    line = {
+        "metric": "SSA ensemble solves/s (batched, mixed)", "value": 1e3 * n_total / batch_ms, "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 sweeps / f64 defect",
+        "data": "synthetic (seeded meshes, dome thickness, log-normal friction)",
+        "config": {"workload": "ensemble of %d dome solves, 2k-50k vertices log-uniform, H0 U[2000,4000] m, "
+                               "log beta^2 GRF(ln 1e3, 1.0, 100 km)" % n_total,
+                   "batch_config": cfg, "autotuned_this_run": bool(args.autotune),
+                   "members_on_rank0": len(mine), "total_vertices": int(np.sum(sizes)),
+                   "l2": "members' arrays together exceed L2; no flush",
+                   "parallelism": "members sharded over ranks" if world > 1 else "1 GPU"},
+        "member_p50_ms": tm["member_p50_ms"], "member_p99_ms": tm["member_p99_ms"],
+        "member_max_ms": tm["member_max_ms"], "grid_ctas": tm["grid_ctas"], "n_classes": tm["n_classes"],
+        "loop_of_single_solves": {"value": 1e3 * n_total / loop_ms, "unit": "solves/s", "total_ms": loop_ms,
+                                  "p50_ms": float(sm[len(sm) // 2]),
+                                  "p99_ms": float(sm[min(len(sm) - 1, int(np.ceil(0.99 * len(sm))) - 1)])},
+        "batched_vs_loop_speedup": loop_ms / batch_ms,
+        "iteration_counts_match_single_solves": bool(same),
+        "e2e": {"value": 1e3 * n_total / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        # per member k_gather + k_scatter, and the one persistent batched launch
+        "gpu_launches": (2 * len(members) + 1) * args.steps,
+        "clocks": clocks,
+        "host_build_s": t_build,
+    }
+    if tuned:
+        line["autotune"] = tuned["tried"]
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-case", choices=["mixed", "fp64", "exact"], default=None,
@@ -288,11 +408,19 @@ def main():
     ap.add_argument("--size", default="200k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sample-sweeps", type=int, default=40)
+    ap.add_argument("--workload", default="dome", choices=["dome", "ensemble"],
+                    help="dome: the 200k-vertex single solve; ensemble: the batched ensemble")
+    ap.add_argument("--members", type=int, default=256)
+    ap.add_argument("--autotune", action="store_true", help="ensemble: run the autotuner first")
+    ap.add_argument("--rows-per-cta", type=int, default=8192)
+    ap.add_argument("--block", type=int, default=1024)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_case:
         return profile_case(args)
+    if args.workload == "ensemble":
+        return ensemble_bench(args)
 
     rank, world, local = dist_info()
     import torch

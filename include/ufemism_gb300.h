@@ -200,25 +200,38 @@ int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_s
 
 /* Batched ensemble (no counterpart in the reference, whose model runs one solve_SSA per
  * time step): many independent solves on meshes of uneven size (friction or rheology
- * ensembles) in one persistent cooperative launch. The grid is cut into teams of
- * team_ctas CTAs; every member mesh is laid out in exactly team_ctas spatial patches, and
- * each team takes the next member (largest expected cost first) from a device queue until
- * none is left. With use_graph the whole batch (gathers, the persistent solve, scatters)
- * is captured once per parameter set and replayed as a CUDA graph. Members share one
- * ufe_params; their inputs are uploaded one by one (the arrays of ufe_ssa_upload). */
+ * ensembles) in one persistent cooperative launch. The grid is cut into teams of CTAs; a
+ * member whose mesh is laid out in T spatial patches is solved by a team of T CTAs. Teams
+ * of one size form a class with its own device queue (largest expected cost first), and
+ * each class gets CTAs in proportion to its estimated work. With use_graph the whole batch
+ * (gathers, the persistent solve, scatters) is captured once per parameter set and upload
+ * state and replayed as a CUDA graph. Members share one ufe_params; their inputs are
+ * uploaded one by one (the arrays of ufe_ssa_upload). */
 typedef struct ufe_batch_s *ufe_batch_h;
 typedef struct ufe_batch_config {
-  int32_t team_ctas;   /* CTAs per member (0: the fewest that fit the largest member) */
-  int32_t block;       /* threads per CTA: 1024, 512 or 256 (0: 1024); 512 and 256 run 2 and 4 CTAs per SM */
-  int32_t use_graph;   /* 1: capture and replay the batch as a CUDA graph */
+  int32_t team_ctas;     /* > 0: every member solved by a team of this many CTAs */
+  int32_t rows_per_cta;  /* team_ctas == 0: member team = the power of two nearest above
+                            rows / rows_per_cta (0: 8192 rows) - the per-CTA packing */
+  int32_t block;         /* threads per CTA: 1024, 512 or 256 (0: 1024); 512 and 256 run 2 and 4 CTAs per SM */
+  int32_t use_graph;     /* 1: capture and replay the batch as a CUDA graph */
 } ufe_batch_config;
+typedef struct ufe_batch_plan_out {
+  int32_t n_classes;
+  int32_t class_team_ctas[16];  /* team size of each class, largest first */
+  int32_t class_teams[16];      /* teams of each class */
+  int32_t grid_ctas;            /* CTAs of the persistent launch */
+} ufe_batch_plan_out;
 typedef struct ufe_batch_timing {
   double device_ms;      /* the whole batch on the device (CUDA events) */
   double solve_ms;       /* first member start to last member end inside the persistent kernel */
   double member_p50_ms, member_p99_ms, member_max_ms;  /* per-member solve time (team start to end) */
   double *member_ms;     /* (n_members) per-member solve time, or NULL */
-  int32_t n_active, n_teams, team_ctas, block;
+  int32_t n_active, n_teams, n_classes, grid_ctas, max_team_ctas, block;
 } ufe_batch_timing;
+/* The planner alone (host only): team size of every member from its row count (nVAaAc)
+ * and the classes' teams for `resident_ctas` co-resident CTAs. */
+int ufe_batch_plan(const int32_t *rows, int32_t n_members, const ufe_batch_config *config,
+                   int32_t resident_ctas, int32_t *team_ctas_of_member, ufe_batch_plan_out *plan);
 int ufe_batch_create(const ufe_mesh_desc *descs, int32_t n_members, const ufe_batch_config *config,
                      ufe_batch_h *out);
 int ufe_batch_destroy(ufe_batch_h batch);
@@ -227,6 +240,23 @@ int ufe_batch_upload(ufe_batch_h batch, int32_t member, const ufe_params *params
 /* stats: (n_members) or NULL. Returns the most severe member status. */
 int ufe_batch_run(ufe_batch_h batch, const ufe_params *params, ufe_ssa_stats *stats, ufe_batch_timing *timing);
 int ufe_batch_download(ufe_batch_h batch, int32_t member, ufe_ssa_inout *inout, ufe_ssa_out *out);
+/* Autotuner: times real batches of the given members over the per-CTA packing
+ * (rows_per_cta 4096..24576 at 1024-thread CTAs), then the CTA size (512, 256) at the best
+ * packing, then the neighbouring packings at the best CTA size, and returns the fastest
+ * configuration. log (capacity entries) receives one entry
+ * per candidate tried. Candidates that cannot hold the members are skipped. */
+typedef struct ufe_batch_tune_entry {
+  int32_t rows_per_cta, block, grid_ctas, n_classes;
+  double device_ms, member_p99_ms;
+} ufe_batch_tune_entry;
+int ufe_batch_autotune(int32_t n_members, const ufe_mesh_desc *descs, const ufe_params *params,
+                       const ufe_ssa_in *in, const ufe_ssa_inout *inout, ufe_batch_config *best,
+                       ufe_batch_tune_entry *log, int32_t log_capacity, int32_t *log_count);
+/* One call for a Fortran caller: create, upload, run, download and destroy. in, inout,
+ * out and stats are arrays of n_members (out and stats may be NULL). */
+int ufe_ssa_solve_batched(int32_t n_members, const ufe_mesh_desc *descs, const ufe_batch_config *config,
+                          const ufe_params *params, const ufe_ssa_in *in, ufe_ssa_inout *inout,
+                          ufe_ssa_out *out, ufe_ssa_stats *stats);
 
 /* Host-side mesh substrate: builds the Ac and combined AaAc mesh, the AaAc and Aa
  * neighbour functions and the five-colouring from a base triangulation, exactly as

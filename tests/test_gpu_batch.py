@@ -71,7 +71,7 @@ def test_batch_matches_single_solves(ensemble, precision):
         assert rc >= 0
         check_members(single, stats, outs)
         assert timing["n_active"] == len(ensemble)
-        assert timing["team_ctas"] == 4
+        assert timing["max_team_ctas"] == 4 and timing["n_classes"] == 1
         assert 0 < timing["member_p50_ms"] <= timing["member_p99_ms"] <= timing["member_max_ms"]
         assert np.all(timing["member_ms"] > 0)
         # graph replay: the same results again
@@ -84,17 +84,51 @@ def test_batch_matches_single_solves(ensemble, precision):
         b.close()
 
 
-@pytest.mark.parametrize("block,team,graph", [(512, 2, True), (256, 8, True), (1024, 1, False)])
-def test_batch_shapes(ensemble, block, team, graph):
+@pytest.mark.parametrize("block,team,rows,graph", [(512, 2, 0, True), (256, 8, 0, True), (1024, 1, 0, False),
+                                                   (1024, 0, 4096, True), (256, 0, 2048, True)])
+def test_batch_shapes(ensemble, block, team, rows, graph):
+    """Uniform teams (team > 0) and per-member team sizes from a rows-per-CTA packing."""
     single = single_results(ensemble, nat.UFE_MIXED)
-    b, p, rc, stats, timing, outs = run_batch(ensemble, nat.UFE_MIXED, team_ctas=team, block=block,
-                                              use_graph=graph)
+    b, p, rc, stats, timing, outs = run_batch(ensemble, nat.UFE_MIXED, team_ctas=team, rows_per_cta=rows,
+                                              block=block, use_graph=graph)
     try:
         assert rc >= 0
-        assert timing["block"] == block and timing["team_ctas"] == team
+        assert timing["block"] == block
+        if team:
+            assert timing["max_team_ctas"] == team and timing["n_classes"] == 1
+        else:
+            assert timing["n_classes"] >= 2
         check_members(single, stats, outs)
     finally:
         b.close()
+
+
+def test_solve_batched_one_call(ensemble):
+    """ufe_ssa_solve_batched (create, upload, run, download, destroy in one call)."""
+    import ctypes as ct
+    single = single_results(ensemble, nat.UFE_MIXED)
+    L = nat.load()
+    n = len(ensemble)
+    descs = (nat.MeshDesc * n)()
+    ins = (nat.SsaIn * n)()
+    ios = (nat.SsaInout * n)()
+    keep = []
+    outs = []
+    for i, (base, mesh, ssa) in enumerate(ensemble):
+        d, k = api._mesh_desc(mesh)
+        descs[i] = d
+        si, sio, io, kk = api._ssa_structs(base.nV, mesh.nAc, mesh.nVAaAc, ssa, None)
+        ins[i] = si
+        ios[i] = sio
+        keep += [k, kk]
+        outs.append(io)
+    p = api.default_params(precision=nat.UFE_MIXED)
+    ps, _z = api._params_struct(p)
+    st = (nat.SsaStats * n)()
+    cfg = nat.BatchConfig(0, 4096, 0, 1)
+    rc = L.ufe_ssa_solve_batched(n, descs, ct.byref(cfg), ct.byref(ps), ins, ios, None, st)
+    assert rc >= 0, nat.last_error()
+    check_members(single, [api.stats_dict(x) for x in st], outs)
 
 
 def test_batch_exact_fp64_bitwise(ensemble):
@@ -110,3 +144,12 @@ def test_batch_rejects_team_larger_than_member(ensemble):
     with pytest.raises(nat.UfeError) as e:
         api.Batch([ensemble[0][1]], team_ctas=400)
     assert e.value.status in (nat.UFE_BAD_ARG, nat.UFE_BAD_MESH)
+
+
+def test_autotune_picks_a_tried_candidate(ensemble):
+    p = api.default_params(precision=nat.UFE_MIXED)
+    best, tried = api.batch_autotune(ensemble, p)
+    assert len(tried) >= 3
+    fastest = min(tried, key=lambda e: e["device_ms"])
+    assert (best["rows_per_cta"], best["block"]) == (fastest["rows_per_cta"], fastest["block"])
+    assert all(e["device_ms"] > 0 for e in tried)

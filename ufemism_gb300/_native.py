@@ -76,13 +76,22 @@ class SiaOut(ct.Structure):
 
 
 class BatchConfig(ct.Structure):
-    _fields_ = [("team_ctas", I32), ("block", I32), ("use_graph", I32)]
+    _fields_ = [("team_ctas", I32), ("rows_per_cta", I32), ("block", I32), ("use_graph", I32)]
+
+
+class BatchPlan(ct.Structure):
+    _fields_ = [("n_classes", I32), ("class_team_ctas", I32 * 16), ("class_teams", I32 * 16), ("grid_ctas", I32)]
 
 
 class BatchTiming(ct.Structure):
     _fields_ = [("device_ms", F64), ("solve_ms", F64), ("member_p50_ms", F64), ("member_p99_ms", F64),
                 ("member_max_ms", F64), ("member_ms", P), ("n_active", I32), ("n_teams", I32),
-                ("team_ctas", I32), ("block", I32)]
+                ("n_classes", I32), ("grid_ctas", I32), ("max_team_ctas", I32), ("block", I32)]
+
+
+class BatchTuneEntry(ct.Structure):
+    _fields_ = [("rows_per_cta", I32), ("block", I32), ("grid_ctas", I32), ("n_classes", I32),
+                ("device_ms", F64), ("member_p99_ms", F64)]
 
 
 class BaseMeshC(ct.Structure):
@@ -113,6 +122,14 @@ PROTOTYPES = {
     "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_batch_plan": (I32, [ct.POINTER(I32), I32, ct.POINTER(BatchConfig), I32, ct.POINTER(I32),
+                             ct.POINTER(BatchPlan)]),
+    "ufe_ssa_solve_batched": (I32, [I32, ct.POINTER(MeshDesc), ct.POINTER(BatchConfig), ct.POINTER(Params),
+                                    ct.POINTER(SsaIn), ct.POINTER(SsaInout), ct.POINTER(SsaOut),
+                                    ct.POINTER(SsaStats)]),
+    "ufe_batch_autotune": (I32, [I32, ct.POINTER(MeshDesc), ct.POINTER(Params), ct.POINTER(SsaIn),
+                                 ct.POINTER(SsaInout), ct.POINTER(BatchConfig), ct.POINTER(BatchTuneEntry), I32,
+                                 ct.POINTER(I32)]),
     "ufe_batch_create": (I32, [ct.POINTER(MeshDesc), I32, ct.POINTER(BatchConfig), ct.POINTER(P)]),
     "ufe_batch_destroy": (I32, [P]),
     "ufe_batch_upload": (I32, [P, I32, ct.POINTER(Params), ct.POINTER(SsaIn), ct.POINTER(SsaInout)]),

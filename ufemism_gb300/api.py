@@ -266,7 +266,7 @@ class Batch:
     """A batched ensemble (ufe_batch_create): independent SSA solves on meshes of uneven
     size, solved together in one persistent launch (replayed as a CUDA graph)."""
 
-    def __init__(self, meshes, team_ctas: int = 0, block: int = 0, use_graph: bool = True):
+    def __init__(self, meshes, team_ctas: int = 0, rows_per_cta: int = 0, block: int = 0, use_graph: bool = True):
         L = nat.load()
         n = len(meshes)
         descs = (nat.MeshDesc * n)()
@@ -277,7 +277,7 @@ class Batch:
             descs[i] = d
             keep.append(k)
             self.sizes.append((m.base.nV, m.nAc, m.nVAaAc))
-        cfg = nat.BatchConfig(team_ctas, block, 1 if use_graph else 0)
+        cfg = nat.BatchConfig(team_ctas, rows_per_cta, block, 1 if use_graph else 0)
         h = ct.c_void_p()
         rc = L.ufe_batch_create(descs, n, ct.byref(cfg), ct.byref(h))
         if rc != nat.UFE_OK:
@@ -326,3 +326,44 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def batch_plan(rows, resident_ctas: int, team_ctas: int = 0, rows_per_cta: int = 0, block: int = 0):
+    """The ensemble planner (ufe_batch_plan, host only): (team size per member, classes as
+    [(team size, teams)], grid CTAs)."""
+    L = nat.load()
+    r = np.ascontiguousarray(rows, dtype=np.int32)
+    t = np.zeros(r.size, dtype=np.int32)
+    cfg = nat.BatchConfig(team_ctas, rows_per_cta, block, 1)
+    pl = nat.BatchPlan()
+    rc = L.ufe_batch_plan(r.ctypes.data_as(ct.POINTER(ct.c_int32)), r.size, ct.byref(cfg), resident_ctas,
+                          t.ctypes.data_as(ct.POINTER(ct.c_int32)), ct.byref(pl))
+    if rc != nat.UFE_OK:
+        raise nat.UfeError(rc, "ufe_batch_plan")
+    classes = [(pl.class_team_ctas[c], pl.class_teams[c]) for c in range(pl.n_classes)]
+    return t, classes, pl.grid_ctas
+
+
+def batch_autotune(members, params: dict):
+    """ufe_batch_autotune over (base, mesh, ssa_fields) members. Returns (best config dict,
+    list of tried candidates)."""
+    L = nat.load()
+    n = len(members)
+    descs = (nat.MeshDesc * n)()
+    ins = (nat.SsaIn * n)()
+    ios = (nat.SsaInout * n)()
+    keep = []
+    for i, (base, mesh, fields) in enumerate(members):
+        d, k = _mesh_desc(mesh)
+        si, sio, io, kk = _ssa_structs(base.nV, mesh.nAc, mesh.nVAaAc, fields, None)
+        descs[i], ins[i], ios[i] = d, si, sio
+        keep += [k, kk, io]
+    ps, _z = _params_struct(params)
+    best = nat.BatchConfig()
+    log = (nat.BatchTuneEntry * 32)()
+    cnt = ct.c_int32(0)
+    rc = L.ufe_batch_autotune(n, descs, ct.byref(ps), ins, ios, ct.byref(best), log, 32, ct.byref(cnt))
+    if rc != nat.UFE_OK:
+        raise nat.UfeError(rc, "ufe_batch_autotune")
+    tried = [{f: getattr(log[i], f) for f, _ in nat.BatchTuneEntry._fields_} for i in range(min(cnt.value, 32))]
+    return {f: getattr(best, f) for f, _ in nat.BatchConfig._fields_}, tried

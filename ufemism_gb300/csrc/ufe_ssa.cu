@@ -811,18 +811,20 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(const Ss
   solve_member<kMode>(a, t);
 }
 
-// Ensemble of independent solves in one launch: the grid is cut into teams of team_size
-// CTAs; each team takes the next member from a queue (members ordered by expected cost,
-// largest first) and solves it with its own barriers, until the queue is empty. Every
-// member's mesh has exactly team_size patches.
+// Ensemble of independent solves in one launch. The grid is cut into teams; a team of T
+// CTAs solves members whose meshes have T patches. Teams of one size form a class with
+// its own queue (members ordered by expected cost, largest first); each team takes the
+// next member of its class until the queue is empty.
 struct BatchArgs {
-  const SsaArgs *members;        // [n_members] in queue order, device
+  const SsaArgs *members;        // [n_members] grouped by class, device
   int n_members;
-  int team_size;
-  unsigned int *queue;           // next queue position
+  const int *team_of_cta;        // [grid]
+  const int4 *team_info;         // [n_teams] (first CTA, CTAs, class, -)
+  const int2 *class_range;       // [n_classes] queue positions [begin, end) in members
+  unsigned int *queue;           // [n_classes * 32] next position of each class (offset from begin)
   unsigned int *team_bar;        // [n_teams * 32] barrier counters
-  unsigned int *team_member;     // [n_teams * 32] queue position being solved
-  unsigned long long *times;     // [n_members * 2] start / end (globaltimer ns) by queue position
+  unsigned int *team_member;     // [n_teams * 32] position being solved
+  unsigned long long *times;     // [n_members * 2] start / end (globaltimer ns) by position
   int *err;                      // first failure of any team
   long long timeout_ns;
 };
@@ -830,11 +832,14 @@ struct BatchArgs {
 template <int kMode, int kBlock, int kPerSm>
 __global__ void __launch_bounds__(kBlock, kPerSm) ssa_batched(const BatchArgs b) {
   __shared__ SsaArgs a;
-  const int team = blockIdx.x / b.team_size;
-  SubTeam t{(int)(blockIdx.x % b.team_size), b.team_size, b.team_bar + 32 * team, 0u};
+  const int team = b.team_of_cta[blockIdx.x];
+  const int4 ti = b.team_info[team];
+  SubTeam t{(int)blockIdx.x - ti.x, ti.y, b.team_bar + 32 * team, 0u};
+  const int2 cr = b.class_range[ti.z];
   for (;;) {
     if (t.rank() == 0 && threadIdx.x == 0) {
-      const unsigned int m = atomicAdd(b.queue, 1u);
+      unsigned int m = (unsigned)cr.x + atomicAdd(b.queue + 32 * ti.z, 1u);
+      if (m >= (unsigned)cr.y) m = 0xffffffffu;
       b.team_member[32 * team] = m;
       if (m < (unsigned)b.n_members) b.times[2 * m] = globaltimer_ns();
     }
@@ -1371,25 +1376,133 @@ extern "C" int ufe_ssa_solve(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in
   return status;
 }
 
+
 // ---------------------------------------------------------------------------------------
 // Batched ensemble: many independent solves in one persistent launch (no counterpart in
 // the reference, whose model runs one solve_SSA per time step).
 // ---------------------------------------------------------------------------------------
+namespace ufe {
+namespace {
+
+constexpr int kMaxClasses = 16;
+constexpr int kDefaultRowsPerCta = 8192;
+// Largest rows per patch the planner allows: 3/4 of the per-CTA slice table (the rest is
+// headroom for the padding of the six row groups to multiples of 32).
+constexpr int kMaxRowsPerPatch = kMaxPatchSlices * kSlice * 3 / 4;
+
+int pow2_ceil(int x) { int p = 1; while (p < x) p <<= 1; return p; }
+int pow2_floor(int x) { int p = 1; while (2 * p <= x) p <<= 1; return p; }
+
+// Estimated CTA-microseconds of a member solved by T CTAs of `block` threads: sqrt(rows)
+// sweeps (the SOR count grows about like the mesh's linear resolution), each a latency
+// floor plus a per-row cost that scales with the rows of a CTA.
+double member_work(int rows, int T, int block) {
+  const double sweeps = std::sqrt((double)rows);
+  const double per_sweep_us = 20.0 + 0.0025 * (double)rows / T * (1024.0 / block);
+  return (double)T * sweeps * per_sweep_us;
+}
+
+int plan_batch(const int32_t *rows, int n, const ufe_batch_config &cfg, int resident, int32_t *team_of_member,
+               ufe_batch_plan_out *plan) {
+  const int block = cfg.block ? cfg.block : 1024;
+  if (resident < 1) { set_error("ufe_batch_plan: no co-resident CTAs"); return UFE_BAD_ARG; }
+  for (int m = 0; m < n; ++m) {
+    const int r = rows[m];
+    if (r < 32) { set_error("ufe_batch_plan: member " + std::to_string(m) + " has fewer than 32 rows"); return UFE_BAD_ARG; }
+    const int cap = std::min(resident, r / kSlice);           // patches of at least 32 rows
+    const int need = (r + kMaxRowsPerPatch - 1) / kMaxRowsPerPatch;
+    int T;
+    if (cfg.team_ctas > 0) {
+      T = cfg.team_ctas;
+    } else {
+      const int R = cfg.rows_per_cta > 0 ? cfg.rows_per_cta : kDefaultRowsPerCta;
+      // Powers of two up to half the resident CTAs: one team of every class always fits
+      // (1 + 2 + ... + 2^k = 2^(k+1) - 1).
+      T = pow2_ceil(std::max(need, (r + R - 1) / R));
+      T = std::min(T, pow2_floor(std::min(cap, (resident + 1) / 2)));
+    }
+    if (T > cap || T < need) {
+      char buf[200];
+      std::snprintf(buf, sizeof buf, "ufe_batch_plan: member %d (%d rows) cannot be cut into %d patches "
+                                     "(between %d and %d fit)", m, r, T, need, cap);
+      set_error(buf);
+      return UFE_BAD_ARG;
+    }
+    team_of_member[m] = T;
+  }
+  // Classes: distinct team sizes, largest first.
+  std::vector<int> sizes(team_of_member, team_of_member + n);
+  std::sort(sizes.begin(), sizes.end(), std::greater<int>());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  if ((int)sizes.size() > kMaxClasses) { set_error("ufe_batch_plan: too many team sizes"); return UFE_BAD_ARG; }
+  const int nc = (int)sizes.size();
+  std::vector<double> W(nc, 0.0);
+  std::vector<int> members(nc, 0), teams(nc, 0);
+  double Wt = 0.0;
+  for (int m = 0; m < n; ++m) {
+    const int c = (int)(std::find(sizes.begin(), sizes.end(), team_of_member[m]) - sizes.begin());
+    const double w = member_work(rows[m], team_of_member[m], block);
+    W[c] += w;
+    Wt += w;
+    members[c] += 1;
+  }
+  // CTAs to each class in proportion to its work, at least one team per class.
+  int used = 0;
+  for (int c = 0; c < nc; ++c) {
+    teams[c] = std::max(1, std::min(members[c], (int)std::floor(resident * W[c] / Wt / sizes[c])));
+    used += teams[c] * sizes[c];
+  }
+  while (used > resident) {   // over-subscribed: take a team from the most generously served class
+    int best = -1;
+    double r = -1.0;
+    for (int c = 0; c < nc; ++c)
+      if (teams[c] > 1 && teams[c] * sizes[c] / W[c] > r) { r = teams[c] * sizes[c] / W[c]; best = c; }
+    if (best < 0) { set_error("ufe_batch_plan: the team sizes need more CTAs than the device holds"); return UFE_BAD_ARG; }
+    teams[best] -= 1;
+    used -= sizes[best];
+  }
+  for (;;) {                  // spare CTAs: give a team to the least served class that can use it
+    int best = -1;
+    double r = 1e300;
+    for (int c = 0; c < nc; ++c)
+      if (teams[c] < members[c] && used + sizes[c] <= resident && teams[c] * sizes[c] / W[c] < r) {
+        r = teams[c] * sizes[c] / W[c];
+        best = c;
+      }
+    if (best < 0) break;
+    teams[best] += 1;
+    used += sizes[best];
+  }
+  std::memset(plan, 0, sizeof(*plan));
+  plan->n_classes = nc;
+  for (int c = 0; c < nc; ++c) { plan->class_team_ctas[c] = sizes[c]; plan->class_teams[c] = teams[c]; }
+  plan->grid_ctas = used;
+  return UFE_OK;
+}
+
+}  // namespace
+}  // namespace ufe
+
 struct ufe_batch_s {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   int n = 0;                          // members
-  int team = 0;                       // CTAs per member (= patches of every member mesh)
   int block = 0;                      // threads per CTA of the batched kernel
   bool use_graph = true;
+  ufe_batch_plan_out plan{};
+  int n_teams = 0;
+  std::vector<int32_t> team_of_member;
   std::vector<ufe_mesh_h> members;    // owned
   std::vector<double> cost;           // expected relative cost of each member
   std::vector<int> order;             // queue position -> member (active members only)
   SsaArgs *args_host = nullptr;       // pinned, [n] by queue position
   SsaArgs *args_dev = nullptr;
-  unsigned int *sched = nullptr;      // queue (32 words), team_bar, team_member
-  int max_teams = 0;
+  int *layout_host = nullptr;         // pinned: team_of_cta, team_info (int4), class_range (int2)
+  int *layout_dev = nullptr;
+  size_t layout_words = 0;
+  unsigned int *sched = nullptr;      // queues (32 words per class), team_bar, team_member
+  size_t sched_words = 0;
   unsigned long long *times_dev = nullptr, *times_host = nullptr;   // [2n]
   int *err_dev = nullptr, *err_host = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1408,11 +1521,11 @@ void batch_free(ufe_batch_s *b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (ufe_mesh_h h : b->members)
     if (h) ufe_mesh_destroy(h);
-  if (b->args_host) cudaFreeHost(b->args_host);
-  if (b->times_host) cudaFreeHost(b->times_host);
-  if (b->err_host) cudaFreeHost(b->err_host);
-  void *ptrs[] = {b->args_dev, b->sched, b->times_dev, b->err_dev};
-  for (void *p : ptrs)
+  void *host[] = {b->args_host, b->times_host, b->err_host, b->layout_host};
+  for (void *p : host)
+    if (p) cudaFreeHost(p);
+  void *dev[] = {b->args_dev, b->sched, b->times_dev, b->err_dev, b->layout_dev};
+  for (void *p : dev)
     if (p) cudaFree(p);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
@@ -1432,6 +1545,21 @@ const void *batched_kernel(int mode, int block) {
     case kMixed * 10000 + 256: return (const void *)ssa_batched<kMixed, 256, 4>;
     default: return nullptr;
   }
+}
+
+// Co-resident CTAs of the batched kernels of one CTA size (the smallest over the modes).
+int resident_ctas(int block, int num_sms, int *out) {
+  int per_sm = 1 << 30;
+  for (int mode = 0; mode < 3; ++mode) {
+    const void *fn = batched_kernel(mode, block);
+    if (!fn) continue;
+    int q = 0;
+    const int rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, fn, block, 0), "occupancy");
+    if (rc) return rc;
+    per_sm = std::min(per_sm, q);
+  }
+  *out = per_sm * num_sms;
+  return UFE_OK;
 }
 
 uint8_t member_flags(ufe_mesh_h h) {
@@ -1454,39 +1582,67 @@ bool same_params(const ufe_params &a, const ufe_params &b) {
 // batched solve over the active members, per member scatter and control-block read-back.
 int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
   cudaStream_t s = b->stream;
+  const ufe_batch_plan_out &pl = b->plan;
+  const int nc = pl.n_classes;
   b->order.clear();
   int rc = UFE_OK;
-  std::vector<int> by_cost(b->n);
-  std::iota(by_cost.begin(), by_cost.end(), 0);
-  std::stable_sort(by_cost.begin(), by_cost.end(), [&](int x, int y) { return b->cost[x] > b->cost[y]; });
+  // Queue order: by class (largest teams first), then by expected cost.
+  std::vector<int> by(b->n);
+  std::iota(by.begin(), by.end(), 0);
+  std::stable_sort(by.begin(), by.end(), [&](int x, int y) {
+    if (b->team_of_member[x] != b->team_of_member[y]) return b->team_of_member[x] > b->team_of_member[y];
+    return b->cost[x] > b->cost[y];
+  });
+  int *tc = b->layout_host;                                     // team_of_cta [grid]
+  int4 *ti = reinterpret_cast<int4 *>(tc + ((pl.grid_ctas + 3) & ~3));   // [n_teams]
+  int2 *cr = reinterpret_cast<int2 *>(ti + b->n_teams);         // [n_classes]
+  for (int c = 0; c < nc; ++c) cr[c] = make_int2(0, 0);
   for (int k = 0; k < b->n && !rc; ++k) {
-    const int m = by_cost[k];
+    const int m = by[k];
     bool solve = false;
     SsaArgs a;
     rc = launch_prepare(b->members[m], p, s, &a, &solve);
     if (!rc && solve) {
-      b->args_host[b->order.size()] = a;
+      const int c = (int)(std::find(pl.class_team_ctas, pl.class_team_ctas + nc, b->team_of_member[m]) -
+                          pl.class_team_ctas);
+      const int q = (int)b->order.size();
+      if (cr[c].y == cr[c].x) cr[c] = make_int2(q, q);
+      cr[c].y = q + 1;
+      b->args_host[q] = a;
       b->order.push_back(m);
     }
   }
   const int n_active = (int)b->order.size();
+  // Team layout: teams of class 0 first, CTAs of a team contiguous.
+  int team = 0, cta = 0;
+  for (int c = 0; c < nc; ++c)
+    for (int k = 0; k < pl.class_teams[c]; ++k, ++team) {
+      ti[team] = make_int4(cta, pl.class_team_ctas[c], c, 0);
+      for (int r = 0; r < pl.class_team_ctas[c]; ++r) tc[cta++] = team;
+    }
   const void *fn = batched_kernel(mode, b->block);
   if (!rc && n_active > 0) {
-    const int n_teams = std::min(n_active, b->max_teams);
-    unsigned int *queue = b->sched, *team_bar = b->sched + 32, *team_member = team_bar + 32 * (size_t)b->max_teams;
-    rc = cuda_status(cudaMemsetAsync(b->sched, 0, (32 + 64 * (size_t)b->max_teams) * sizeof(unsigned int), s), "memset sched");
+    unsigned int *queue = b->sched, *team_bar = queue + 32 * (size_t)kMaxClasses;
+    unsigned int *team_member = team_bar + 32 * (size_t)b->n_teams;
+    rc = cuda_status(cudaMemsetAsync(b->sched, 0, b->sched_words * sizeof(unsigned int), s), "memset sched");
     if (!rc) rc = cuda_status(cudaMemsetAsync(b->err_dev, 0, sizeof(int), s), "memset err");
     if (!rc) rc = cuda_status(cudaMemsetAsync(b->times_dev, 0, 2 * (size_t)b->n * sizeof(unsigned long long), s), "memset times");
     if (!rc)
       rc = cuda_status(cudaMemcpyAsync(b->args_dev, b->args_host, (size_t)n_active * sizeof(SsaArgs),
                                        cudaMemcpyHostToDevice, s), "args H2D");
+    if (!rc)
+      rc = cuda_status(cudaMemcpyAsync(b->layout_dev, b->layout_host, b->layout_words * sizeof(int),
+                                       cudaMemcpyHostToDevice, s), "layout H2D");
+    const int *tcd = b->layout_dev;
+    const int4 *tid = reinterpret_cast<const int4 *>(tcd + ((pl.grid_ctas + 3) & ~3));
     BatchArgs ba;
-    ba.members = b->args_dev; ba.n_members = n_active; ba.team_size = b->team;
+    ba.members = b->args_dev; ba.n_members = n_active;
+    ba.team_of_cta = tcd; ba.team_info = tid; ba.class_range = reinterpret_cast<const int2 *>(tid + b->n_teams);
     ba.queue = queue; ba.team_bar = team_bar; ba.team_member = team_member;
     ba.times = b->times_dev; ba.err = b->err_dev; ba.timeout_ns = 20LL * 1000 * 1000 * 1000;
     if (!rc) {
       cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3((unsigned)(n_teams * b->team));
+      cfg.gridDim = dim3((unsigned)pl.grid_ctas);
       cfg.blockDim = dim3((unsigned)b->block);
       cfg.stream = s;
       cudaLaunchAttribute attr[1];
@@ -1506,66 +1662,79 @@ int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
   return rc;
 }
 
+int check_block(const ufe_batch_config *cfg, int *block, const char *who) {
+  *block = cfg && cfg->block ? cfg->block : 1024;
+  if (*block != 1024 && *block != 512 && *block != 256) {
+    set_error(std::string(who) + ": block must be 1024, 512 or 256 threads");
+    return UFE_BAD_ARG;
+  }
+  if (cfg && (cfg->team_ctas < 0 || cfg->rows_per_cta < 0)) {
+    set_error(std::string(who) + ": team_ctas and rows_per_cta must be >= 0");
+    return UFE_BAD_ARG;
+  }
+  return UFE_OK;
+}
+
 }  // namespace
 }  // namespace ufe
+
+extern "C" int ufe_batch_plan(const int32_t *rows, int32_t n, const ufe_batch_config *cfg, int32_t resident,
+                              int32_t *team_ctas_of_member, ufe_batch_plan_out *plan) {
+  if (!rows || n < 1 || !team_ctas_of_member || !plan) { set_error("ufe_batch_plan: null argument"); return UFE_BAD_ARG; }
+  int block = 0;
+  int rc = check_block(cfg, &block, "ufe_batch_plan");
+  if (rc) return rc;
+  ufe_batch_config c = cfg ? *cfg : ufe_batch_config{};
+  c.block = block;
+  return plan_batch(rows, n, c, resident, team_ctas_of_member, plan);
+}
 
 extern "C" int ufe_batch_create(const ufe_mesh_desc *descs, int32_t n, const ufe_batch_config *cfg,
                                 ufe_batch_h *out) {
   if (!descs || !out || n < 1) { set_error("ufe_batch_create: null argument or no members"); return UFE_BAD_ARG; }
   *out = nullptr;
-  int team = cfg ? cfg->team_ctas : 0;
-  const int block = cfg && cfg->block ? cfg->block : 1024;
-  if (block != 1024 && block != 512 && block != 256) {
-    set_error("ufe_batch_create: block must be 1024, 512 or 256 threads");
-    return UFE_BAD_ARG;
-  }
-  if (team < 0) { set_error("ufe_batch_create: team_ctas must be >= 0"); return UFE_BAD_ARG; }
-  int max_nA = 0;
-  for (int k = 0; k < n; ++k) max_nA = std::max(max_nA, descs[k].nVAaAc);
-  // Default team: the fewest CTAs per member that keep every patch at <= 3/4 of the
-  // per-CTA slice table (the rest is padding headroom).
-  if (team == 0) team = std::max(1, (max_nA + (kMaxPatchSlices * kSlice * 3 / 4) - 1) / (kMaxPatchSlices * kSlice * 3 / 4));
+  int block = 0;
+  int rc = check_block(cfg, &block, "ufe_batch_create");
+  if (rc) return rc;
   ufe_batch_s *b = new ufe_batch_s();
-  b->n = n; b->team = team; b->block = block; b->use_graph = !cfg || cfg->use_graph != 0;
-  int rc = cuda_status(cudaGetDevice(&b->device), "cudaGetDevice");
+  b->n = n; b->block = block; b->use_graph = !cfg || cfg->use_graph != 0;
+  rc = cuda_status(cudaGetDevice(&b->device), "cudaGetDevice");
   if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, b->device), "SM count");
+  int resident = 0;
+  if (!rc) rc = resident_ctas(block, b->num_sms, &resident);
+  std::vector<int32_t> rows(n);
+  for (int k = 0; k < n; ++k) rows[k] = descs[k].nVAaAc;
+  b->team_of_member.assign(n, 0);
+  if (!rc) {
+    ufe_batch_config c = cfg ? *cfg : ufe_batch_config{};
+    c.block = block;
+    rc = plan_batch(rows.data(), n, c, resident, b->team_of_member.data(), &b->plan);
+  }
   if (!rc) rc = cuda_status(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
   b->members.assign(n, nullptr);
   b->cost.assign(n, 0.0);
   for (int k = 0; k < n && !rc; ++k) {
-    rc = mesh_create(descs + k, team, &b->members[k]);
-    if (!rc && b->members[k]->m.n_patch != team) {
-      char buf[160];
-      std::snprintf(buf, sizeof buf, "ufe_batch_create: member %d has too few rows for %d patches", k, team);
-      set_error(buf);
+    rc = mesh_create(descs + k, b->team_of_member[k], &b->members[k]);
+    if (!rc && b->members[k]->m.n_patch != b->team_of_member[k]) {
+      set_error("ufe_batch_create: member " + std::to_string(k) + " has too few rows for its team");
       rc = UFE_BAD_ARG;
-    }
-    if (rc == UFE_BAD_MESH) {
+    } else if (rc) {
       const std::string e = ufe_last_error_string();
       set_error("ufe_batch_create: member " + std::to_string(k) + ": " + e);
     }
-    // Expected cost: rows x sweeps, the sweep count of SOR growing like the square root of the rows.
-    if (!rc) b->cost[k] = (double)descs[k].nVAaAc * std::sqrt((double)descs[k].nVAaAc);
-  }
-  // Co-resident CTAs of the batched kernel: every mode's variant of this block size.
-  int per_sm = 1 << 30;
-  for (int mode = 0; mode < 3 && !rc; ++mode) {
-    const void *fn = batched_kernel(mode, block);
-    if (!fn) continue;
-    int q = 0;
-    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, fn, block, 0), "occupancy");
-    per_sm = std::min(per_sm, q);
+    if (!rc) b->cost[k] = member_work(rows[k], 1, 1024);
   }
   if (!rc) {
-    b->max_teams = per_sm * b->num_sms / team;
-    if (b->max_teams < 1) {
-      set_error("ufe_batch_create: team_ctas exceeds the co-resident CTAs of the device");
-      rc = UFE_BAD_ARG;
-    }
+    b->n_teams = 0;
+    for (int c = 0; c < b->plan.n_classes; ++c) b->n_teams += b->plan.class_teams[c];
+    b->layout_words = (size_t)((b->plan.grid_ctas + 3) & ~3) + 4 * (size_t)b->n_teams + 2 * (size_t)kMaxClasses;
+    b->sched_words = 32 * (size_t)kMaxClasses + 64 * (size_t)b->n_teams;
   }
   if (!rc) rc = cuda_status(cudaMallocHost(&b->args_host, (size_t)n * sizeof(SsaArgs)), "batch args host");
   if (!rc) rc = cuda_status(cudaMalloc(&b->args_dev, (size_t)n * sizeof(SsaArgs)), "batch args");
-  if (!rc) rc = cuda_status(cudaMalloc(&b->sched, (32 + 64 * (size_t)b->max_teams) * sizeof(unsigned int)), "batch sched");
+  if (!rc) rc = cuda_status(cudaMallocHost(&b->layout_host, b->layout_words * sizeof(int)), "batch layout host");
+  if (!rc) rc = cuda_status(cudaMalloc(&b->layout_dev, b->layout_words * sizeof(int)), "batch layout");
+  if (!rc) rc = cuda_status(cudaMalloc(&b->sched, b->sched_words * sizeof(unsigned int)), "batch sched");
   if (!rc) rc = cuda_status(cudaMalloc(&b->times_dev, 2 * (size_t)n * sizeof(unsigned long long)), "batch times");
   if (!rc) rc = cuda_status(cudaMallocHost(&b->times_host, 2 * (size_t)n * sizeof(unsigned long long)), "batch times host");
   if (!rc) rc = cuda_status(cudaMalloc(&b->err_dev, sizeof(int)), "batch err");
@@ -1616,8 +1785,8 @@ extern "C" int ufe_batch_run(ufe_batch_h b, const ufe_params *p, ufe_ssa_stats *
   for (int m = 0; m < b->n; ++m) std::memset(b->members[m]->ssa->ctl_host, 0, sizeof(SsaCtl));
   *b->err_host = 0;
   if (b->use_graph) {
-    // Capture once per parameter set and upload state; replays re-run every step, including
-    // the gathers of the current uploaded inputs.
+    // Captured once per parameter set and upload state; a replay re-runs every step,
+    // including the gathers of the currently uploaded inputs.
     std::vector<uint8_t> flags(b->n);
     for (int m = 0; m < b->n; ++m) flags[m] = member_flags(b->members[m]);
     if (!b->exec || !same_params(b->graph_params, *p) || flags != b->graph_flags) {
@@ -1665,8 +1834,8 @@ extern "C" int ufe_batch_run(ufe_batch_h b, const ufe_params *p, ufe_ssa_stats *
         dur.push_back(1e-6 * (double)(e - a));
         t0 = std::min(t0, a);
         t1 = std::max(t1, e);
+        if (timing->member_ms) timing->member_ms[b->order[q]] = 1e-6 * (double)(e - a);
       }
-      if (timing->member_ms && e > a) timing->member_ms[b->order[q]] = 1e-6 * (double)(e - a);
     }
     std::sort(dur.begin(), dur.end());
     auto pct = [&](double f) {   // nearest-rank percentile
@@ -1680,9 +1849,86 @@ extern "C" int ufe_batch_run(ufe_batch_h b, const ufe_params *p, ufe_ssa_stats *
     timing->member_p99_ms = pct(0.99);
     timing->member_max_ms = dur.empty() ? 0.0 : dur.back();
     timing->n_active = n_active;
-    timing->n_teams = std::min(n_active, b->max_teams);
-    timing->team_ctas = b->team;
+    timing->n_teams = b->n_teams;
+    timing->n_classes = b->plan.n_classes;
+    timing->grid_ctas = b->plan.grid_ctas;
+    timing->max_team_ctas = b->plan.class_team_ctas[0];
     timing->block = b->block;
   }
   return worst;
+}
+
+extern "C" int ufe_ssa_solve_batched(int32_t n, const ufe_mesh_desc *descs, const ufe_batch_config *cfg,
+                                     const ufe_params *p, const ufe_ssa_in *in, ufe_ssa_inout *io, ufe_ssa_out *out,
+                                     ufe_ssa_stats *stats) {
+  if (!descs || !p || !in || !io || n < 1) { set_error("ufe_ssa_solve_batched: null argument"); return UFE_BAD_ARG; }
+  ufe_batch_h b = nullptr;
+  int rc = ufe_batch_create(descs, n, cfg, &b);
+  for (int m = 0; m < n && !rc; ++m) rc = ufe_batch_upload(b, m, p, in + m, io + m);
+  int status = UFE_OK;
+  if (!rc) {
+    status = ufe_batch_run(b, p, stats, nullptr);
+    if (status < 0 && status != UFE_DIVERGED) rc = status;
+  }
+  for (int m = 0; m < n && !rc; ++m) rc = ufe_batch_download(b, m, io + m, out ? out + m : nullptr);
+  if (b) ufe_batch_destroy(b);
+  return rc ? rc : status;
+}
+
+// Autotuner of the batched solve: the per-CTA packing (rows_per_cta, hence the team size of
+// every member) first at 1024-thread CTAs, then the CTA size at the best packing, then the
+// neighbouring packings at the best CTA size. Each
+// candidate is a real batch of the caller's members, solved twice (the first run captures
+// the graph); the second run's device time decides.
+extern "C" int ufe_batch_autotune(int32_t n, const ufe_mesh_desc *descs, const ufe_params *p, const ufe_ssa_in *in,
+                                  const ufe_ssa_inout *io, ufe_batch_config *best, ufe_batch_tune_entry *log,
+                                  int32_t log_capacity, int32_t *log_count) {
+  if (!descs || !p || !in || !io || !best || n < 1) { set_error("ufe_batch_autotune: null argument"); return UFE_BAD_ARG; }
+  int n_log = 0;
+  double best_ms = 1e300;
+  ufe_batch_config best_cfg{0, kDefaultRowsPerCta, 1024, 1};
+  auto trial = [&](const ufe_batch_config &c) -> int {
+    ufe_batch_h b = nullptr;
+    int rc = ufe_batch_create(descs, n, &c, &b);
+    if (rc == UFE_BAD_ARG) return UFE_OK;   // this packing does not fit these members: skip it
+    for (int m = 0; m < n && !rc; ++m) rc = ufe_batch_upload(b, m, p, in + m, io + m);
+    ufe_batch_timing t{};
+    for (int k = 0; k < 2 && !rc; ++k) {
+      const int st = ufe_batch_run(b, p, nullptr, &t);
+      if (st < 0 && st != UFE_DIVERGED) rc = st;
+    }
+    if (b) ufe_batch_destroy(b);
+    if (rc) return rc;
+    if (log && n_log < log_capacity) {
+      log[n_log].rows_per_cta = c.rows_per_cta;
+      log[n_log].block = c.block;
+      log[n_log].grid_ctas = t.grid_ctas;
+      log[n_log].n_classes = t.n_classes;
+      log[n_log].device_ms = t.device_ms;
+      log[n_log].member_p99_ms = t.member_p99_ms;
+    }
+    ++n_log;
+    if (t.device_ms < best_ms) { best_ms = t.device_ms; best_cfg = c; }
+    return UFE_OK;
+  };
+  int rc = UFE_OK;
+  const int packings[] = {4096, 8192, 16384, kMaxRowsPerPatch};
+  const int n_pack = 4;
+  for (int R : packings)
+    if (!rc) rc = trial(ufe_batch_config{0, R, 1024, 1});
+  const int R = best_cfg.rows_per_cta;
+  for (int blk : {512, 256})
+    if (!rc) rc = trial(ufe_batch_config{0, R, blk, 1});
+  // The packings next to the best one at the best CTA size.
+  const int blk = best_cfg.block;
+  if (blk != 1024) {
+    const int i = (int)(std::find(packings, packings + n_pack, R) - packings);
+    for (int j : {i - 1, i + 1})
+      if (!rc && j >= 0 && j < n_pack) rc = trial(ufe_batch_config{0, packings[j], blk, 1});
+  }
+  if (log_count) *log_count = n_log;
+  if (rc) return rc;
+  if (best_ms == 1e300) { set_error("ufe_batch_autotune: no candidate fits these members"); return UFE_BAD_ARG; }
+  *best = best_cfg;
+  return UFE_OK;
 }
