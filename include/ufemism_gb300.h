@@ -198,6 +198,44 @@ int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *i
 int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
                           ufe_sia_out *out);
 
+/* VJP of the converged solve (no counterpart in the reference): for a misfit J(u) of the
+ * velocities of the last ufe_ssa_solve / ufe_ssa_run on this handle, solves the adjoint
+ * system (dF/du)^T mu = dJ/du of the discrete fixed point F(u) = 0 the Picard/SOR loop
+ * converged to (viscosity and friction linearised at the converged state, Neumann rows as
+ * averaging constraints, masks frozen) by a transposed coloured SOR on the device, and
+ * returns dJ/d(log beta^2) on AaAc, the sensitivities to the gathered driving-stress slopes
+ * and Hi_AaAc and, given the Aa and Ac derivative stencils, dJ/dHi on Aa. Linear sliding law
+ * only; the grounding-line flux option is not differentiated. Output arrays may be NULL.
+ * The forward solve should be converged well below the tolerances the gradient is wanted
+ * to (the VJP differentiates the fixed point, not the truncated iteration). */
+typedef struct ufe_vjp_params {
+  double tol;          /* stop when max |update| < tol * max |mu| (0: 1e-12) */
+  int32_t max_sweeps;  /* 0: 200000 */
+  double omega;        /* 0: SSA_SOR_omega */
+} ufe_vjp_params;
+typedef struct ufe_vjp_in {
+  const double *dJ_dU, *dJ_dV;          /* (nV) */
+  const double *dJ_dUx_Ac, *dJ_dUy_Ac;  /* (nAc) */
+} ufe_vjp_in;
+typedef struct ufe_vjp_geom {           /* the type_mesh arrays of get_mesh_derivatives and _Ac */
+  const int32_t *nC, *C;                /* (nV), (nV,nC_mem) */
+  const double *Nx, *Ny;                /* (nV,nC_mem+1) Aa neighbour functions */
+  const int32_t *Aci;                   /* (nAc,4) */
+  const double *Nx_Ac, *Ny_Ac;          /* (nAc,4) */
+} ufe_vjp_geom;
+typedef struct ufe_vjp_out {
+  double *dJ_dlogbeta_sq_AaAc;          /* (nVAaAc) */
+  double *dJ_dHi;                       /* (nV), needs geom */
+  double *dJ_dhx_AaAc, *dJ_dhy_AaAc, *dJ_dHi_AaAc;  /* (nVAaAc) sensitivities to the gathered fields */
+  double *lambda_U_AaAc, *lambda_V_AaAc;            /* (nVAaAc) adjoint state */
+} ufe_vjp_out;
+typedef struct ufe_vjp_stats {
+  int32_t status, sweeps;
+  double last_rel_update, device_ms;
+} ufe_vjp_stats;
+int ufe_ssa_vjp(ufe_mesh_h mesh, const ufe_params *params, const ufe_vjp_params *vjp_params,
+                const ufe_vjp_in *in, const ufe_vjp_geom *geom, ufe_vjp_out *out, ufe_vjp_stats *stats);
+
 /* Batched ensemble (no counterpart in the reference, whose model runs one solve_SSA per
  * time step): many independent solves on meshes of uneven size (friction or rheology
  * ensembles) in one persistent cooperative launch. The grid is cut into teams of CTAs; a

@@ -1,0 +1,93 @@
+"""The FP64 CPU adjoint reference (oracle/ssa_adjoint.py) pinned against the oracle's own
+forward solve: its Jacobian against finite differences of the residual, and its gradients
+against central finite differences of the misfit (h = 1e-4) and against its tangent-linear
+model. Runs on CPU."""
+import numpy as np
+import pytest
+
+from conftest import oracle_aaac, oracle_inputs
+
+import oracle as orc
+import ssa_adjoint as adj
+from ufemism_gb300 import workloads as wl
+
+TIGHT = dict(SSA_RN_tol=1e-13, SSA_max_residual_UV=1e-11, SSA_max_outer_loops=300, SSA_max_inner_loops=1000000)
+
+
+@pytest.fixture(scope="module")
+def problem():
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, "dome")
+    logb = wl.log_beta_field(m, std=1.0, ell=100e3, seed=5)
+    P = orc.default_params(**TIGHT)
+
+    def solve(lb, fields=None):
+        f = dict(fields or ssa)
+        f["beta_sq_AaAc"] = np.exp(lb)
+        rc, out, st = orc.solve_ssa(m, f, P)
+        assert rc == 0 and st["last_RN"] < 1e-12
+        return adj.aaac_velocity(out), f
+
+    (U, V), f0 = solve(logb)
+    (Uo, Vo), _ = solve(logb + wl.log_beta_field(m, std=0.3, ell=100e3, seed=11))
+    return m, ssa, logb, solve, U, V, f0, Uo, Vo
+
+
+def fields_for(m, ssa, H):
+    g = orc.update_geometry(m, H, ssa["Hb"], ssa["SL"])
+    f = dict(ssa)
+    for k in ("Hi_Ac", "dHs_dx_shelf", "dHs_dy_shelf", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac", "Hb_Ac", "SL_Ac"):
+        f[k] = g[k]
+    f["Hi"] = H
+    return f, g
+
+
+def test_residual_vanishes_and_jacobian_matches_finite_differences(problem):
+    m, ssa, logb, solve, U, V, f0, Uo, Vo = problem
+    lin = adj.Linearisation(m, f0, U, V)
+    F = lin.residual()
+    scale = np.abs(adj.RHO_I * adj.GRAV * lin.g["hx"] / lin.eta).max()    # driving-stress term
+    assert np.abs(F).max() < 1e-9 * scale
+    K = lin.jacobian()
+    rng = np.random.default_rng(0)
+    nA = m.nVAaAc
+    for _ in range(2):
+        d = rng.normal(size=2 * nA)
+        h = 1e-6 * np.abs(U).max()
+        Fp = adj.Linearisation(m, f0, U + h * d[:nA], V + h * d[nA:]).residual()
+        Fm = adj.Linearisation(m, f0, U - h * d[:nA], V - h * d[nA:]).residual()
+        fd = (Fp - Fm) / (2 * h)
+        an = K @ d
+        assert np.linalg.norm(fd - an) / np.linalg.norm(an) < 1e-7
+
+
+def test_gradients_match_finite_differences_and_tangent_linear(problem):
+    m, ssa, logb, solve, U, V, f0, Uo, Vo = problem
+    lin = adj.Linearisation(m, f0, U, V)
+    G = adj.geometry_matrix(m, ssa["Hi"], ssa["Hb"], ssa["SL"])
+    gU, gV = U - Uo, V - Vo
+    mx, my, dlb, dHi, sens = adj.adjoint_gradient(lin, gU, gV, G)
+    rng = np.random.default_rng(1)
+    h = 1e-4
+    for _ in range(2):
+        d = rng.normal(size=m.nVAaAc)
+        (Up, Vp), _ = solve(logb + h * d)
+        (Um, Vm), _ = solve(logb - h * d)
+        fd = (adj.misfit(Up, Vp, Uo, Vo) - adj.misfit(Um, Vm, Uo, Vo)) / (2 * h)
+        an = float(dlb @ d)
+        du, dv = adj.tangent_linear(lin, d_logbeta=d)
+        assert abs(fd - an) <= 1e-5 * abs(an)
+        assert abs(float(gU @ du + gV @ dv) - an) <= 1e-10 * abs(an)
+    Hi = ssa["Hi"]
+    for _ in range(2):
+        d = rng.normal(size=m.base.nV) * (Hi > 50.0)
+        fp, gp = fields_for(m, ssa, Hi + h * d)
+        fm, gm = fields_for(m, ssa, Hi - h * d)
+        assert np.array_equal(gp["mask_ocean"], gm["mask_ocean"])
+        (Up, Vp), _ = solve(logb, fp)
+        (Um, Vm), _ = solve(logb, fm)
+        fd = (adj.misfit(Up, Vp, Uo, Vo) - adj.misfit(Um, Vm, Uo, Vo)) / (2 * h)
+        an = float(dHi @ d)
+        du, dv = adj.tangent_linear(lin, d_Hi=d, G=G)
+        assert abs(fd - an) <= 1e-5 * abs(an)
+        assert abs(float(gU @ du + gV @ dv) - an) <= 1e-10 * abs(an)

@@ -1,0 +1,112 @@
+"""GPU VJP of the converged SSA solve through the C-ABI (run with -m gpu), against the FP64
+CPU adjoint reference evaluated at the GPU's converged velocities (which itself is pinned
+against finite differences in test_adjoint_oracle.py), and against central finite
+differences (h = 1e-4) of the GPU forward solve. Tolerances: adjoint state and gradients
+1e-8 relative L2 against the reference; directional derivatives 1e-5 against finite
+differences."""
+import numpy as np
+import pytest
+
+from conftest import oracle_aaac, oracle_inputs, rel_l2
+
+import oracle as orc
+import ssa_adjoint as adj
+from ufemism_gb300 import _native as nat
+from ufemism_gb300 import api
+from ufemism_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+TIGHT = dict(SSA_RN_tol=1e-13, SSA_max_residual_UV=1e-11, SSA_max_outer_loops=300, SSA_max_inner_loops=1000000)
+REF_TOL = 1e-8
+FD_TOL = 1e-5
+
+
+def setup_case(name, kind):
+    api.init(0)
+    m = oracle_aaac(name)
+    ssa, sia, g = oracle_inputs(m, kind)
+    logb = wl.log_beta_field(m, std=1.0, ell=100e3, seed=5)
+    dm = api.DeviceMesh(m)
+    p = api.default_params(precision=nat.UFE_FP64, **TIGHT)
+
+    def solve(lb, fields=None):
+        f = dict(fields or ssa)
+        f["beta_sq_AaAc"] = np.exp(lb)
+        rc, out, st = dm.solve_ssa(f, p)
+        assert rc == 0 and st["last_RN"] < 1e-12, st
+        return adj.aaac_velocity(out), f
+
+    (Uo, Vo), _ = solve(logb + wl.log_beta_field(m, std=0.3, ell=100e3, seed=11))
+    (U, V), f0 = solve(logb)          # the handle now holds the solve the VJP differentiates
+    return m, ssa, logb, dm, p, solve, U, V, f0, Uo, Vo
+
+
+def split(m, a):
+    nV = m.base.nV
+    return a[:nV], a[nV:]
+
+
+@pytest.mark.parametrize("name,kind", [("1k", "dome"), ("1k", "marine")])
+def test_vjp_matches_cpu_reference_and_finite_differences(name, kind):
+    m, ssa, logb, dm, p, solve, U, V, f0, Uo, Vo = setup_case(name, kind)
+    gU, gV = U - Uo, V - Vo
+    dJ = dict(zip(("U_SSA", "Ux_SSA_Ac"), split(m, gU)))
+    dJ.update(zip(("V_SSA", "Uy_SSA_Ac"), split(m, gV)))
+    rc, out, st = dm.ssa_vjp(dJ, p, geom_mesh=m)
+    assert rc == nat.UFE_OK, st
+    # CPU reference at the GPU's converged state
+    lin = adj.Linearisation(m, f0, U, V)
+    G = adj.geometry_matrix(m, ssa["Hi"], ssa["Hb"], ssa["SL"])
+    mx, my, dlb, dHi, sens = adj.adjoint_gradient(lin, gU, gV, G)
+    assert rel_l2(out["lambda_U_AaAc"], mx) <= REF_TOL
+    assert rel_l2(out["lambda_V_AaAc"], my) <= REF_TOL
+    assert rel_l2(out["dJ_dlogbeta_sq_AaAc"], dlb) <= REF_TOL
+    assert rel_l2(out["dJ_dhx_AaAc"], sens["hx"]) <= REF_TOL
+    assert rel_l2(out["dJ_dHi_AaAc"], sens["Hi"]) <= REF_TOL
+    assert rel_l2(out["dJ_dHi"], dHi) <= REF_TOL
+    # finite differences of the GPU forward solve
+    rng = np.random.default_rng(3)
+    h = 1e-4
+    for _ in range(2):
+        d = rng.normal(size=m.nVAaAc)
+        (Up, Vp), _ = solve(logb + h * d)
+        (Um, Vm), _ = solve(logb - h * d)
+        fd = (adj.misfit(Up, Vp, Uo, Vo) - adj.misfit(Um, Vm, Uo, Vo)) / (2 * h)
+        an = float(out["dJ_dlogbeta_sq_AaAc"] @ d)
+        assert abs(fd - an) <= FD_TOL * abs(an), (fd, an)
+    Hi = ssa["Hi"]
+    for _ in range(2):
+        d = rng.normal(size=m.base.nV) * (Hi > 50.0)
+        gp = orc.update_geometry(m, Hi + h * d, ssa["Hb"], ssa["SL"])
+        gm = orc.update_geometry(m, Hi - h * d, ssa["Hb"], ssa["SL"])
+        assert np.array_equal(gp["mask_ocean"], gm["mask_ocean"])
+        assert np.array_equal(gp["mask_ocean_Ac"], gm["mask_ocean_Ac"])
+        res = []
+        for H, gg in ((Hi + h * d, gp), (Hi - h * d, gm)):
+            f = dict(ssa)
+            for k in ("Hi_Ac", "dHs_dx_shelf", "dHs_dy_shelf", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac"):
+                f[k] = gg[k]
+            f["Hi"] = H
+            (Uh, Vh), _ = solve(logb, f)
+            res.append(adj.misfit(Uh, Vh, Uo, Vo))
+        fd = (res[0] - res[1]) / (2 * h)
+        an = float(out["dJ_dHi"] @ d)
+        assert abs(fd - an) <= FD_TOL * abs(an), (fd, an)
+    dm.close()
+
+
+def test_vjp_rejects_coulomb_law_and_missing_solve():
+    api.init(0)
+    m = oracle_aaac("tiny")
+    dm = api.DeviceMesh(m)
+    dJ = {k: np.zeros(n) for k, n in (("U_SSA", m.base.nV), ("V_SSA", m.base.nV), ("Ux_SSA_Ac", m.nAc),
+                                      ("Uy_SSA_Ac", m.nAc))}
+    rc, out, st = dm.ssa_vjp(dJ, api.default_params(), check=False)
+    assert rc == nat.UFE_BAD_ARG
+    ssa, sia, g = oracle_inputs(m, "dome")
+    p = api.default_params(sliding_law=nat.UFE_SLIDING_COULOMB_REGULARISED)
+    dm.solve_ssa(ssa, p)
+    rc, out, st = dm.ssa_vjp(dJ, p, check=False)
+    assert rc == nat.UFE_BAD_ARG and "linear sliding" in nat.last_error()
+    dm.close()

@@ -75,6 +75,30 @@ class SiaOut(ct.Structure):
                                  "U_SIA", "V_SIA", "D_SIA")]
 
 
+class VjpParams(ct.Structure):
+    _fields_ = [("tol", F64), ("max_sweeps", I32), ("omega", F64)]
+
+
+class VjpIn(ct.Structure):
+    _fields_ = [(n, P) for n in ("dJ_dU", "dJ_dV", "dJ_dUx_Ac", "dJ_dUy_Ac")]
+
+
+class VjpGeom(ct.Structure):
+    _fields_ = [(n, P) for n in ("nC", "C", "Nx", "Ny", "Aci", "Nx_Ac", "Ny_Ac")]
+
+
+VJP_OUT_FIELDS = ("dJ_dlogbeta_sq_AaAc", "dJ_dHi", "dJ_dhx_AaAc", "dJ_dhy_AaAc", "dJ_dHi_AaAc", "lambda_U_AaAc",
+                  "lambda_V_AaAc")
+
+
+class VjpOut(ct.Structure):
+    _fields_ = [(n, P) for n in VJP_OUT_FIELDS]
+
+
+class VjpStats(ct.Structure):
+    _fields_ = [("status", I32), ("sweeps", I32), ("last_rel_update", F64), ("device_ms", F64)]
+
+
 class BatchConfig(ct.Structure):
     _fields_ = [("team_ctas", I32), ("rows_per_cta", I32), ("block", I32), ("use_graph", I32)]
 
@@ -122,6 +146,8 @@ PROTOTYPES = {
     "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_ssa_vjp": (I32, [P, ct.POINTER(Params), ct.POINTER(VjpParams), ct.POINTER(VjpIn), ct.POINTER(VjpGeom),
+                          ct.POINTER(VjpOut), ct.POINTER(VjpStats)]),
     "ufe_batch_plan": (I32, [ct.POINTER(I32), I32, ct.POINTER(BatchConfig), I32, ct.POINTER(I32),
                              ct.POINTER(BatchPlan)]),
     "ufe_ssa_solve_batched": (I32, [I32, ct.POINTER(MeshDesc), ct.POINTER(BatchConfig), ct.POINTER(Params),

@@ -230,6 +230,39 @@ class DeviceMesh:
             raise nat.UfeError(rc, "ufe_ssa_download")
         return io
 
+    def ssa_vjp(self, dJ: dict, params: dict, geom_mesh=None, tol: float = 0.0, max_sweeps: int = 0,
+                omega: float = 0.0, check: bool = True):
+        """VJP of the last solve on this handle (ufe_ssa_vjp). ``dJ`` holds dJ/du as U_SSA,
+        V_SSA (nV) and Ux_SSA_Ac, Uy_SSA_Ac (nAc). With ``geom_mesh`` (an AaAc mesh with the
+        Aa and Ac derivative stencils) dJ/dHi on Aa is returned too. Returns (status,
+        outputs, stats)."""
+        L = nat.load()
+        keep = [np.ascontiguousarray(dJ[k], dtype=np.float64) for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac")]
+        vin = nat.VjpIn(*(a.ctypes.data for a in keep))
+        out = {k: np.zeros(self.nVAaAc) for k in nat.VJP_OUT_FIELDS if k != "dJ_dHi"}
+        geom = None
+        if geom_mesh is not None:
+            gm = geom_mesh
+            ncm = gm.CAaAc.shape[1]
+            if gm.base.C.shape != (self.nV, ncm) or np.shape(gm.Nx) != (self.nV, ncm + 1) or \
+                    np.shape(gm.Nx_Ac) != (self.nAc, 4) or np.shape(gm.Aci) != (self.nAc, 4):
+                raise ValueError("geom_mesh arrays do not match this mesh (C: (nV, nC_mem), Nx: (nV, nC_mem+1))")
+            gk = dict(nC=_i32(gm.base.nC), C=_i32(gm.base.C), Nx=_f64(gm.Nx), Ny=_f64(gm.Ny), Aci=_i32(gm.Aci),
+                      Nx_Ac=_f64(gm.Nx_Ac), Ny_Ac=_f64(gm.Ny_Ac))
+            keep.append(gk)
+            geom = nat.VjpGeom(*(_ptr(gk[k]) for k in ("nC", "C", "Nx", "Ny", "Aci", "Nx_Ac", "Ny_Ac")))
+            out["dJ_dHi"] = np.zeros(self.nV)
+        vo = nat.VjpOut(*(_ptr(out.get(k)) for k in nat.VJP_OUT_FIELDS))
+        vp = nat.VjpParams(tol, max_sweeps, omega)
+        ps, _z = _params_struct(params)
+        st = nat.VjpStats()
+        rc = L.ufe_ssa_vjp(self._h, ct.byref(ps), ct.byref(vp), ct.byref(vin), ct.byref(geom) if geom else None,
+                           ct.byref(vo), ct.byref(st))
+        if check and rc < 0:
+            raise nat.UfeError(rc, "ufe_ssa_vjp")
+        return rc, out, dict(status=st.status, sweeps=st.sweeps, last_rel_update=st.last_rel_update,
+                             device_ms=st.device_ms)
+
     # ---------------------------------------------------------------- SIA
     def solve_sia(self, fields: dict, params: dict, want_3d: bool = True):
         L = nat.load()

@@ -104,6 +104,7 @@ struct DevMesh {
 
 struct SsaWork;   // per-handle device buffers of the SSA solve (ufe_ssa.cu)
 struct SiaWork;   // per-handle device buffers of the SIA solve (ufe_sia.cu)
+struct AdjWork;   // per-handle device buffers of the SSA adjoint (ufe_ssa.cu)
 
 }  // namespace ufe
 
@@ -114,9 +115,11 @@ struct ufe_mesh_s {
   ufe::DevMesh m;
   ufe::SsaWork *ssa = nullptr;
   ufe::SiaWork *sia = nullptr;
+  ufe::AdjWork *adj = nullptr;
 };
 
 namespace ufe {
 void ssa_free(SsaWork *w);
 void sia_free(SiaWork *w);
+void adj_free(AdjWork *w);
 }  // namespace ufe

@@ -381,6 +381,7 @@ extern "C" int ufe_mesh_destroy(ufe_mesh_h h) {
   cudaStreamSynchronize(h->stream);
   ssa_free(h->ssa);
   sia_free(h->sia);
+  adj_free(h->adj);
   free_mesh(h->m);
   cudaStreamDestroy(h->stream);
   delete h;

@@ -634,8 +634,8 @@ __device__ void phase_zero_velocity(const SsaArgs &a, const Team &t, bool mixed)
 // ---------------------------------------------------------------------------------------
 
 // Progress of this CTA's patch: the number of colour phases it has completed in this launch.
-template <class Team>
-__device__ __forceinline__ void publish_progress(const SsaArgs &a, const Team &t, unsigned int value) {
+template <class Args, class Team>
+__device__ __forceinline__ void publish_progress(const Args &a, const Team &t, unsigned int value) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -645,7 +645,8 @@ __device__ __forceinline__ void publish_progress(const SsaArgs &a, const Team &t
 
 // Wait until every patch this patch synchronises with has completed `target` colour phases.
 // Bounded: after timeout_ns the CTA records UFE_TIMEOUT (the next grid barrier then fails).
-__device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSmem &ps, unsigned int target,
+template <class Args>
+__device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &ps, unsigned int target,
                                                 unsigned int *team_bar) {
   if (threadIdx.x < ps.nsync) {
     const unsigned int *q = a.prog + 32 * ps.sync[threadIdx.x];
@@ -669,6 +670,24 @@ __device__ __forceinline__ void wait_neighbours(const SsaArgs &a, const PatchSme
   __syncthreads();
 }
 
+// Patch b's slice table, edge range and synchronisation set into shared memory.
+template <class Args>
+__device__ __forceinline__ void load_patch(const Args &a, int b, PatchSmem &ps) {
+  if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
+  if (threadIdx.x == 0) {
+    ps.edge0 = a.patch_edge0[b];
+    ps.edge1 = a.patch_edge0[b + 1];
+    ps.nsync = a.sync_ptr[b + 1] - a.sync_ptr[b];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < ps.nsync; i += blockDim.x) ps.sync[i] = a.sync_list[a.sync_ptr[b] + i];
+  for (int s = ps.ps[0] + threadIdx.x; s < ps.ps[kGroups]; s += blockDim.x) {
+    ps.e0[s - ps.ps[0]] = a.slice_e0[s];
+    ps.w[s - ps.ps[0]] = a.slice_w[s];
+  }
+  __syncthreads();
+}
+
 // The whole solve_SSA of one problem, run by the CTAs of a team (each CTA owns one patch).
 // Returns false when a bounded wait failed; the error is recorded in the problem's control
 // block and the team's barrier counter.
@@ -679,22 +698,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
   unsigned int phases = 0;   // colour phases completed by this patch
   const bool leader = t.rank() == 0 && threadIdx.x == 0;
   __shared__ PatchSmem ps;
-  {
-    const int b = t.rank();
-    if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
-    if (threadIdx.x == 0) {
-      ps.edge0 = a.patch_edge0[b];
-      ps.edge1 = a.patch_edge0[b + 1];
-      ps.nsync = a.sync_ptr[b + 1] - a.sync_ptr[b];
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < ps.nsync; i += blockDim.x) ps.sync[i] = a.sync_list[a.sync_ptr[b] + i];
-    for (int s = ps.ps[0] + threadIdx.x; s < ps.ps[kGroups]; s += blockDim.x) {
-      ps.e0[s - ps.ps[0]] = a.slice_e0[s];
-      ps.w[s - ps.ps[0]] = a.slice_w[s];
-    }
-    __syncthreads();
-  }
+  load_patch(a, t.rank(), ps);
   double *N = a.Na, *Nprev = a.Nb;
   int did_reset_before = 0;
   int it = 0;
@@ -852,6 +856,367 @@ __global__ void __launch_bounds__(kBlock, kPerSm) ssa_batched(const BatchArgs b)
       return;
     }
     if (t.rank() == 0 && threadIdx.x == 0) b.times[2 * m + 1] = globaltimer_ns();
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Adjoint of the converged solve (no counterpart in the reference)
+//
+// F(u) = 0 is the discrete system the Picard/SOR loop converges to: on interior rows the
+// momentum balance with eta = eta(u) (and the friction factor S / (max(0.1, H) eta) on
+// grounded rows), on edge rows the Neumann averages. The VJP solves (dF/du)^T mu = dJ/du by
+// a transposed coloured SOR: per sweep the corners, the other edge rows, then colours 5..1
+// (the reverse of the forward's block order, which makes the transposed iteration converge
+// like the forward one). Transposed row j gathers over its neighbours i the coefficients of
+// u_j in equation i: Cu_ij mu_x,i + kU_ij s_i, with s_i = alpha_x,i mu_x,i + alpha_y,i mu_y,i
+// the linearised viscosity of row i (eta' lumped per row) and kU_ij the strain-rate
+// derivative d(eps^2)/dU_j through row i's neighbour functions; for an edge or corner
+// neighbour i the coefficient is its averaging weight.
+// ---------------------------------------------------------------------------------------
+struct AdjCtl {
+  unsigned int bar_count;         // monotonic grid-barrier counter (bit 30: error)
+  int err;
+  int status;
+  int sweeps;
+  unsigned long long maxd[3];     // max |update| per sweep (ring), ordered bits
+  unsigned long long maxm[3];     // max |mu| per sweep (ring)
+  double last_rel;
+  int not_found;                  // transposed entries without a reverse entry (asymmetric mesh)
+  int pad_;
+};
+
+struct AdjArgs {
+  const int *col;
+  const uint8_t *deg;
+  const int *orig_of_dev;
+  const int *slice_e0;
+  const uint8_t *slice_w;
+  const int *patch_slice;
+  const int *patch_edge0;
+  const int *sync_ptr;
+  const int *sync_list;
+  unsigned int *prog;
+  const double2 *cT, *kT;   // [nE] transposed coefficients
+  const double2 *ee;        // [nP] (eu, ev) on interior rows
+  const double *c3;         // [nP] 3 sNxy
+  const double2 *kh;        // [nP] home strain derivatives (kU_ii, kV_ii)
+  const double2 *alpha;     // [nP]
+  const double2 *dinv;      // [nP] 1 / transposed diagonal
+  const double2 *g;         // [nP] dJ/du
+  double2 *mu;
+  double *s;
+  AdjCtl *ctl;
+  double omega, tol;
+  int max_sweeps;
+  long long timeout_ns;
+};
+
+// One phase of the transposed sweep over group g of the patch. kind 0: interior rows of a
+// colour (SOR update); 1: the corners, 2: the other edge rows (exact update, unit diagonal).
+__device__ void adj_phase(const AdjArgs &a, const PatchSmem &ps, int g, int kind, unsigned long long &mxd,
+                          unsigned long long &mxm) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (int s = ps.ps[g] + wid; s < ps.ps[g + 1]; s += nwarps) {
+    const int w = ps.w[s - ps.ps[0]];
+    const int64_t e0 = ps.e0[s - ps.ps[0]] + lane;
+    const int p = s * kSlice + lane;
+    if (a.deg[p] == 0) continue;
+    if (kind != 0 && ((kind == 1) != (a.orig_of_dev[p] < 4))) continue;
+    double rx = 0.0, ry = 0.0;
+    for (int k = 0; k < w; ++k) {
+      const int64_t e = e0 + (int64_t)k * kSlice;
+      const int j = a.col[e];
+      if (j < 0) break;
+      const double2 c = a.cT[e];
+      const double2 kk = a.kT[e];
+      const double2 m = a.mu[j];
+      const double sj = a.s[j];
+      rx = fma(c.x, m.x, fma(kk.x, sj, rx));
+      ry = fma(c.y, m.y, fma(kk.y, sj, ry));
+    }
+    const double2 mi = a.mu[p];
+    const double2 gi = a.g[p];
+    double dx, dy;
+    if (kind == 0) {
+      const double2 ec = a.ee[p];
+      const double c3 = a.c3[p];
+      const double2 kh = a.kh[p];
+      const double sp = a.s[p];
+      rx = fma(ec.x, mi.x, fma(c3, mi.y, fma(kh.x, sp, rx))) - gi.x;
+      ry = fma(ec.y, mi.y, fma(c3, mi.x, fma(kh.y, sp, ry))) - gi.y;
+      const double2 di = a.dinv[p];
+      dx = -a.omega * rx * di.x;
+      dy = -a.omega * ry * di.y;
+    } else {
+      dx = -(rx + mi.x - gi.x);
+      dy = -(ry + mi.y - gi.y);
+    }
+    const double2 mn = make_double2(mi.x + dx, mi.y + dy);
+    a.mu[p] = mn;
+    if (kind == 0) {
+      const double2 al = a.alpha[p];
+      a.s[p] = fma(al.x, mn.x, al.y * mn.y);
+    }
+    unsigned long long b = abs_bits(dx);
+    mxd = b > mxd ? b : mxd;
+    b = abs_bits(dy);
+    mxd = b > mxd ? b : mxd;
+    b = abs_bits(mn.x);
+    mxm = b > mxm ? b : mxm;
+    b = abs_bits(mn.y);
+    mxm = b > mxm ? b : mxm;
+  }
+}
+
+__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_adjoint_sor(const AdjArgs a) {
+  GridTeam t{&a.ctl->bar_count, 0u};
+  AdjCtl *ctl = a.ctl;
+  __shared__ PatchSmem ps;
+  load_patch(a, t.rank(), ps);
+  const bool leader = t.rank() == 0 && threadIdx.x == 0;
+  unsigned int phases = 0;
+  int sweeps = 0;
+  for (;;) {
+    ++sweeps;
+    const int slot = sweeps % 3;
+    if (leader) { ctl->maxd[(sweeps + 1) % 3] = 0ull; ctl->maxm[(sweeps + 1) % 3] = 0ull; }
+    unsigned long long mxd = 0ull, mxm = 0ull;
+    for (int ph = 0; ph < 7; ++ph) {
+      if (ph > 0) wait_neighbours(a, ps, phases, t.bar());
+      if (ph == 0) adj_phase(a, ps, 5, 1, mxd, mxm);
+      else if (ph == 1) adj_phase(a, ps, 5, 2, mxd, mxm);
+      else adj_phase(a, ps, 6 - ph, 0, mxd, mxm);   // colours 5, 4, 3, 2, 1
+      ++phases;
+      publish_progress(a, t, phases);
+    }
+    block_max_to(&ctl->maxd[slot], mxd);
+    block_max_to(&ctl->maxm[slot], mxm);
+    if (!team_barrier(t, &ctl->err, a.timeout_ns)) {
+      if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu;
+      return;
+    }
+    const double md = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxd[slot]);
+    const double mm = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxm[slot]);
+    const double rel = mm > 0.0 ? md / mm : 0.0;
+    if (rel < a.tol || sweeps >= a.max_sweeps) {
+      if (leader) {
+        ctl->sweeps = sweeps;
+        ctl->last_rel = rel;
+        ctl->status = rel < a.tol ? UFE_OK : UFE_NOT_CONVERGED;
+      }
+      return;
+    }
+  }
+}
+
+// Per-row set-up of the adjoint operator at the converged velocities: strain rates,
+// viscosity, friction factor, the linearised-viscosity weights alpha and the transposed
+// diagonal. Boundary rows get unit diagonals and no viscosity term.
+struct AdjSetup {
+  int nP, nV;
+  const int *col;
+  const uint8_t *deg;
+  const int *slice_e0;
+  const uint8_t *slice_g;
+  const int *orig_of_dev;
+  const double2 *nxy, *h_nxy, *h_cuv;
+  const double *sNxy;
+  const double *Hi, *Hb, *SL, *hx, *hy, *Af, *beta;
+  double beta_const, m_enh;
+  const double2 *UV;
+  const double *dJ_U, *dJ_V, *dJ_Ux, *dJ_Uy;   // caller order, staged on the device
+  double2 *ee, *kh, *alpha, *dinv, *g, *mu;
+  double *c3, *s, *eta, *fr, *inv_nb;
+  double *K;                                   // [3 nP] strain combinations 2ux+vy, (uy+vx)/2, 2vy+ux
+  double omega;
+};
+
+__device__ __forceinline__ int64_t sell_entry(const int *slice_e0, int p, int k) {
+  return (int64_t)slice_e0[p / kSlice] + (int64_t)k * kSlice + (p % kSlice);
+}
+
+__global__ void k_adj_rows(const AdjSetup a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.nP) return;
+  const int n = a.deg[p];
+  const int r = a.orig_of_dev[p];
+  a.mu[p] = make_double2(0.0, 0.0);
+  a.s[p] = 0.0;
+  if (n == 0 || r < 0) {
+    a.ee[p] = make_double2(1.0, 1.0); a.kh[p] = make_double2(0.0, 0.0); a.alpha[p] = make_double2(0.0, 0.0);
+    a.dinv[p] = make_double2(1.0, 1.0); a.g[p] = make_double2(0.0, 0.0); a.c3[p] = 0.0;
+    a.eta[p] = 1.0; a.fr[p] = 0.0; a.inv_nb[p] = 0.0;
+    a.K[p] = 0.0; a.K[a.nP + p] = 0.0; a.K[2 * a.nP + p] = 0.0;
+    return;
+  }
+  a.g[p] = r < a.nV ? make_double2(a.dJ_U[r], a.dJ_V[r]) : make_double2(a.dJ_Ux[r - a.nV], a.dJ_Uy[r - a.nV]);
+  const bool edge = a.slice_g[p / kSlice] == 5;
+  const bool corner = r < 4;
+  // strain rates (get_mesh_derivatives_AaAc, home term first)
+  const double2 ui = a.UV[p];
+  const double2 hn = a.h_nxy[p];
+  double ux = hn.x * ui.x, uy = hn.y * ui.x, vx = hn.x * ui.y, vy = hn.y * ui.y;
+  int nb = 0;
+  for (int k = 0; k < n; ++k) {
+    const int64_t e = sell_entry(a.slice_e0, p, k);
+    const int j = a.col[e];
+    const double2 c = a.nxy[e];
+    const double2 u = a.UV[j];
+    ux = fma(c.x, u.x, ux); uy = fma(c.y, u.x, uy);
+    vx = fma(c.x, u.y, vx); vy = fma(c.y, u.y, vy);
+    if (corner || a.slice_g[j / kSlice] != 5) ++nb;
+  }
+  const double t = uy + vx;
+  const double eps2 = (((ux * ux + vy * vy) + ux * vy) + 0.25 * (t * t)) + 1e-12;
+  const double K1 = 2.0 * ux + vy, K2 = 0.5 * t, K3 = 2.0 * vy + ux;
+  a.K[p] = K1; a.K[a.nP + p] = K2; a.K[2 * a.nP + p] = K3;
+  a.inv_nb[p] = edge && nb > 0 ? 1.0 / (double)nb : 0.0;
+  if (edge) {
+    a.ee[p] = make_double2(1.0, 1.0); a.kh[p] = make_double2(0.0, 0.0); a.alpha[p] = make_double2(0.0, 0.0);
+    a.dinv[p] = make_double2(1.0, 1.0); a.c3[p] = 0.0; a.eta[p] = 1.0; a.fr[p] = 0.0;
+    return;
+  }
+  const double pexp = (1.0 - 3.0) / (2.0 * 3.0);
+  const double eta = pow((a.m_enh * 0.5) * a.Af[p], -1.0 / 3.0) * pow(eps2, pexp);
+  const double mH = fmax(0.1, a.Hi[p]);
+  const double S = a.beta ? a.beta[p] : a.beta_const;
+  const double fr = is_floating(a.Hi[p], a.Hb[p], a.SL[p]) ? 0.0 : S / (mH * eta);
+  const double rg = kIceDensity * kGrav;
+  const double2 hc = a.h_cuv[p];
+  const double eu = hc.x - fr, ev = hc.y - fr;
+  // dF/deta * deta/d(eps2): alpha = p (fr u + rho g h / eta) / eps2
+  const double ax = pexp * (fr * ui.x + rg * a.hx[p] / eta) / eps2;
+  const double ay = pexp * (fr * ui.y + rg * a.hy[p] / eta) / eps2;
+  const double kU = K1 * hn.x + K2 * hn.y, kV = K2 * hn.x + K3 * hn.y;
+  a.ee[p] = make_double2(eu, ev);
+  a.c3[p] = 3.0 * a.sNxy[p];
+  a.kh[p] = make_double2(kU, kV);
+  a.alpha[p] = make_double2(ax, ay);
+  a.dinv[p] = make_double2(1.0 / (eu + kU * ax), 1.0 / (ev + kV * ay));
+  a.eta[p] = eta;
+  a.fr[p] = fr;
+}
+
+// Transposed coefficients per entry: entry (p -> q) holds the coefficient of u_p in
+// equation q, found through q's own entry (q -> p).
+__global__ void k_adj_entries(const AdjSetup a, double2 *cT, double2 *kT, const double2 *cuv, AdjCtl *ctl) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.nP) return;
+  const int n = a.deg[p];
+  const bool p_edge = a.slice_g[p / kSlice] == 5;
+  for (int k = 0; k < n; ++k) {
+    const int64_t e = sell_entry(a.slice_e0, p, k);
+    const int q = a.col[e];
+    const int nq = a.deg[q];
+    int64_t f = -1;
+    for (int kk = 0; kk < nq; ++kk) {
+      const int64_t e2 = sell_entry(a.slice_e0, q, kk);
+      if (a.col[e2] == p) { f = e2; break; }
+    }
+    double2 c = make_double2(0.0, 0.0), kc = make_double2(0.0, 0.0);
+    if (f < 0) {
+      atomicAdd(&ctl->not_found, 1);
+    } else if (a.slice_g[q / kSlice] == 5) {
+      // q is an edge row (averages its non-edge neighbours) or a corner (all neighbours)
+      const bool member = a.orig_of_dev[q] < 4 || !p_edge;
+      if (member) c = make_double2(-a.inv_nb[q], -a.inv_nb[q]);
+    } else {
+      c = cuv[f];
+      const double2 nq2 = a.nxy[f];
+      const double K1 = a.K[q], K2 = a.K[a.nP + q], K3 = a.K[2 * a.nP + q];
+      kc = make_double2(K1 * nq2.x + K2 * nq2.y, K2 * nq2.x + K3 * nq2.y);
+    }
+    cT[e] = c;
+    kT[e] = kc;
+  }
+}
+
+// Gradients per row (caller order out): dJ/dlog(beta^2), and the sensitivities to the
+// gathered fields hx, hy and Hi_AaAc; the adjoint state itself.
+struct AdjGrad {
+  int nP, nV;
+  const int *orig_of_dev;
+  const uint8_t *deg;
+  const uint8_t *slice_g;
+  const double2 *UV, *mu;
+  const double *eta, *fr, *Hi;
+  double *d_logbeta, *s_hx, *s_hy, *s_H, *lam_U, *lam_V;   // [nA] caller order
+};
+
+__global__ void k_adj_grad(const AdjGrad a) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.nP) return;
+  const int r = a.orig_of_dev[p];
+  if (r < 0 || a.deg[p] == 0) return;
+  const double2 m = a.mu[p];
+  a.lam_U[r] = m.x;
+  a.lam_V[r] = m.y;
+  if (a.slice_g[p / kSlice] == 5) {
+    a.d_logbeta[r] = 0.0; a.s_hx[r] = 0.0; a.s_hy[r] = 0.0; a.s_H[r] = 0.0;
+    return;
+  }
+  const double2 u = a.UV[p];
+  const double w = a.fr[p] * fma(m.x, u.x, m.y * u.y);
+  const double rg = kIceDensity * kGrav;
+  a.d_logbeta[r] = w;
+  a.s_hx[r] = rg * m.x / a.eta[p];
+  a.s_hy[r] = rg * m.y / a.eta[p];
+  a.s_H[r] = a.Hi[p] > 0.1 ? -w / a.Hi[p] : 0.0;
+}
+
+// dJ/dHi on Aa from the field sensitivities: Hi_AaAc (identity on Aa rows, the mean of the
+// two end vertices on Ac rows) and the driving-stress slopes (Aa and Ac derivative
+// stencils of Hs, or (1 - rho_i/rho_sw) times those of Hi on floating rows), masks frozen.
+struct AdjGeom {
+  int nV, nAc, ncm;
+  const int *dev_of_orig;
+  const double *Hi, *Hb, *SL;        // device order fields
+  const double *s_hx, *s_hy, *s_H;   // caller order sensitivities
+  const int *nC, *C;                 // (nV), (nV, ncm) 1-based
+  const double *Nx, *Ny;             // (nV, ncm + 1)
+  const int *Aci;                    // (nAc, 4) 1-based
+  const double *Nx_Ac, *Ny_Ac;       // (nAc, 4)
+  double *dHi;                       // (nV), zeroed
+};
+
+__device__ __forceinline__ double hs_slope(const AdjGeom &a, int v) {
+  const int p = a.dev_of_orig[v];
+  return is_floating(a.Hi[p], a.Hb[p], a.SL[p]) ? 1.0 - kIceDensity / kSeawaterDensity : 1.0;
+}
+
+__global__ void k_adj_geom(const AdjGeom a) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nA = a.nV + a.nAc;
+  if (r >= nA) return;
+  const double shx = a.s_hx[r], shy = a.s_hy[r], sH = a.s_H[r];
+  const int p = a.dev_of_orig[r];
+  const bool ocean = is_floating(a.Hi[p], a.Hb[p], a.SL[p]);
+  const double shelf = 1.0 - kIceDensity / kSeawaterDensity;
+  if (r < a.nV) {
+    const int v = r;
+    if (sH != 0.0) atomicAdd(&a.dHi[v], sH);
+    if (shx == 0.0 && shy == 0.0) return;
+    const int n = a.nC[v];
+    for (int c = 0; c <= n; ++c) {
+      const int k = c < n ? a.C[v + (size_t)c * a.nV] - 1 : v;
+      const double fac = ocean ? shelf : hs_slope(a, k);
+      const double w = shx * a.Nx[v + (size_t)c * a.nV] + shy * a.Ny[v + (size_t)c * a.nV];
+      atomicAdd(&a.dHi[k], w * fac);
+    }
+  } else {
+    const int ac = r - a.nV;
+    if (sH != 0.0) {
+      atomicAdd(&a.dHi[a.Aci[ac] - 1], 0.5 * sH);
+      atomicAdd(&a.dHi[a.Aci[ac + a.nAc] - 1], 0.5 * sH);
+    }
+    if (shx == 0.0 && shy == 0.0) return;
+    for (int c = 0; c < 4; ++c) {
+      const int k = a.Aci[ac + (size_t)c * a.nAc] - 1;
+      if (k < 0) continue;
+      const double fac = ocean ? shelf : hs_slope(a, k);
+      const double w = shx * a.Nx_Ac[ac + (size_t)c * a.nAc] + shy * a.Ny_Ac[ac + (size_t)c * a.nAc];
+      atomicAdd(&a.dHi[k], w * fac);
+    }
   }
 }
 
@@ -1931,4 +2296,202 @@ extern "C" int ufe_batch_autotune(int32_t n, const ufe_mesh_desc *descs, const u
   if (best_ms == 1e300) { set_error("ufe_batch_autotune: no candidate fits these members"); return UFE_BAD_ARG; }
   *best = best_cfg;
   return UFE_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// VJP of the converged solve (no counterpart in the reference)
+// ---------------------------------------------------------------------------------------
+namespace ufe {
+
+struct AdjWork {
+  int nP = 0, nV = 0, nAc = 0, nA = 0;
+  int64_t nE = 0;
+  double2 *cT = nullptr, *kT = nullptr;
+  double2 *ee = nullptr, *kh = nullptr, *alpha = nullptr, *dinv = nullptr, *g = nullptr, *mu = nullptr;
+  double *c3 = nullptr, *s = nullptr, *eta = nullptr, *fr = nullptr, *inv_nb = nullptr, *K = nullptr;
+  double *stage = nullptr;        // dJ/du in (4 blocks), sensitivities out (6 nA), dHi (nV)
+  int *geom_int = nullptr;        // nC, C, Aci
+  double *geom_dbl = nullptr;     // Nx, Ny, Nx_Ac, Ny_Ac
+  unsigned int *prog = nullptr;
+  AdjCtl *ctl = nullptr;
+  AdjCtl *ctl_host = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+void adj_free(AdjWork *w) {
+  if (!w) return;
+  void *ptrs[] = {w->cT, w->kT, w->ee, w->kh, w->alpha, w->dinv, w->g, w->mu, w->c3, w->s, w->eta, w->fr,
+                  w->inv_nb, w->K, w->stage, w->geom_int, w->geom_dbl, w->prog, w->ctl};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (w->ctl_host) cudaFreeHost(w->ctl_host);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  delete w;
+}
+
+namespace {
+
+int ensure_adj(ufe_mesh_h h) {
+  if (h->adj) return UFE_OK;
+  const DevMesh &m = h->m;
+  AdjWork *w = new AdjWork();
+  w->nP = m.nP; w->nV = m.nV; w->nAc = m.nAc; w->nA = m.nA; w->nE = m.nE;
+  const size_t nP = m.nP, nE = (size_t)m.nE, nA = m.nA, nV = m.nV, nAc = m.nAc, ncm = m.ncm;
+  int rc = cuda_status(cudaMalloc(&w->cT, nE * sizeof(double2)), "adj cT");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->kT, nE * sizeof(double2)), "adj kT");
+  double2 **d2[] = {&w->ee, &w->kh, &w->alpha, &w->dinv, &w->g, &w->mu};
+  for (double2 **q : d2)
+    if (!rc) rc = cuda_status(cudaMalloc(q, nP * sizeof(double2)), "adj rows");
+  double **d1[] = {&w->c3, &w->s, &w->eta, &w->fr, &w->inv_nb};
+  for (double **q : d1)
+    if (!rc) rc = cuda_status(cudaMalloc(q, nP * sizeof(double)), "adj rows");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->K, 3 * nP * sizeof(double)), "adj strain");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->stage, (2 * nV + 2 * nAc + 6 * nA + nV) * sizeof(double)), "adj stage");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->geom_int, (nV + nV * ncm + 4 * nAc) * sizeof(int)), "adj geom");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->geom_dbl, (2 * nV * (ncm + 1) + 8 * nAc) * sizeof(double)), "adj geom");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->prog, 32 * (size_t)m.n_patch * sizeof(unsigned int)), "adj progress");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(AdjCtl)), "adj ctl");
+  if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(AdjCtl)), "adj ctl host");
+  if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
+  if (!rc) rc = cuda_status(cudaEventCreate(&w->ev1), "event");
+  if (!rc) {
+    int per_sm = 0;
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)ssa_adjoint_sor, kSsaBlock, 0),
+                     "occupancy");
+    if (!rc && per_sm * h->num_sms < m.n_patch) {
+      set_error("ssa adjoint: not enough co-resident CTAs for one per patch");
+      rc = UFE_CUDA_ERROR;
+    }
+  }
+  if (rc) { adj_free(w); return rc; }
+  h->adj = w;
+  return UFE_OK;
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_params *vp, const ufe_vjp_in *in,
+                           const ufe_vjp_geom *geom, ufe_vjp_out *out, ufe_vjp_stats *stats) {
+  if (!h || !p || !in || !out) { set_error("ufe_ssa_vjp: null argument"); return UFE_BAD_ARG; }
+  SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) { set_error("ufe_ssa_vjp: no solve on this mesh handle"); return UFE_BAD_ARG; }
+  if (w->zero) { set_error("ufe_ssa_vjp: the last solve took the zero-velocity early-out"); return UFE_BAD_ARG; }
+  if (w->gl) { set_error("ufe_ssa_vjp: the grounding-line flux option is not differentiated"); return UFE_BAD_ARG; }
+  if (p->sliding_law != UFE_SLIDING_LINEAR) {
+    set_error("ufe_ssa_vjp: the adjoint is implemented for the linear sliding law (S = beta^2)");
+    return UFE_BAD_ARG;
+  }
+  if (!in->dJ_dU || !in->dJ_dV || !in->dJ_dUx_Ac || !in->dJ_dUy_Ac) { set_error("ufe_ssa_vjp: missing dJ/du"); return UFE_BAD_ARG; }
+  if (out->dJ_dHi && (!geom || !geom->nC || !geom->C || !geom->Nx || !geom->Ny || !geom->Aci || !geom->Nx_Ac || !geom->Ny_Ac)) {
+    set_error("ufe_ssa_vjp: dJ_dHi needs the Aa and Ac derivative stencils (ufe_vjp_geom)");
+    return UFE_BAD_ARG;
+  }
+  int rc = ensure_adj(h);
+  if (rc) return rc;
+  AdjWork *a = h->adj;
+  const DevMesh &m = h->m;
+  cudaStream_t s = h->stream;
+  const size_t nV = m.nV, nAc = m.nAc, nA = m.nA, nP = m.nP, ncm = m.ncm;
+  const double tol = vp && vp->tol > 0 ? vp->tol : 1e-12;
+  const int max_sweeps = vp && vp->max_sweeps > 0 ? vp->max_sweeps : 200000;
+  const double omega = vp && vp->omega > 0 ? vp->omega : p->SSA_SOR_omega;
+  double *st = a->stage;
+  double *gU = st, *gV = st + nV, *gUx = st + 2 * nV, *gUy = gUx + nAc;
+  double *o_lb = gUy + nAc, *o_hx = o_lb + nA, *o_hy = o_hx + nA, *o_H = o_hy + nA, *o_lU = o_H + nA, *o_lV = o_lU + nA;
+  double *o_dHi = o_lV + nA;
+  std::memset(a->ctl_host, 0, sizeof(AdjCtl));
+  rc = cuda_status(cudaEventRecord(a->ev0, s), "event");
+  if (!rc) rc = h2d(gU, in->dJ_dU, nV, s);
+  if (!rc) rc = h2d(gV, in->dJ_dV, nV, s);
+  if (!rc) rc = h2d(gUx, in->dJ_dUx_Ac, nAc, s);
+  if (!rc) rc = h2d(gUy, in->dJ_dUy_Ac, nAc, s);
+  if (!rc) rc = cuda_status(cudaMemsetAsync(a->ctl, 0, sizeof(AdjCtl), s), "memset adj ctl");
+  if (!rc) rc = cuda_status(cudaMemsetAsync(a->prog, 0, 32 * (size_t)m.n_patch * sizeof(unsigned int), s), "memset prog");
+  const double *F = w->f;
+  AdjSetup su;
+  su.nP = (int)nP; su.nV = (int)nV; su.col = m.col; su.deg = m.deg; su.slice_e0 = m.slice_e0; su.slice_g = m.slice_g;
+  su.orig_of_dev = m.orig_of_dev; su.nxy = m.nxy; su.h_nxy = m.h_nxy; su.h_cuv = m.h_cuv; su.sNxy = m.sNxy;
+  su.Hi = F + F_HI * nP; su.Hb = F + F_HB * nP; su.SL = F + F_SL * nP; su.hx = F + F_HX * nP; su.hy = F + F_HY * nP;
+  su.Af = F + F_AF * nP; su.beta = w->has_beta ? F + F_BETA * nP : nullptr;
+  su.beta_const = p->beta_sq; su.m_enh = p->m_enh_ssa; su.UV = w->UV;
+  su.dJ_U = gU; su.dJ_V = gV; su.dJ_Ux = gUx; su.dJ_Uy = gUy;
+  su.ee = a->ee; su.kh = a->kh; su.alpha = a->alpha; su.dinv = a->dinv; su.g = a->g; su.mu = a->mu;
+  su.c3 = a->c3; su.s = a->s; su.eta = a->eta; su.fr = a->fr; su.inv_nb = a->inv_nb; su.K = a->K; su.omega = omega;
+  const unsigned gb = (unsigned)((nP + 255) / 256);
+  if (!rc) {
+    k_adj_rows<<<gb, 256, 0, s>>>(su);
+    rc = cuda_status(cudaGetLastError(), "k_adj_rows");
+  }
+  if (!rc) {
+    k_adj_entries<<<gb, 256, 0, s>>>(su, a->cT, a->kT, m.cuv, a->ctl);
+    rc = cuda_status(cudaGetLastError(), "k_adj_entries");
+  }
+  AdjArgs aa;
+  aa.col = m.col; aa.deg = m.deg; aa.orig_of_dev = m.orig_of_dev; aa.slice_e0 = m.slice_e0; aa.slice_w = m.slice_w;
+  aa.patch_slice = m.patch_slice; aa.patch_edge0 = m.patch_edge0; aa.sync_ptr = m.sync_ptr; aa.sync_list = m.sync_list;
+  aa.prog = a->prog; aa.cT = a->cT; aa.kT = a->kT; aa.ee = a->ee; aa.c3 = a->c3; aa.kh = a->kh; aa.alpha = a->alpha;
+  aa.dinv = a->dinv; aa.g = a->g; aa.mu = a->mu; aa.s = a->s; aa.ctl = a->ctl; aa.omega = omega; aa.tol = tol;
+  aa.max_sweeps = max_sweeps; aa.timeout_ns = 20LL * 1000 * 1000 * 1000;
+  if (!rc) {
+    void *args[] = {(void *)&aa};
+    rc = cuda_status(cudaLaunchCooperativeKernel((const void *)ssa_adjoint_sor, dim3(m.n_patch), dim3(kSsaBlock), args, 0, s),
+                     "ssa_adjoint_sor");
+  }
+  AdjGrad ag;
+  ag.nP = (int)nP; ag.nV = (int)nV; ag.orig_of_dev = m.orig_of_dev; ag.deg = m.deg; ag.slice_g = m.slice_g;
+  ag.UV = w->UV; ag.mu = a->mu; ag.eta = a->eta; ag.fr = a->fr; ag.Hi = F + F_HI * nP;
+  ag.d_logbeta = o_lb; ag.s_hx = o_hx; ag.s_hy = o_hy; ag.s_H = o_H; ag.lam_U = o_lU; ag.lam_V = o_lV;
+  if (!rc) {
+    k_adj_grad<<<gb, 256, 0, s>>>(ag);
+    rc = cuda_status(cudaGetLastError(), "k_adj_grad");
+  }
+  if (!rc && out->dJ_dHi) {
+    int *gi = a->geom_int;
+    double *gd = a->geom_dbl;
+    rc = cuda_status(cudaMemcpyAsync(gi, geom->nC, nV * sizeof(int), cudaMemcpyHostToDevice, s), "H2D geom");
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(gi + nV, geom->C, nV * ncm * sizeof(int), cudaMemcpyHostToDevice, s), "H2D geom");
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(gi + nV + nV * ncm, geom->Aci, 4 * nAc * sizeof(int), cudaMemcpyHostToDevice, s), "H2D geom");
+    if (!rc) rc = h2d(gd, geom->Nx, nV * (ncm + 1), s);
+    if (!rc) rc = h2d(gd + nV * (ncm + 1), geom->Ny, nV * (ncm + 1), s);
+    if (!rc) rc = h2d(gd + 2 * nV * (ncm + 1), geom->Nx_Ac, 4 * nAc, s);
+    if (!rc) rc = h2d(gd + 2 * nV * (ncm + 1) + 4 * nAc, geom->Ny_Ac, 4 * nAc, s);
+    if (!rc) rc = cuda_status(cudaMemsetAsync(o_dHi, 0, nV * sizeof(double), s), "memset dHi");
+    AdjGeom ge;
+    ge.nV = (int)nV; ge.nAc = (int)nAc; ge.ncm = (int)ncm; ge.dev_of_orig = m.dev_of_orig;
+    ge.Hi = F + F_HI * nP; ge.Hb = F + F_HB * nP; ge.SL = F + F_SL * nP;
+    ge.s_hx = o_hx; ge.s_hy = o_hy; ge.s_H = o_H; ge.nC = gi; ge.C = gi + nV; ge.Aci = gi + nV + nV * ncm;
+    ge.Nx = gd; ge.Ny = gd + nV * (ncm + 1); ge.Nx_Ac = gd + 2 * nV * (ncm + 1); ge.Ny_Ac = ge.Nx_Ac + 4 * nAc;
+    ge.dHi = o_dHi;
+    if (!rc) {
+      k_adj_geom<<<(unsigned)((nA + 255) / 256), 256, 0, s>>>(ge);
+      rc = cuda_status(cudaGetLastError(), "k_adj_geom");
+    }
+  }
+  if (!rc) rc = cuda_status(cudaEventRecord(a->ev1, s), "event");
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(a->ctl_host, a->ctl, sizeof(AdjCtl), cudaMemcpyDeviceToHost, s), "ctl D2H");
+  if (!rc) rc = d2h(out->dJ_dlogbeta_sq_AaAc, o_lb, nA, s);
+  if (!rc) rc = d2h(out->dJ_dhx_AaAc, o_hx, nA, s);
+  if (!rc) rc = d2h(out->dJ_dhy_AaAc, o_hy, nA, s);
+  if (!rc) rc = d2h(out->dJ_dHi_AaAc, o_H, nA, s);
+  if (!rc) rc = d2h(out->lambda_U_AaAc, o_lU, nA, s);
+  if (!rc) rc = d2h(out->lambda_V_AaAc, o_lV, nA, s);
+  if (!rc && out->dJ_dHi) rc = d2h(out->dJ_dHi, o_dHi, nV, s);
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa vjp");
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a->ev0, a->ev1);
+  const AdjCtl &c = *a->ctl_host;
+  int status = c.status;
+  if (c.err) { status = c.err; set_error("ufe_ssa_vjp: a device-side bounded wait timed out"); }
+  else if (c.not_found) { status = UFE_BAD_MESH; set_error("ufe_ssa_vjp: the AaAc neighbour relation is not symmetric"); }
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->status = status;
+    stats->sweeps = c.sweeps;
+    stats->last_rel_update = c.last_rel;
+    stats->device_ms = ms;
+  }
+  return status;
 }
