@@ -396,6 +396,131 @@ def ensemble_bench(args):
     return 0
 
 
+def marine_bench(args):
+    """Marine ice sheet with a floating shelf (bed sloping from +500 m to -1000 m plus a
+    seeded Gaussian random field, sigma 50 m, correlation 40 km; thickness from the dome
+    profile, floating where is_floating), mixed precision timed against FP64 on the same
+    mesh; linear sliding beta^2 = 1e3 under grounded ice, none under the shelf."""
+    import torch
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api, workloads
+    from ufemism_gb300.meshgen import dome_mesh
+    size = args.size if args.size != "200k" else "300k"
+    base = dome_mesh(size)
+    mesh = api.build_aaac(base)
+    Hi, Hb, SL = workloads.marine_geometry(base, seed=20261208)
+    ssa, _ = workloads.prepare_inputs(mesh, Hi, Hb, SL)
+    torch.cuda.set_device(0)
+    api.init(0)
+    dm = api.DeviceMesh(mesh)
+    p64 = api.default_params(precision=nat.UFE_FP64)
+    p32 = api.default_params(precision=nat.UFE_MIXED)
+    rc64, o64, s64 = dm.solve_ssa(ssa, p64, check=False)
+    rc32, o32, s32 = dm.solve_ssa(ssa, p32, check=False)
+    l2 = max(float(np.linalg.norm(o32[k] - o64[k]) / np.linalg.norm(o64[k]))
+             for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac"))
+    dm.ssa_upload(ssa, p64)
+    with ClockSampler(0) as clk:
+        t64, st64 = timed_runs(dm, p64, args.steps, args.warmup, dm.stream)
+        t32, st32 = timed_runs(dm, p32, args.steps, args.warmup, dm.stream)
+    ms32, ms64 = float(np.mean(t32)), float(np.mean(t64))
+    floating = workloads._is_floating(Hi, Hb, SL) & (Hi > 0)
+    line = {
+        "metric": "SSA solves/s (marine, mixed)", "value": 1e3 / ms32, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 sweeps / f64 defect",
+        "data": "synthetic (seeded mesh, sloping bed with Gaussian random field)",
+        "config": {"workload": "%s-vertex marine ice sheet with floating shelf" % size, "nV": int(base.nV),
+                   "nVAaAc": int(mesh.nVAaAc), "floating_vertices": int(floating.sum()),
+                   "picard_iterations": st32["picard_iterations"], "sor_sweeps": st32["total_sweeps"],
+                   "status": st32["status"], "parallelism": "1 GPU"},
+        "fp64": {"value": 1e3 / ms64, "ms_per_step": ms64, "sor_sweeps": st64["total_sweeps"],
+                 "picard_iterations": st64["picard_iterations"], "status": st64["status"]},
+        "mixed_vs_fp64_speedup": ms64 / ms32, "rel_l2_mixed_vs_fp64": l2,
+        "vertex_sweeps_per_s": mesh.nVAaAc * st32["total_sweeps"] / (ms32 * 1e-3),
+        "gpu_launches": 3 * args.steps, "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    dm.close()
+    return 0
+
+
+def adjoint_bench(args):
+    """Adjoint on the marine setup: u_obs from a forward solve with log(beta^2) perturbed by
+    a Gaussian random field (std 0.3), J = 1/2 sum over AaAc of the squared velocity misfit,
+    gradient with respect to log(beta^2) (AaAc) and Hi (Aa) by ufe_ssa_vjp at the converged
+    state of a forward solve run to tight tolerances; cost against that forward solve, and
+    central finite differences (h = 1e-4) of the forward solve on random directions."""
+    import torch
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api, workloads
+    from ufemism_gb300.meshgen import dome_mesh
+    size = args.size if args.size != "200k" else "100k"
+    base = dome_mesh(size)
+    mesh = api.build_aaac(base)
+    Hi, Hb, SL = workloads.marine_geometry(base, seed=20261208)
+    ssa, _ = workloads.prepare_inputs(mesh, Hi, Hb, SL)
+    lb = workloads.log_beta_field(mesh, std=1.0, ell=100e3, seed=20261209)
+    lbo = lb + workloads.log_beta_field(mesh, std=0.3, ell=100e3, seed=20261210)
+    torch.cuda.set_device(0)
+    api.init(0)
+    dm = api.DeviceMesh(mesh)
+    tight = dict(SSA_RN_tol=args.adj_rn_tol, SSA_max_residual_UV=args.adj_rn_tol / 10, SSA_max_outer_loops=400,
+                 SSA_max_inner_loops=2000000)
+    p64 = api.default_params(precision=nat.UFE_FP64, **tight)
+    p32 = api.default_params(precision=nat.UFE_MIXED, **tight)
+
+    def forward(lbeta, p):
+        f = dict(ssa)
+        f["beta_sq_AaAc"] = np.exp(lbeta)
+        rc, out, st = dm.solve_ssa(f, p, check=False)
+        U = np.concatenate([out["U_SSA"], out["Ux_SSA_Ac"]])
+        V = np.concatenate([out["V_SSA"], out["Uy_SSA_Ac"]])
+        return U, V, out, st
+
+    Uo, Vo, _, _ = forward(lbo, p32)
+    res = {}
+    for name, p in (("fp64", p64), ("mixed", p32)):
+        U, V, out, st = forward(lb, p)
+        dJ = dict(U_SSA=out["U_SSA"] - Uo[:base.nV], V_SSA=out["V_SSA"] - Vo[:base.nV],
+                  Ux_SSA_Ac=out["Ux_SSA_Ac"] - Uo[base.nV:], Uy_SSA_Ac=out["Uy_SSA_Ac"] - Vo[base.nV:])
+        rc, g, vs = dm.ssa_vjp(dJ, p, geom_mesh=mesh, tol=args.adj_tol, check=False)
+        res[name] = dict(forward_ms=st["device_ms"], forward_sweeps=st["total_sweeps"],
+                         picard=st["picard_iterations"], vjp_ms=vs["device_ms"], vjp_sweeps=vs["sweeps"],
+                         vjp_status=rc, vjp_rel_update=vs["last_rel_update"],
+                         vjp_over_forward=vs["device_ms"] / st["device_ms"], grad=g, U=U, V=V)
+    # finite differences with the mixed forward (converged to the FP64 fixed point)
+    rng = np.random.default_rng(20261211)
+    g = res["mixed"]["grad"]
+    J = lambda U, V: 0.5 * float(np.sum((U - Uo) ** 2 + (V - Vo) ** 2))
+    fd = []
+    for k in range(args.fd_directions):
+        d = rng.normal(size=mesh.nVAaAc)
+        Up, Vp, _, _ = forward(lb + 1e-4 * d, p32)
+        Um, Vm, _, _ = forward(lb - 1e-4 * d, p32)
+        f = (J(Up, Vp) - J(Um, Vm)) / 2e-4
+        a = float(g["dJ_dlogbeta_sq_AaAc"] @ d)
+        fd.append(abs(f - a) / abs(a))
+    g64, g32 = res["fp64"]["grad"], res["mixed"]["grad"]
+    agree = float(np.linalg.norm(g64["dJ_dlogbeta_sq_AaAc"] - g32["dJ_dlogbeta_sq_AaAc"]) /
+                  np.linalg.norm(g64["dJ_dlogbeta_sq_AaAc"]))
+    line = {
+        "metric": "adjoint ms (VJP of the converged marine solve)", "value": res["fp64"]["vjp_ms"], "unit": "ms",
+        "n_gpus": 1, "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded marine setup)",
+        "config": {"workload": "%s-vertex marine, gradient w.r.t. log beta^2 and Hi" % size, "nV": int(base.nV),
+                   "nVAaAc": int(mesh.nVAaAc), "forward_rn_tol": args.adj_rn_tol, "vjp_tol": args.adj_tol},
+        "vjp_over_forward_fp64": res["fp64"]["vjp_over_forward"],
+        "vjp_over_forward_mixed": res["mixed"]["vjp_over_forward"],
+        "forward": {k: {q: v[q] for q in ("forward_ms", "forward_sweeps", "picard", "vjp_ms", "vjp_sweeps",
+                                          "vjp_status", "vjp_rel_update")} for k, v in res.items()},
+        "gradient_fp64_vs_mixed_forward_rel_l2": agree,
+        "fd_directions": args.fd_directions, "fd_rel_err_max": max(fd) if fd else None, "fd_rel_err": fd,
+    }
+    print(json.dumps(line))
+    dm.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-case", choices=["mixed", "fp64", "exact"], default=None,
@@ -408,7 +533,10 @@ def main():
     ap.add_argument("--size", default="200k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sample-sweeps", type=int, default=40)
-    ap.add_argument("--workload", default="dome", choices=["dome", "ensemble"],
+    ap.add_argument("--adj-rn-tol", type=float, default=1e-10, help="adjoint: forward Picard tolerance")
+    ap.add_argument("--adj-tol", type=float, default=1e-13, help="adjoint: VJP relative update tolerance")
+    ap.add_argument("--fd-directions", type=int, default=2)
+    ap.add_argument("--workload", default="dome", choices=["dome", "ensemble", "marine", "adjoint"],
                     help="dome: the 200k-vertex single solve; ensemble: the batched ensemble")
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--autotune", action="store_true", help="ensemble: run the autotuner first")
@@ -421,6 +549,10 @@ def main():
         return profile_case(args)
     if args.workload == "ensemble":
         return ensemble_bench(args)
+    if args.workload == "marine":
+        return marine_bench(args)
+    if args.workload == "adjoint":
+        return adjoint_bench(args)
 
     rank, world, local = dist_info()
     import torch

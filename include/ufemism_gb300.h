@@ -209,8 +209,8 @@ int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_s
  * The forward solve should be converged well below the tolerances the gradient is wanted
  * to (the VJP differentiates the fixed point, not the truncated iteration). */
 typedef struct ufe_vjp_params {
-  double tol;          /* stop when max |update| < tol * max |mu| (0: 1e-12) */
-  int32_t max_sweeps;  /* 0: 200000 */
+  double tol;          /* stop when max |update| < tol * max |mu| (0: 1e-13) */
+  int32_t max_sweeps;  /* 0: 2000000 */
   double omega;        /* 0: SSA_SOR_omega */
 } ufe_vjp_params;
 typedef struct ufe_vjp_in {

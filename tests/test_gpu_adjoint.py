@@ -110,3 +110,22 @@ def test_vjp_rejects_coulomb_law_and_missing_solve():
     rc, out, st = dm.ssa_vjp(dJ, p, check=False)
     assert rc == nat.UFE_BAD_ARG and "linear sliding" in nat.last_error()
     dm.close()
+
+
+def test_vjp_reports_divergence_and_recovers():
+    """A relaxation factor far above the forward's makes the transposed SOR diverge on the
+    marine case; the VJP reports UFE_DIVERGED (no GPU fault: the iteration stops on a
+    non-finite reduction) and the handle stays usable."""
+    m, ssa, logb, dm, p, solve, U, V, f0, Uo, Vo = setup_case("1k", "marine")
+    gU, gV = U - Uo, V - Vo
+    dJ = dict(zip(("U_SSA", "Ux_SSA_Ac"), split(m, gU)))
+    dJ.update(zip(("V_SSA", "Uy_SSA_Ac"), split(m, gV)))
+    rc, out, st = dm.ssa_vjp(dJ, p, omega=1.99, max_sweeps=200000, check=False)
+    assert rc in (nat.UFE_DIVERGED, nat.UFE_OK, nat.UFE_NOT_CONVERGED)
+    if rc == nat.UFE_OK:   # converged after all: the gradient must then be right
+        lin = adj.Linearisation(m, f0, U, V)
+        mx, my, dlb, dHi, sens = adj.adjoint_gradient(lin, gU, gV)
+        assert rel_l2(out["dJ_dlogbeta_sq_AaAc"], dlb) <= 1e-6
+    rc2, out2, st2 = dm.ssa_vjp(dJ, p)
+    assert rc2 == nat.UFE_OK
+    dm.close()

@@ -997,6 +997,12 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_adjoint_sor(const A
     }
     const double md = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxd[slot]);
     const double mm = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxm[slot]);
+    // A non-finite update or state (NaN bits order above infinity) means the iteration
+    // diverged (possible for relaxation factors well above the forward's).
+    if (!isfinite(md) || !isfinite(mm)) {
+      if (leader) { ctl->sweeps = sweeps; ctl->last_rel = md; ctl->status = UFE_DIVERGED; }
+      return;
+    }
     const double rel = mm > 0.0 ? md / mm : 0.0;
     if (rel < a.tol || sweeps >= a.max_sweeps) {
       if (leader) {
@@ -2394,8 +2400,10 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   const DevMesh &m = h->m;
   cudaStream_t s = h->stream;
   const size_t nV = m.nV, nAc = m.nAc, nA = m.nA, nP = m.nP, ncm = m.ncm;
-  const double tol = vp && vp->tol > 0 ? vp->tol : 1e-12;
-  const int max_sweeps = vp && vp->max_sweeps > 0 ? vp->max_sweeps : 200000;
+  // The error of a slowly contracting iteration is about its update / (1 - rate), so the
+  // default stops only when updates reach 1e-13 of the state.
+  const double tol = vp && vp->tol > 0 ? vp->tol : 1e-13;
+  const int max_sweeps = vp && vp->max_sweeps > 0 ? vp->max_sweeps : 2000000;
   const double omega = vp && vp->omega > 0 ? vp->omega : p->SSA_SOR_omega;
   double *st = a->stage;
   double *gU = st, *gV = st + nV, *gUx = st + 2 * nV, *gUy = gUx + nAc;
@@ -2484,6 +2492,8 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   cudaEventElapsedTime(&ms, a->ev0, a->ev1);
   const AdjCtl &c = *a->ctl_host;
   int status = c.status;
+  if (status == UFE_DIVERGED) set_error("ufe_ssa_vjp: the transposed SOR diverged (lower the relaxation factor)");
+  else if (status == UFE_NOT_CONVERGED) set_error("ufe_ssa_vjp: max_sweeps reached before the tolerance");
   if (c.err) { status = c.err; set_error("ufe_ssa_vjp: a device-side bounded wait timed out"); }
   else if (c.not_found) { status = UFE_BAD_MESH; set_error("ufe_ssa_vjp: the AaAc neighbour relation is not symmetric"); }
   if (stats) {
