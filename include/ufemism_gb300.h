@@ -198,6 +198,57 @@ int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *i
 int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
                           ufe_sia_out *out);
 
+/* Geometry preparation on the device: the fields update_general_ice_model_data
+ * (general_ice_model_data_module.f90:23-96) derives from Hi, Hb and SL for the velocity
+ * solve — Aa-to-Ac maps, Hs, ocean/ice/sheet/shelf masks on Aa and Ac, the grounding-line
+ * mask on Ac, the Aa slopes of Hi and Hs, the Ac slopes of Hi, Hb, Hs and SL, and the shelf
+ * slopes — bit-identical to the reference's. ufe_geometry_attach uploads the derivative
+ * stencils once per mesh; ufe_ssa_upload_geometry then replaces ufe_ssa_upload with only
+ * Hi, Hb, SL, the flow factor and the optional friction field crossing from the host. */
+typedef struct ufe_geometry_mesh {
+  const int32_t *nC, *C;                /* (nV), (nV,nC_mem) */
+  const double *Nx, *Ny;                /* (nV,nC_mem+1) Aa neighbour functions */
+  const int32_t *Aci;                   /* (nAc,4) */
+  const double *Nx_Ac, *Ny_Ac, *No_Ac;  /* (nAc,4) */
+  const double *Np_Ac;                  /* (nAc) */
+} ufe_geometry_mesh;
+typedef struct ufe_geometry_out {       /* host arrays, each may be NULL */
+  double *Hs, *dHi_dx, *dHi_dy, *dHs_dx, *dHs_dy, *dHs_dx_shelf, *dHs_dy_shelf;     /* (nV) */
+  int32_t *mask_ocean, *mask_ice, *mask_sheet, *mask_shelf;                        /* (nV) */
+  double *Hi_Ac, *Hb_Ac, *SL_Ac, *Hs_Ac;                                            /* (nAc) */
+  double *dHi_dx_Ac, *dHi_dy_Ac, *dHi_dp_Ac, *dHi_do_Ac, *dHb_dx_Ac, *dHb_dy_Ac, *dHb_dp_Ac, *dHb_do_Ac;
+  double *dHs_dx_Ac, *dHs_dy_Ac, *dHs_dp_Ac, *dHs_do_Ac, *dSL_dx_Ac, *dSL_dy_Ac, *dSL_dp_Ac, *dSL_do_Ac;
+  double *dHs_dx_shelf_Ac, *dHs_dy_shelf_Ac;                                        /* (nAc) */
+  int32_t *mask_ocean_Ac, *mask_ice_Ac, *mask_sheet_Ac, *mask_shelf_Ac, *mask_gl_Ac; /* (nAc) */
+} ufe_geometry_out;
+int ufe_geometry_attach(ufe_mesh_h mesh, const ufe_geometry_mesh *geometry);
+int ufe_geometry_update(ufe_mesh_h mesh, const double *Hi, const double *Hb, const double *SL,
+                        ufe_geometry_out *out);
+int ufe_ssa_upload_geometry(ufe_mesh_h mesh, const ufe_params *params, const double *Hi, const double *Hb,
+                            const double *SL, const double *A_flow_mean, const double *A_flow_mean_Ac,
+                            const double *beta_sq_AaAc, const ufe_ssa_inout *inout);
+
+/* calculate_ice_thickness_change (ice_dynamics_module.f90:31-237) on the device: upwind ice
+ * volume fluxes across every Aa connection from Up_SIA_Ac + Up_SSA_Ac, the outflux rescale
+ * against the available ice plus SMB and BMB, dHi/dt, the update of Hi (in place), the
+ * domain-edge rule and the no-ice mask. NULL velocity arrays take the handle's last SSA / SIA
+ * solution from the device (the velocities never leave it). Needs ufe_geometry_attach (the
+ * mesh's C and Aci). */
+typedef struct ufe_thickness_in {
+  const double *A;                      /* (nV) Voronoi cell areas */
+  const double *Cw;                     /* (nV,nC_mem) connection widths */
+  const double *Up_SIA_Ac, *Up_SSA_Ac;  /* (nAc), or NULL: the handle's last solves */
+  const double *SMB_year, *BMB;         /* (nV) */
+  const int32_t *mask_noice;            /* (nV) or NULL */
+  double dt;
+  int32_t zero_edges;                   /* 1: Hi = 0 on domain-edge vertices (all configurations but SSA_icestream) */
+} ufe_thickness_in;
+typedef struct ufe_thickness_out {      /* host arrays, each may be NULL */
+  double *Hi_prev, *dHi_dt;             /* (nV) */
+  double *dVi_in;                       /* (nV,nC_mem) the rescaled fluxes */
+} ufe_thickness_out;
+int ufe_thickness_update(ufe_mesh_h mesh, const ufe_thickness_in *in, double *Hi, ufe_thickness_out *out);
+
 /* VJP of the converged solve (no counterpart in the reference): for a misfit J(u) of the
  * velocities of the last ufe_ssa_solve / ufe_ssa_run on this handle, solves the adjoint
  * system (dF/du)^T mu = dJ/du of the discrete fixed point F(u) = 0 the Picard/SOR loop

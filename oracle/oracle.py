@@ -27,7 +27,7 @@ ZETA_DEFAULT = np.array([0.00, 0.10, 0.20, 0.30, 0.40, 0.50, 0.60, 0.70, 0.80, 0
 def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB) or any(
             os.path.getmtime(os.path.join(_HERE, f)) > os.path.getmtime(_LIB)
-            for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle.h")):
+            for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle_thickness.c", "ufe_oracle.h")):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
 
@@ -317,3 +317,25 @@ def ddx_ddy_aaac(m: AaAcMesh, d):
     ms = _aaac_struct(m)
     lib().or_ddx_ddy_AaAc(ct.byref(ms), ct.c_int(m.base.C.shape[1]), _vp(d), _vp(dx), _vp(dy))
     return dx, dy
+
+
+def thickness_change(m: AaAcMesh, A, Cw, Up_SIA_Ac, Up_SSA_Ac, SMB_year, BMB, dt, Hi, mask_noice=None,
+                     zero_edges=True):
+    """calculate_ice_thickness_change. Returns (Hi_new, Hi_prev, dHi_dt, dVi_in)."""
+    base = m.base
+    nV = base.nV
+    ncm = base.C.shape[1]
+    Hi_new = np.array(Hi, dtype=np.float64, copy=True)
+    Hi_prev = np.zeros(nV)
+    dHi_dt = np.zeros(nV)
+    dVi_in = np.zeros((nV, ncm), order="F")
+    keep = [_f64(A), _f64(Cw), _f64(Up_SIA_Ac), _f64(Up_SSA_Ac), _f64(SMB_year), _f64(BMB)]
+    mk = None if mask_noice is None else _i32(mask_noice)
+    bs, bkeep = _base_struct(base)
+    ms = _aaac_struct(m)
+    rc = lib().or_thickness_change(ct.byref(bs), ct.byref(ms), *(_vp(k) for k in keep), None if mk is None else _vp(mk),
+                                   ct.c_double(dt), ct.c_int(1 if zero_edges else 0), _vp(Hi_new), _vp(Hi_prev),
+                                   _vp(dHi_dt), _vp(dVi_in))
+    if rc != OR_OK:
+        raise RuntimeError("or_thickness_change failed: %d" % rc)
+    return Hi_new, Hi_prev, dHi_dt, dVi_in

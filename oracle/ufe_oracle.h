@@ -181,6 +181,14 @@ typedef struct or_geom {
 
 int or_update_geometry(const or_base *b, const or_aaac *m, or_geom *g);
 
+/* calculate_ice_thickness_change (ice_dynamics_module.f90:31-237); Cw and dVi_in are
+ * (nV, nC_mem); zero_edges applies the domain-edge rule (every configuration except the
+ * SSA_icestream benchmark); mask_noice may be NULL. Hi is updated in place. */
+int or_thickness_change(const or_base *b, const or_aaac *m, const double *A, const double *Cw,
+                        const double *Up_SIA_Ac, const double *Up_SSA_Ac, const double *SMB_year,
+                        const double *BMB, const int32_t *mask_noice, double dt, int zero_edges,
+                        double *Hi, double *Hi_prev, double *dHi_dt, double *dVi_in);
+
 /* Primitive operators, for tests. */
 void or_map_Aa_to_Ac(const or_aaac *m, int nV, const double *d_Aa, double *d_Ac);
 void or_map_Ac_to_Aa(const or_base *b, const or_aaac *m, const double *d_Ac, double *d_Aa);

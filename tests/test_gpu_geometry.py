@@ -1,0 +1,115 @@
+"""Geometry preparation on the device (run with -m gpu): every derived field bit-identical to
+the oracle's restatement of update_general_ice_model_data, and a solve fed by the device
+geometry identical to one fed by host-prepared fields."""
+import numpy as np
+import pytest
+
+from conftest import oracle_aaac, oracle_inputs
+
+import oracle as orc
+from ufemism_gb300 import _native as nat
+from ufemism_gb300 import api
+from ufemism_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def device():
+    api.init(0)
+
+
+@pytest.mark.parametrize("kind", ["dome", "marine"])
+def test_device_geometry_bit_identical_to_oracle(kind):
+    m = oracle_aaac("4k")
+    base = m.base
+    Hi, Hb, SL = wl.dome_geometry(base) if kind == "dome" else wl.marine_geometry(base, seed=20261206)
+    ref = orc.update_geometry(m, Hi, Hb, SL)
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    got = dm.geometry_update(Hi, Hb, SL)
+    for k in nat.GEOM_OUT_FIELDS:
+        assert np.array_equal(got[k], np.asarray(ref[k]).astype(got[k].dtype)), k
+    if kind == "marine":
+        assert got["mask_gl_Ac"].sum() > 0 and got["mask_shelf"].sum() > 0
+    dm.close()
+
+
+def test_solve_from_device_geometry_matches_host_fields():
+    m = oracle_aaac("4k")
+    ssa, sia, g = oracle_inputs(m, "marine")
+    beta = np.exp(wl.log_beta_field(m, std=1.0, ell=100e3, seed=3))
+    p = api.default_params(precision=nat.UFE_FP64)
+    dm = api.DeviceMesh(m)
+    f = dict(ssa, beta_sq_AaAc=beta)
+    rc1, o1, s1 = dm.solve_ssa(f, p)
+    dm.geometry_attach(m)
+    dm.ssa_upload_geometry(ssa["Hi"], ssa["Hb"], ssa["SL"], ssa["A_flow_mean"], ssa["A_flow_mean_Ac"], p, beta=beta)
+    rc2, s2 = dm.ssa_run(p)
+    o2 = dm.ssa_download()
+    assert rc2 == rc1 and s2["sweeps"] == s1["sweeps"]
+    for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc"):
+        assert np.array_equal(o2[k], o1[k]), k
+    dm.close()
+
+
+def test_geometry_attach_rejects_bad_indices():
+    m = oracle_aaac("tiny")
+    dm = api.DeviceMesh(m)
+
+    class Bad:
+        pass
+    bad = Bad()
+    for k in ("base", "Nx", "Ny", "Aci", "Nx_Ac", "Ny_Ac", "No_Ac", "Np_Ac", "CAaAc"):
+        setattr(bad, k, getattr(m, k))
+    b2 = Bad()
+    b2.nC, b2.C = m.base.nC, m.base.C.copy()
+    b2.C[3, 0] = m.base.nV + 10
+    bad.base = b2
+    with pytest.raises(nat.UfeError) as e:
+        dm.geometry_attach(bad)
+    assert e.value.status == nat.UFE_BAD_MESH
+    dm.close()
+
+
+def _thickness_case(name="4k"):
+    m = oracle_aaac(name)
+    ssa, sia, g = oracle_inputs(m, "marine")
+    A, Cw = wl.areas_and_widths(m.base)
+    rng = np.random.default_rng(11)
+    up_sia = rng.normal(size=m.nAc) * 50.0
+    up_ssa = rng.normal(size=m.nAc) * 400.0
+    smb = rng.normal(size=m.base.nV) * 0.5
+    bmb = -np.abs(rng.normal(size=m.base.nV)) * 20.0 * (ssa["Hi"] > 0)
+    noice = (rng.uniform(size=m.base.nV) < 0.01).astype(np.int32)
+    return m, ssa, A, Cw, up_sia, up_ssa, smb, bmb, noice
+
+
+@pytest.mark.parametrize("dt", [10.0, 0.0, 250.0])
+def test_thickness_update_bit_identical_to_oracle(dt):
+    """dt = 250 yr forces outflux rescales on many vertices."""
+    m, ssa, A, Cw, up_sia, up_ssa, smb, bmb, noice = _thickness_case()
+    ref = orc.thickness_change(m, A, Cw, up_sia, up_ssa, smb, bmb, dt, ssa["Hi"], mask_noice=noice)
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    got = dm.thickness_update(ssa["Hi"], A, Cw, smb, bmb, dt, Up_SIA_Ac=up_sia, Up_SSA_Ac=up_ssa, mask_noice=noice)
+    for k, (a, b) in enumerate(zip(got, ref)):
+        assert np.array_equal(a, b), ("Hi", "Hi_prev", "dHi_dt", "dVi_in")[k]
+    if dt == 250.0:
+        # rescaled outfluxes leave at most rounding-level negative thickness (as the reference)
+        assert np.any(got[0] == 0.0) and np.all(got[0] >= -1e-9 * ssa["Hi"].max())
+    dm.close()
+
+
+def test_thickness_update_from_device_velocities():
+    """Velocities left on the device by the SSA and SIA solves of the same handle."""
+    m, ssa, A, Cw, up_sia, up_ssa, smb, bmb, noice = _thickness_case("1k")
+    sia = oracle_inputs(m, "marine")[1]
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    rc, o, st = dm.solve_ssa(ssa, api.default_params(), check=False)
+    so = dm.solve_sia(sia, api.default_params())
+    got = dm.thickness_update(ssa["Hi"], A, Cw, smb, bmb, 5.0)
+    ref = orc.thickness_change(m, A, Cw, so["Up_SIA_Ac"], o["Up_SSA_Ac"], smb, bmb, 5.0, ssa["Hi"])
+    assert np.array_equal(got[0], ref[0])
+    dm.close()

@@ -75,6 +75,34 @@ class SiaOut(ct.Structure):
                                  "U_SIA", "V_SIA", "D_SIA")]
 
 
+GEOM_MESH_FIELDS = ("nC", "C", "Nx", "Ny", "Aci", "Nx_Ac", "Ny_Ac", "No_Ac", "Np_Ac")
+
+
+class GeometryMesh(ct.Structure):
+    _fields_ = [(n, P) for n in GEOM_MESH_FIELDS]
+
+
+GEOM_OUT_FIELDS = ("Hs", "dHi_dx", "dHi_dy", "dHs_dx", "dHs_dy", "dHs_dx_shelf", "dHs_dy_shelf",
+                   "mask_ocean", "mask_ice", "mask_sheet", "mask_shelf", "Hi_Ac", "Hb_Ac", "SL_Ac", "Hs_Ac",
+                   "dHi_dx_Ac", "dHi_dy_Ac", "dHi_dp_Ac", "dHi_do_Ac", "dHb_dx_Ac", "dHb_dy_Ac", "dHb_dp_Ac",
+                   "dHb_do_Ac", "dHs_dx_Ac", "dHs_dy_Ac", "dHs_dp_Ac", "dHs_do_Ac", "dSL_dx_Ac", "dSL_dy_Ac",
+                   "dSL_dp_Ac", "dSL_do_Ac", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac", "mask_ocean_Ac", "mask_ice_Ac",
+                   "mask_sheet_Ac", "mask_shelf_Ac", "mask_gl_Ac")
+
+
+class GeometryOut(ct.Structure):
+    _fields_ = [(n, P) for n in GEOM_OUT_FIELDS]
+
+
+class ThicknessIn(ct.Structure):
+    _fields_ = [(n, P) for n in ("A", "Cw", "Up_SIA_Ac", "Up_SSA_Ac", "SMB_year", "BMB", "mask_noice")] + \
+               [("dt", F64), ("zero_edges", I32)]
+
+
+class ThicknessOut(ct.Structure):
+    _fields_ = [(n, P) for n in ("Hi_prev", "dHi_dt", "dVi_in")]
+
+
 class VjpParams(ct.Structure):
     _fields_ = [("tol", F64), ("max_sweeps", I32), ("omega", F64)]
 
@@ -146,6 +174,10 @@ PROTOTYPES = {
     "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_geometry_attach": (I32, [P, ct.POINTER(GeometryMesh)]),
+    "ufe_geometry_update": (I32, [P, P, P, P, ct.POINTER(GeometryOut)]),
+    "ufe_ssa_upload_geometry": (I32, [P, ct.POINTER(Params), P, P, P, P, P, P, ct.POINTER(SsaInout)]),
+    "ufe_thickness_update": (I32, [P, ct.POINTER(ThicknessIn), P, ct.POINTER(ThicknessOut)]),
     "ufe_ssa_vjp": (I32, [P, ct.POINTER(Params), ct.POINTER(VjpParams), ct.POINTER(VjpIn), ct.POINTER(VjpGeom),
                           ct.POINTER(VjpOut), ct.POINTER(VjpStats)]),
     "ufe_batch_plan": (I32, [ct.POINTER(I32), I32, ct.POINTER(BatchConfig), I32, ct.POINTER(I32),

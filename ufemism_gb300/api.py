@@ -263,6 +263,69 @@ class DeviceMesh:
         return rc, out, dict(status=st.status, sweeps=st.sweeps, last_rel_update=st.last_rel_update,
                              device_ms=st.device_ms)
 
+    # ---------------------------------------------------------------- geometry on the device
+    def geometry_attach(self, mesh):
+        """Upload the Aa and Ac derivative stencils of ``mesh`` (ufe_geometry_attach)."""
+        L = nat.load()
+        k = dict(nC=_i32(mesh.base.nC), C=_i32(mesh.base.C), Nx=_f64(mesh.Nx), Ny=_f64(mesh.Ny), Aci=_i32(mesh.Aci),
+                 Nx_Ac=_f64(mesh.Nx_Ac), Ny_Ac=_f64(mesh.Ny_Ac), No_Ac=_f64(mesh.No_Ac), Np_Ac=_f64(mesh.Np_Ac))
+        if k["C"].shape != (self.nV, mesh.CAaAc.shape[1]) or k["Nx"].shape != (self.nV, mesh.CAaAc.shape[1] + 1):
+            raise ValueError("mesh stencils do not match this handle")
+        g = nat.GeometryMesh(*(_ptr(k[n]) for n in nat.GEOM_MESH_FIELDS))
+        rc = L.ufe_geometry_attach(self._h, ct.byref(g))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_geometry_attach")
+
+    def geometry_update(self, Hi, Hb, SL) -> dict:
+        """Derived geometry fields computed on the device (ufe_geometry_update)."""
+        L = nat.load()
+        ints = {"mask_ocean", "mask_ice", "mask_sheet", "mask_shelf", "mask_ocean_Ac", "mask_ice_Ac", "mask_sheet_Ac",
+                "mask_shelf_Ac", "mask_gl_Ac"}
+        out = {}
+        for k in nat.GEOM_OUT_FIELDS:
+            n = self.nAc if k.endswith("_Ac") else self.nV
+            out[k] = np.zeros(n, dtype=np.int32 if k in ints else np.float64)
+        go = nat.GeometryOut(*(out[k].ctypes.data for k in nat.GEOM_OUT_FIELDS))
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (Hi, Hb, SL)]
+        rc = L.ufe_geometry_update(self._h, *(a.ctypes.data for a in arrs), ct.byref(go))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_geometry_update")
+        return out
+
+    def ssa_upload_geometry(self, Hi, Hb, SL, A_flow_mean, A_flow_mean_Ac, params: dict, beta=None,
+                            warm: dict | None = None):
+        """ufe_ssa_upload_geometry: the solve's inputs derived on the device from Hi, Hb, SL."""
+        L = nat.load()
+        _, sio, io, _ = self._ssa_structs({}, warm)
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (Hi, Hb, SL, A_flow_mean, A_flow_mean_Ac)]
+        b = None if beta is None else np.ascontiguousarray(beta, dtype=np.float64)
+        ps, _z = _params_struct(params)
+        rc = L.ufe_ssa_upload_geometry(self._h, ct.byref(ps), *(a.ctypes.data for a in arrs), _ptr(b), ct.byref(sio))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_ssa_upload_geometry")
+
+    def thickness_update(self, Hi, A, Cw, SMB_year, BMB, dt, Up_SIA_Ac=None, Up_SSA_Ac=None, mask_noice=None,
+                         zero_edges=True):
+        """calculate_ice_thickness_change on the device (ufe_thickness_update). Velocities left
+        as None come from the handle's last SSA / SIA solves. Returns (Hi_new, Hi_prev,
+        dHi_dt, dVi_in)."""
+        L = nat.load()
+        keep = dict(A=_f64(A), Cw=_f64(Cw), SMB=_f64(SMB_year), BMB=_f64(BMB),
+                    usia=None if Up_SIA_Ac is None else _f64(Up_SIA_Ac),
+                    ussa=None if Up_SSA_Ac is None else _f64(Up_SSA_Ac),
+                    noice=None if mask_noice is None else _i32(mask_noice))
+        ti = nat.ThicknessIn(_ptr(keep["A"]), _ptr(keep["Cw"]), _ptr(keep["usia"]), _ptr(keep["ussa"]),
+                             _ptr(keep["SMB"]), _ptr(keep["BMB"]), _ptr(keep["noice"]), float(dt),
+                             1 if zero_edges else 0)
+        H = np.array(Hi, dtype=np.float64, copy=True)
+        out = dict(Hi_prev=np.zeros(self.nV), dHi_dt=np.zeros(self.nV),
+                   dVi_in=np.zeros(keep["Cw"].shape, order="F"))
+        to = nat.ThicknessOut(*(out[k].ctypes.data for k in ("Hi_prev", "dHi_dt", "dVi_in")))
+        rc = L.ufe_thickness_update(self._h, ct.byref(ti), H.ctypes.data, ct.byref(to))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_thickness_update")
+        return H, out["Hi_prev"], out["dHi_dt"], out["dVi_in"]
+
     # ---------------------------------------------------------------- SIA
     def solve_sia(self, fields: dict, params: dict, want_3d: bool = True):
         L = nat.load()

@@ -19,7 +19,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libufemism_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["ufe_mesh.cu", "ufe_ssa.cu", "ufe_sia.cu"]
+CU_SOURCES = ["ufe_mesh.cu", "ufe_ssa.cu", "ufe_sia.cu", "ufe_geom.cu"]
 CPP_SOURCES = ["ufe_capi.cpp", "aaac_build.cpp"]
 
 

@@ -1,0 +1,535 @@
+// Geometry preparation on the device: the part of update_general_ice_model_data
+// (general_ice_model_data_module.f90:23-96) that the velocity solve reads — the Aa-to-Ac maps
+// of Hi, Hb, SL (map_Aa_to_Ac, mesh_ArakawaC_module.f90:726-747), the surface Hs, the
+// ocean / ice / sheet / shelf masks on Aa and Ac and the grounding-line mask on Ac
+// (determine_masks, 97-297), the Aa slopes of Hi and Hs (get_mesh_derivatives,
+// mesh_derivatives_module.f90:315-371), the Ac slopes of Hi, Hb, Hs, SL
+// (get_mesh_derivatives_Ac, mesh_ArakawaC_module.f90:542-581) and the shelf-slope rule
+// (general_ice_model_data_module.f90:70-87). Same expression order as the reference and
+// built without FMA contraction, so the fields are bit-identical to its.
+//
+// With it a time step uploads Hi, Hb, SL (and the flow factor) instead of about twenty
+// derived fields, and the solve's inputs are born on the device.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "ufe_internal.h"
+
+namespace ufe {
+
+struct GeomWork {
+  int nV = 0, nAc = 0, ncm = 0;
+  // stencils
+  int *nC = nullptr, *C = nullptr, *Aci = nullptr;
+  double *Nx = nullptr, *Ny = nullptr, *Nx_Ac = nullptr, *Ny_Ac = nullptr, *No_Ac = nullptr, *Np_Ac = nullptr;
+  // fields (see GeomFields)
+  double *dbl = nullptr;
+  int *msk = nullptr;
+  double *beta = nullptr;      // (nV + nAc), allocated on first use
+  double *thk = nullptr;       // thickness-update work, allocated on first use
+  int *thk_int = nullptr;
+  bool computed = false;
+};
+
+void geom_free(GeomWork *w) {
+  if (!w) return;
+  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete w;
+}
+
+namespace {
+
+// Double fields: Aa (nV each) then Ac (nAc each), in the order of the enums.
+enum AaD { A_HI, A_HB, A_SL, A_HS, A_AF, A_DHI_DX, A_DHI_DY, A_DHS_DX, A_DHS_DY, A_DHS_DX_SH, A_DHS_DY_SH, A_COUNT };
+enum AcD {
+  C_HI, C_HB, C_SL, C_HS, C_AF,
+  C_DHI_DX, C_DHI_DY, C_DHI_DP, C_DHI_DO, C_DHB_DX, C_DHB_DY, C_DHB_DP, C_DHB_DO,
+  C_DHS_DX, C_DHS_DY, C_DHS_DP, C_DHS_DO, C_DSL_DX, C_DSL_DY, C_DSL_DP, C_DSL_DO,
+  C_DHS_DX_SH, C_DHS_DY_SH, C_COUNT
+};
+// Integer masks: Aa ocean, ice, sheet, shelf (nV each), then Ac ocean, ice, sheet, shelf, gl.
+enum AaM { M_OCEAN, M_ICE, M_SHEET, M_SHELF, M_COUNT };
+enum AcM { MC_OCEAN, MC_ICE, MC_SHEET, MC_SHELF, MC_GL, MC_COUNT };
+
+struct GeomArgs {
+  int nV, nAc, ncm;
+  const int *nC, *C, *Aci;
+  const double *Nx, *Ny, *Nx_Ac, *Ny_Ac, *No_Ac, *Np_Ac;
+  double *aa, *ac;     // field bases
+  int *ma, *mc;
+};
+
+__device__ __forceinline__ bool floating(double Hi, double Hb, double SL) {
+  return Hi < ((SL - Hb) * kSeawaterDensity) / kIceDensity;   // is_floating, general_ice_model_data_module.f90:464-475
+}
+
+#define AAF(a, k) ((a).aa + (size_t)(k) * (a).nV)
+#define ACF(a, k) ((a).ac + (size_t)(k) * (a).nAc)
+#define AAM(a, k) ((a).ma + (size_t)(k) * (a).nV)
+#define ACM(a, k) ((a).mc + (size_t)(k) * (a).nAc)
+
+// Hs and the Aa masks (general_ice_model_data_module.f90:45-47, determine_masks 136-160).
+__global__ void k_geom_aa1(const GeomArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const double Hi = AAF(a, A_HI)[v], Hb = AAF(a, A_HB)[v], SL = AAF(a, A_SL)[v];
+  AAF(a, A_HS)[v] = Hi + fmax(SL - kIceDensity / kSeawaterDensity * Hi, Hb);
+  const int ocean = floating(Hi, Hb, SL);
+  const int ice = Hi > 0.0;
+  AAM(a, M_OCEAN)[v] = ocean;
+  AAM(a, M_ICE)[v] = ice;
+  AAM(a, M_SHEET)[v] = ice && !ocean;
+  AAM(a, M_SHELF)[v] = ice && ocean;
+}
+
+// Ac maps, Hs_Ac and the Ac masks (map_Aa_to_Ac; determine_masks 207-235 and the grounding
+// line of 236-297: a sheet vertex on one end and a shelf vertex on the other).
+__global__ void k_geom_ac1(const GeomArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nAc) return;
+  const int vi = a.Aci[c] - 1, vj = a.Aci[c + a.nAc] - 1;
+  const double Hi = (AAF(a, A_HI)[vi] + AAF(a, A_HI)[vj]) / 2.0;
+  const double Hb = (AAF(a, A_HB)[vi] + AAF(a, A_HB)[vj]) / 2.0;
+  const double SL = (AAF(a, A_SL)[vi] + AAF(a, A_SL)[vj]) / 2.0;
+  ACF(a, C_HI)[c] = Hi;
+  ACF(a, C_HB)[c] = Hb;
+  ACF(a, C_SL)[c] = SL;
+  ACF(a, C_HS)[c] = Hi + fmax(SL - kIceDensity / kSeawaterDensity * Hi, Hb);
+  const int ocean = floating(Hi, Hb, SL);
+  const int ice = Hi > 0.0;
+  ACM(a, MC_OCEAN)[c] = ocean;
+  ACM(a, MC_ICE)[c] = ice;
+  ACM(a, MC_SHEET)[c] = ice && !ocean;
+  ACM(a, MC_SHELF)[c] = ice && ocean;
+  const int *sheet = AAM(a, M_SHEET), *shelf = AAM(a, M_SHELF);
+  ACM(a, MC_GL)[c] = (sheet[vi] == 1 && shelf[vj] == 1) || (sheet[vj] == 1 && shelf[vi] == 1);
+}
+
+// Aa slopes of Hi and Hs (home term first, then the neighbours in C order) and the shelf rule.
+__global__ void k_geom_aa2(const GeomArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const int n = a.nC[v];
+  const double *Hi = AAF(a, A_HI), *Hs = AAF(a, A_HS);
+  const size_t ld = a.nV;
+  double ix = a.Nx[v + n * ld] * Hi[v], iy = a.Ny[v + n * ld] * Hi[v];
+  double sx = a.Nx[v + n * ld] * Hs[v], sy = a.Ny[v + n * ld] * Hs[v];
+  for (int c = 0; c < n; ++c) {
+    const int j = a.C[v + c * ld] - 1;
+    const double nx = a.Nx[v + c * ld], ny = a.Ny[v + c * ld];
+    ix = ix + nx * Hi[j];
+    iy = iy + ny * Hi[j];
+    sx = sx + nx * Hs[j];
+    sy = sy + ny * Hs[j];
+  }
+  AAF(a, A_DHI_DX)[v] = ix; AAF(a, A_DHI_DY)[v] = iy;
+  AAF(a, A_DHS_DX)[v] = sx; AAF(a, A_DHS_DY)[v] = sy;
+  if (AAM(a, M_OCEAN)[v] == 0) {
+    AAF(a, A_DHS_DX_SH)[v] = sx;
+    AAF(a, A_DHS_DY_SH)[v] = sy;
+  } else {
+    AAF(a, A_DHS_DX_SH)[v] = (1.0 - kIceDensity / kSeawaterDensity) * ix;
+    AAF(a, A_DHS_DY_SH)[v] = (1.0 - kIceDensity / kSeawaterDensity) * iy;
+  }
+}
+
+// Ac slopes of Hi, Hb, Hs, SL (4-point stencil in Aci order; p along the edge) and the shelf rule.
+__global__ void k_geom_ac2(const GeomArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nAc) return;
+  const size_t ld = a.nAc;
+  int idx[4];
+  for (int k = 0; k < 4; ++k) idx[k] = a.Aci[c + k * ld] - 1;
+  const double *src[4] = {AAF(a, A_HI), AAF(a, A_HB), AAF(a, A_HS), AAF(a, A_SL)};
+  const int dst[4] = {C_DHI_DX, C_DHB_DX, C_DHS_DX, C_DSL_DX};
+  const double np = a.Np_Ac[c];
+  for (int f = 0; f < 4; ++f) {
+    const double *d = src[f];
+    double dx = 0.0, dy = 0.0, dO = 0.0;
+    for (int k = 0; k < 4; ++k) {
+      const double dv = d[idx[k]];
+      dx = dx + a.Nx_Ac[c + k * ld] * dv;
+      dy = dy + a.Ny_Ac[c + k * ld] * dv;
+      dO = dO + a.No_Ac[c + k * ld] * dv;
+    }
+    ACF(a, dst[f])[c] = dx;
+    ACF(a, dst[f] + 1)[c] = dy;
+    ACF(a, dst[f] + 2)[c] = np * (d[idx[1]] - d[idx[0]]);
+    ACF(a, dst[f] + 3)[c] = dO;
+  }
+  if (ACM(a, MC_OCEAN)[c] == 0) {
+    ACF(a, C_DHS_DX_SH)[c] = ACF(a, C_DHS_DX)[c];
+    ACF(a, C_DHS_DY_SH)[c] = ACF(a, C_DHS_DY)[c];
+  } else {
+    ACF(a, C_DHS_DX_SH)[c] = (1.0 - kIceDensity / kSeawaterDensity) * ACF(a, C_DHI_DX)[c];
+    ACF(a, C_DHS_DY_SH)[c] = (1.0 - kIceDensity / kSeawaterDensity) * ACF(a, C_DHI_DY)[c];
+  }
+}
+
+GeomArgs args_of(GeomWork *w) {
+  GeomArgs a;
+  a.nV = w->nV; a.nAc = w->nAc; a.ncm = w->ncm;
+  a.nC = w->nC; a.C = w->C; a.Aci = w->Aci; a.Nx = w->Nx; a.Ny = w->Ny;
+  a.Nx_Ac = w->Nx_Ac; a.Ny_Ac = w->Ny_Ac; a.No_Ac = w->No_Ac; a.Np_Ac = w->Np_Ac;
+  a.aa = w->dbl; a.ac = w->dbl + (size_t)A_COUNT * w->nV;
+  a.ma = w->msk; a.mc = w->msk + (size_t)M_COUNT * w->nV;
+  return a;
+}
+
+template <class T>
+int up(T *dst, const T *src, size_t n, cudaStream_t s) {
+  return cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s), "geometry H2D");
+}
+
+// Upload Hi, Hb, SL and compute every derived field on the handle's stream.
+int compute(ufe_mesh_h h, const double *Hi, const double *Hb, const double *SL) {
+  GeomWork *w = h->geom;
+  cudaStream_t s = h->stream;
+  GeomArgs a = args_of(w);
+  const size_t nV = w->nV;
+  int rc = up(AAF(a, A_HI), Hi, nV, s);
+  if (!rc) rc = up(AAF(a, A_HB), Hb, nV, s);
+  if (!rc) rc = up(AAF(a, A_SL), SL, nV, s);
+  const unsigned gv = (unsigned)((w->nV + 255) / 256), gc = (unsigned)((w->nAc + 255) / 256);
+  if (!rc) { k_geom_aa1<<<gv, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_aa1"); }
+  if (!rc) { k_geom_ac1<<<gc, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_ac1"); }
+  if (!rc) { k_geom_aa2<<<gv, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_aa2"); }
+  if (!rc) { k_geom_ac2<<<gc, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_ac2"); }
+  w->computed = rc == UFE_OK;
+  return rc;
+}
+
+}  // namespace
+}  // namespace ufe
+
+using namespace ufe;
+
+extern "C" int ufe_geometry_attach(ufe_mesh_h h, const ufe_geometry_mesh *g) {
+  if (!h || !g || !g->nC || !g->C || !g->Nx || !g->Ny || !g->Aci || !g->Nx_Ac || !g->Ny_Ac || !g->No_Ac || !g->Np_Ac) {
+    set_error("ufe_geometry_attach: missing array");
+    return UFE_BAD_ARG;
+  }
+  const DevMesh &m = h->m;
+  const int nV = m.nV, nAc = m.nAc, ncm = m.ncm;
+  // validate the index arrays on the host before any kernel reads them
+  for (int v = 0; v < nV; ++v) {
+    if (g->nC[v] < 2 || g->nC[v] > ncm) { set_error("ufe_geometry_attach: nC out of range"); return UFE_BAD_MESH; }
+    for (int c = 0; c < g->nC[v]; ++c) {
+      const int j = g->C[v + (size_t)c * nV];
+      if (j < 1 || j > nV) { set_error("ufe_geometry_attach: C out of range"); return UFE_BAD_MESH; }
+    }
+  }
+  for (size_t k = 0; k < 4 * (size_t)nAc; ++k)
+    if (g->Aci[k] < 1 || g->Aci[k] > nV) { set_error("ufe_geometry_attach: Aci out of range"); return UFE_BAD_MESH; }
+  // every Ac edge joins two connected vertices (the thickness update looks them up in C)
+  auto connected = [&](int v, int w) {
+    for (int c = 0; c < g->nC[v]; ++c)
+      if (g->C[v + (size_t)c * nV] - 1 == w) return true;
+    return false;
+  };
+  for (int c = 0; c < nAc; ++c) {
+    const int vi = g->Aci[c] - 1, vj = g->Aci[c + (size_t)nAc] - 1;
+    if (!connected(vi, vj) || !connected(vj, vi)) { set_error("ufe_geometry_attach: Aci(:,1:2) not connected in C"); return UFE_BAD_MESH; }
+  }
+  if (h->geom) { geom_free(h->geom); h->geom = nullptr; }
+  GeomWork *w = new GeomWork();
+  w->nV = nV; w->nAc = nAc; w->ncm = ncm;
+  cudaStream_t s = h->stream;
+  const size_t nv = nV, nac = nAc, nc = ncm;
+  int rc = cuda_status(cudaMalloc(&w->nC, nv * sizeof(int)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->C, nv * nc * sizeof(int)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Aci, 4 * nac * sizeof(int)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Nx, nv * (nc + 1) * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Ny, nv * (nc + 1) * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Nx_Ac, 4 * nac * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Ny_Ac, 4 * nac * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->No_Ac, 4 * nac * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Np_Ac, nac * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->dbl, ((size_t)A_COUNT * nv + (size_t)C_COUNT * nac) * sizeof(double)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->msk, ((size_t)M_COUNT * nv + (size_t)MC_COUNT * nac) * sizeof(int)), "geometry");
+  if (!rc) rc = up(w->nC, g->nC, nv, s);
+  if (!rc) rc = up(w->C, g->C, nv * nc, s);
+  if (!rc) rc = up(w->Aci, g->Aci, 4 * nac, s);
+  if (!rc) rc = up(w->Nx, g->Nx, nv * (nc + 1), s);
+  if (!rc) rc = up(w->Ny, g->Ny, nv * (nc + 1), s);
+  if (!rc) rc = up(w->Nx_Ac, g->Nx_Ac, 4 * nac, s);
+  if (!rc) rc = up(w->Ny_Ac, g->Ny_Ac, 4 * nac, s);
+  if (!rc) rc = up(w->No_Ac, g->No_Ac, 4 * nac, s);
+  if (!rc) rc = up(w->Np_Ac, g->Np_Ac, nac, s);
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "geometry attach");
+  if (rc) { geom_free(w); return rc; }
+  h->geom = w;
+  return UFE_OK;
+}
+
+extern "C" int ufe_geometry_update(ufe_mesh_h h, const double *Hi, const double *Hb, const double *SL,
+                                   ufe_geometry_out *out) {
+  if (!h || !Hi || !Hb || !SL) { set_error("ufe_geometry_update: null argument"); return UFE_BAD_ARG; }
+  if (!h->geom) { set_error("ufe_geometry_update: call ufe_geometry_attach first"); return UFE_BAD_ARG; }
+  int rc = compute(h, Hi, Hb, SL);
+  if (rc) return rc;
+  GeomWork *w = h->geom;
+  GeomArgs a = args_of(w);
+  cudaStream_t s = h->stream;
+  if (out) {
+    const size_t nV = w->nV, nAc = w->nAc;
+    auto dd = [&](double *dst, const double *src, size_t n) {
+      if (!dst || rc) return;
+      rc = cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, s), "geometry D2H");
+    };
+    auto di = [&](int32_t *dst, const int *src, size_t n) {
+      if (!dst || rc) return;
+      rc = cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(int), cudaMemcpyDeviceToHost, s), "geometry D2H");
+    };
+    dd(out->Hs, AAF(a, A_HS), nV);
+    dd(out->dHi_dx, AAF(a, A_DHI_DX), nV); dd(out->dHi_dy, AAF(a, A_DHI_DY), nV);
+    dd(out->dHs_dx, AAF(a, A_DHS_DX), nV); dd(out->dHs_dy, AAF(a, A_DHS_DY), nV);
+    dd(out->dHs_dx_shelf, AAF(a, A_DHS_DX_SH), nV); dd(out->dHs_dy_shelf, AAF(a, A_DHS_DY_SH), nV);
+    di(out->mask_ocean, AAM(a, M_OCEAN), nV); di(out->mask_ice, AAM(a, M_ICE), nV);
+    di(out->mask_sheet, AAM(a, M_SHEET), nV); di(out->mask_shelf, AAM(a, M_SHELF), nV);
+    dd(out->Hi_Ac, ACF(a, C_HI), nAc); dd(out->Hb_Ac, ACF(a, C_HB), nAc); dd(out->SL_Ac, ACF(a, C_SL), nAc);
+    dd(out->Hs_Ac, ACF(a, C_HS), nAc);
+    double *acd[16] = {out->dHi_dx_Ac, out->dHi_dy_Ac, out->dHi_dp_Ac, out->dHi_do_Ac,
+                       out->dHb_dx_Ac, out->dHb_dy_Ac, out->dHb_dp_Ac, out->dHb_do_Ac,
+                       out->dHs_dx_Ac, out->dHs_dy_Ac, out->dHs_dp_Ac, out->dHs_do_Ac,
+                       out->dSL_dx_Ac, out->dSL_dy_Ac, out->dSL_dp_Ac, out->dSL_do_Ac};
+    for (int k = 0; k < 16; ++k) dd(acd[k], ACF(a, C_DHI_DX + k), nAc);
+    dd(out->dHs_dx_shelf_Ac, ACF(a, C_DHS_DX_SH), nAc); dd(out->dHs_dy_shelf_Ac, ACF(a, C_DHS_DY_SH), nAc);
+    di(out->mask_ocean_Ac, ACM(a, MC_OCEAN), nAc); di(out->mask_ice_Ac, ACM(a, MC_ICE), nAc);
+    di(out->mask_sheet_Ac, ACM(a, MC_SHEET), nAc); di(out->mask_shelf_Ac, ACM(a, MC_SHELF), nAc);
+    di(out->mask_gl_Ac, ACM(a, MC_GL), nAc);
+  }
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "geometry update");
+  return rc;
+}
+
+extern "C" int ufe_ssa_upload_geometry(ufe_mesh_h h, const ufe_params *p, const double *Hi, const double *Hb,
+                                       const double *SL, const double *A_flow_mean, const double *A_flow_mean_Ac,
+                                       const double *beta_sq_AaAc, const ufe_ssa_inout *io) {
+  if (!h || !p || !Hi || !Hb || !SL || !A_flow_mean || !A_flow_mean_Ac || !io) {
+    set_error("ufe_ssa_upload_geometry: null argument");
+    return UFE_BAD_ARG;
+  }
+  if (!h->geom) { set_error("ufe_ssa_upload_geometry: call ufe_geometry_attach first"); return UFE_BAD_ARG; }
+  int rc = compute(h, Hi, Hb, SL);
+  if (rc) return rc;
+  GeomWork *w = h->geom;
+  GeomArgs a = args_of(w);
+  cudaStream_t s = h->stream;
+  const size_t nV = w->nV, nAc = w->nAc, nA = nV + nAc;
+  rc = up(AAF(a, A_AF), A_flow_mean, nV, s);
+  if (!rc) rc = up(ACF(a, C_AF), A_flow_mean_Ac, nAc, s);
+  double *beta_dev = nullptr;
+  if (!rc && beta_sq_AaAc) {
+    if (!w->beta) rc = cuda_status(cudaMalloc(&w->beta, nA * sizeof(double)), "geometry beta");
+    beta_dev = w->beta;
+    if (!rc) rc = up(beta_dev, beta_sq_AaAc, nA, s);
+  }
+  if (rc) return rc;
+  // grounded-ice vertices (the early-out of solve_SSA), counted on the host from the inputs
+  long long sheet = 0;
+  for (size_t v = 0; v < nV; ++v)
+    sheet += (Hi[v] > 0.0) && !(Hi[v] < ((SL[v] - Hb[v]) * kSeawaterDensity) / kIceDensity);
+  ufe_ssa_in in;
+  std::memset(&in, 0, sizeof(in));
+  in.Hi = AAF(a, A_HI); in.Hb = AAF(a, A_HB); in.SL = AAF(a, A_SL);
+  in.dHs_dx_shelf = AAF(a, A_DHS_DX_SH); in.dHs_dy_shelf = AAF(a, A_DHS_DY_SH); in.A_flow_mean = AAF(a, A_AF);
+  in.mask_sheet = AAM(a, M_SHEET);
+  in.Hi_Ac = ACF(a, C_HI); in.Hb_Ac = ACF(a, C_HB); in.SL_Ac = ACF(a, C_SL);
+  in.dHs_dx_shelf_Ac = ACF(a, C_DHS_DX_SH); in.dHs_dy_shelf_Ac = ACF(a, C_DHS_DY_SH); in.A_flow_mean_Ac = ACF(a, C_AF);
+  in.beta_sq_AaAc = beta_dev;
+  in.mask_gl_Ac = ACM(a, MC_GL);
+  in.dHi_dx_Ac = ACF(a, C_DHI_DX); in.dHi_dy_Ac = ACF(a, C_DHI_DY);
+  in.dSL_dx_Ac = ACF(a, C_DSL_DX); in.dSL_dy_Ac = ACF(a, C_DSL_DY);
+  in.dHb_dx_Ac = ACF(a, C_DHB_DX); in.dHb_dy_Ac = ACF(a, C_DHB_DY);
+  return ssa_upload_impl(h, p, &in, io, true, sheet);
+}
+
+// ---------------------------------------------------------------------------------------
+// Ice thickness update: calculate_ice_thickness_change (ice_dynamics_module.f90:31-237).
+//
+// The reference rescales outfluxes vertex by vertex; the rescale factor of a vertex depends
+// only on its own outfluxes, its ice volume and its SMB/BMB (inflow entries are what other
+// vertices change), and every connection's flux is owned by the vertex it leaves. So the
+// device computes every factor in parallel and applies them when it sums: an outflux entry
+// is scaled by its own vertex's factor, an influx entry by the factor of the vertex it came
+// from — the same products the sequential loop forms, summed in the same order.
+// ---------------------------------------------------------------------------------------
+namespace ufe {
+namespace {
+
+struct ThkArgs {
+  int nV, nAc, ncm;
+  const int *nC, *C, *Aci;          // 1-based
+  const double *A, *Cw, *Up_SIA, *Up_SSA, *SMB, *BMB;
+  const int *noice;                 // may be null
+  const int *dev_of_orig;
+  const uint8_t *slice_g;           // edge rows: group 5
+  double dt;
+  int zero_edges;
+  double *Hi, *Hi_prev, *dHi_dt;
+  double *dVi;                      // (nV, ncm) column-major, zeroed
+  double *factor, *Vi_SMB;          // (nV)
+};
+
+__device__ __forceinline__ int slot_of(const ThkArgs &a, int v, int w) {
+  const int n = a.nC[v];
+  for (int c = 0; c < n; ++c)
+    if (a.C[v + (size_t)c * a.nV] - 1 == w) return c;
+  return -1;
+}
+
+__global__ void k_thk_flux(const ThkArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nAc) return;
+  const int vi = a.Aci[c] - 1, vj = a.Aci[c + a.nAc] - 1;
+  const int ci = slot_of(a, vi, vj), cj = slot_of(a, vj, vi);
+  if (ci < 0 || cj < 0) return;   // ruled out by the host check of the connectivity
+  const double Upar = a.Up_SIA[c] + a.Up_SSA[c];
+  const double cw = a.Cw[vi + (size_t)ci * a.nV];
+  const double dVi = Upar > 0.0 ? ((a.Hi[vi] * Upar) * cw) * a.dt : ((a.Hi[vj] * Upar) * cw) * a.dt;
+  a.dVi[vi + (size_t)ci * a.nV] = -dVi;
+  a.dVi[vj + (size_t)cj * a.nV] = dVi;
+}
+
+__global__ void k_thk_factor(const ThkArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  double smb = ((a.SMB[v] + a.BMB[v]) * a.A[v]) * a.dt;
+  const double avail = a.A[v] * a.Hi[v];
+  double out = 0.0;
+  for (int c = 0; c < a.nC[v]; ++c) {
+    const double d = a.dVi[v + (size_t)c * a.nV];
+    if (!(d > 0.0)) out = out - d;
+  }
+  double f = 1.0;
+  if (-smb >= avail) {
+    smb = -avail;
+    f = 0.0;
+  }
+  if (out > avail + smb) f = (avail + smb) / out;
+  a.factor[v] = f;
+  a.Vi_SMB[v] = smb;
+}
+
+__global__ void k_thk_apply(const ThkArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const double fv = a.factor[v];
+  double sum = 0.0;
+  for (int c = 0; c < a.ncm; ++c) {
+    double d = a.dVi[v + (size_t)c * a.nV];
+    if (c < a.nC[v]) {
+      if (d < 0.0) {
+        if (fv < 1.0) d = d * fv;
+      } else if (d > 0.0) {
+        const int w = a.C[v + (size_t)c * a.nV] - 1;
+        const double fw = a.factor[w];
+        if (fw < 1.0) d = -((-d) * fw);   // the neighbour's scaled outflux, negated
+      }
+    }
+    sum = sum + d;
+  }
+  double rate = (sum + a.Vi_SMB[v]) / (a.A[v] * a.dt);
+  if (a.dt == 0.0) rate = 0.0;
+  a.dHi_dt[v] = rate;
+  const double h = a.Hi[v];
+  a.Hi_prev[v] = h;
+  double hn = h + (rate * a.dt);
+  if (a.zero_edges && a.slice_g[a.dev_of_orig[v] / kSlice] == 5) hn = 0.0;
+  if (a.noice && a.noice[v] == 1) hn = 0.0;
+  a.Hi[v] = hn;
+}
+
+// The scaled fluxes themselves, for callers that keep dVi_in (a separate pass so that the
+// summation above reads the unscaled entries of every neighbour).
+__global__ void k_thk_fluxes_out(const ThkArgs a, double *out) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const double fv = a.factor[v];
+  for (int c = 0; c < a.ncm; ++c) {
+    double d = a.dVi[v + (size_t)c * a.nV];
+    if (c < a.nC[v]) {
+      if (d < 0.0) {
+        if (fv < 1.0) d = d * fv;
+      } else if (d > 0.0) {
+        const double fw = a.factor[a.C[v + (size_t)c * a.nV] - 1];
+        if (fw < 1.0) d = -((-d) * fw);
+      }
+    }
+    out[v + (size_t)c * a.nV] = d;
+  }
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_thickness_update(ufe_mesh_h h, const ufe_thickness_in *in, double *Hi, ufe_thickness_out *out) {
+  if (!h || !in || !Hi || !in->A || !in->Cw || !in->SMB_year || !in->BMB) {
+    set_error("ufe_thickness_update: null argument");
+    return UFE_BAD_ARG;
+  }
+  if (!h->geom) { set_error("ufe_thickness_update: call ufe_geometry_attach first"); return UFE_BAD_ARG; }
+  GeomWork *g = h->geom;
+  const DevMesh &m = h->m;
+  const double *up_ssa = in->Up_SSA_Ac ? nullptr : ssa_device_Up(h);
+  const double *up_sia = in->Up_SIA_Ac ? nullptr : sia_device_Up(h);
+  if ((!in->Up_SSA_Ac && !up_ssa) || (!in->Up_SIA_Ac && !up_sia)) {
+    set_error("ufe_thickness_update: no velocities given and no solve on this handle to take them from");
+    return UFE_BAD_ARG;
+  }
+  cudaStream_t s = h->stream;
+  const size_t nV = m.nV, nAc = m.nAc, ncm = m.ncm;
+  // work: dVi (nV ncm), factor, Vi_SMB, Hi, Hi_prev, dHi_dt, A, SMB, BMB (nV each), Cw (nV ncm),
+  // Up_SIA, Up_SSA (nAc each), noice (nV ints)
+  const size_t nd = 2 * nV * ncm + 8 * nV + 2 * nAc;
+  if (!g->thk) {
+    int rc = cuda_status(cudaMalloc(&g->thk, nd * sizeof(double)), "thickness work");
+    if (!rc) rc = cuda_status(cudaMalloc(&g->thk_int, nV * sizeof(int)), "thickness work");
+    if (rc) return rc;
+  }
+  double *d = g->thk;
+  ThkArgs a;
+  a.nV = (int)nV; a.nAc = (int)nAc; a.ncm = (int)ncm; a.nC = g->nC; a.C = g->C; a.Aci = g->Aci;
+  a.dVi = d; double *Cw = d + nV * ncm; a.factor = Cw + nV * ncm; a.Vi_SMB = a.factor + nV;
+  a.Hi = a.Vi_SMB + nV; a.Hi_prev = a.Hi + nV; a.dHi_dt = a.Hi_prev + nV;
+  double *A = a.dHi_dt + nV, *SMB = A + nV, *BMB = SMB + nV, *usia = BMB + nV, *ussa = usia + nAc;
+  a.A = A; a.Cw = Cw; a.SMB = SMB; a.BMB = BMB;
+  a.Up_SIA = in->Up_SIA_Ac ? usia : up_sia;
+  a.Up_SSA = in->Up_SSA_Ac ? ussa : up_ssa;
+  a.noice = in->mask_noice ? g->thk_int : nullptr;
+  a.dev_of_orig = m.dev_of_orig; a.slice_g = m.slice_g; a.dt = in->dt; a.zero_edges = in->zero_edges != 0;
+  int rc = cuda_status(cudaMemsetAsync(a.dVi, 0, nV * ncm * sizeof(double), s), "memset fluxes");
+  if (!rc) rc = up(Cw, in->Cw, nV * ncm, s);
+  if (!rc) rc = up(A, in->A, nV, s);
+  if (!rc) rc = up(SMB, in->SMB_year, nV, s);
+  if (!rc) rc = up(BMB, in->BMB, nV, s);
+  if (!rc) rc = up(a.Hi, (const double *)Hi, nV, s);
+  if (!rc && in->Up_SIA_Ac) rc = up(usia, in->Up_SIA_Ac, nAc, s);
+  if (!rc && in->Up_SSA_Ac) rc = up(ussa, in->Up_SSA_Ac, nAc, s);
+  if (!rc && in->mask_noice) rc = up(g->thk_int, (const int *)in->mask_noice, nV, s);
+  const unsigned gv = (unsigned)((nV + 255) / 256), gc = (unsigned)((nAc + 255) / 256);
+  if (!rc) { k_thk_flux<<<gc, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_thk_flux"); }
+  if (!rc) { k_thk_factor<<<gv, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_thk_factor"); }
+  if (!rc && out && out->dVi_in) {
+    // Cw is no longer needed after the flux kernel: the scaled fluxes go there.
+    k_thk_fluxes_out<<<gv, 256, 0, s>>>(a, Cw);
+    rc = cuda_status(cudaGetLastError(), "k_thk_fluxes_out");
+  }
+  if (!rc) { k_thk_apply<<<gv, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_thk_apply"); }
+  auto dn = [&](double *dst, const double *src, size_t n) {
+    if (!dst || rc) return;
+    rc = cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, s), "thickness D2H");
+  };
+  dn(Hi, a.Hi, nV);
+  if (out) {
+    dn(out->Hi_prev, a.Hi_prev, nV);
+    dn(out->dHi_dt, a.dHi_dt, nV);
+    dn(out->dVi_in, Cw, nV * ncm);
+  }
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "thickness update");
+  return rc;
+}

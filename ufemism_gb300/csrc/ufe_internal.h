@@ -105,6 +105,7 @@ struct DevMesh {
 struct SsaWork;   // per-handle device buffers of the SSA solve (ufe_ssa.cu)
 struct SiaWork;   // per-handle device buffers of the SIA solve (ufe_sia.cu)
 struct AdjWork;   // per-handle device buffers of the SSA adjoint (ufe_ssa.cu)
+struct GeomWork;  // per-handle geometry preparation (ufe_geom.cu)
 
 }  // namespace ufe
 
@@ -116,10 +117,18 @@ struct ufe_mesh_s {
   ufe::SsaWork *ssa = nullptr;
   ufe::SiaWork *sia = nullptr;
   ufe::AdjWork *adj = nullptr;
+  ufe::GeomWork *geom = nullptr;
 };
 
 namespace ufe {
 void ssa_free(SsaWork *w);
 void sia_free(SiaWork *w);
 void adj_free(AdjWork *w);
+void geom_free(GeomWork *w);
+// Velocities of the last solves on a handle, on the device (caller order), or null.
+const double *ssa_device_Up(ufe_mesh_h h);
+const double *sia_device_Up(ufe_mesh_h h);
+// ufe_ssa_upload from device arrays of this device (sheet_count: grounded-ice vertices).
+int ssa_upload_impl(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, const ufe_ssa_inout *io,
+                    bool in_on_device, long long sheet_count);
 }  // namespace ufe

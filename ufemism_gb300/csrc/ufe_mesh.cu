@@ -382,6 +382,7 @@ extern "C" int ufe_mesh_destroy(ufe_mesh_h h) {
   ssa_free(h->ssa);
   sia_free(h->sia);
   adj_free(h->adj);
+  geom_free(h->geom);
   free_mesh(h->m);
   cudaStreamDestroy(h->stream);
   delete h;

@@ -25,6 +25,7 @@ struct SiaWork {
   int *mask = nullptr;     // nAc
   double *out = nullptr;   // D3 (nAc nZ), D, Ux, Uy, Up, Uo (5 nAc), U, V, D Aa (3 nV)
   double *zc = nullptr;    // zeta (nZ), zeta^3 (nZ)
+  bool solved = false;
 };
 
 void sia_free(SiaWork *w) {
@@ -116,6 +117,16 @@ __global__ void k_ac_to_aa3(int nV, const int *__restrict__ nC, const int *__res
 
 using namespace ufe;
 
+namespace ufe {
+// Up_SIA_Ac of the last ufe_sia_solve on this handle, on the device, or null.
+const double *sia_device_Up(ufe_mesh_h h) {
+  const SiaWork *w = h->sia;
+  if (!w || !w->solved) return nullptr;
+  const size_t na = w->nAc;
+  return w->out + na * w->nZ + 3 * na;
+}
+}  // namespace ufe
+
 extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out) {
   if (!h || !p || !in || !out) { set_error("ufe_sia_solve: null argument"); return UFE_BAD_ARG; }
   if (!in->mask_sheet_Ac || !in->Hi_Ac || !in->dHs_dx_Ac || !in->dHs_dy_Ac || !in->dHs_dp_Ac ||
@@ -179,6 +190,7 @@ extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in
   back(out->V_SIA, Va, nV);
   back(out->D_SIA, Da, nV);
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "sia solve");
+  w->solved = rc == UFE_OK;
   return rc;
 }
 

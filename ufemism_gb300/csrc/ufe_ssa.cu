@@ -1477,21 +1477,25 @@ int d2h(double *dst, const double *src, size_t n, cudaStream_t s) {
 
 using namespace ufe;
 
-extern "C" int ufe_ssa_upload(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, const ufe_ssa_inout *io) {
-  if (!h || !p || !in || !io) { set_error("ufe_ssa_upload: null argument"); return UFE_BAD_ARG; }
+namespace ufe {
+// ufe_ssa_upload; with in_on_device the arrays of `in` are device arrays of this device (the
+// device geometry preparation) and sheet_count is the number of grounded-ice vertices.
+int ssa_upload_impl(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, const ufe_ssa_inout *io,
+                    bool in_on_device, long long sheet_count) {
+  if (!h || !p || !in || !io) { set_error(std::string(in_on_device ? "ufe_ssa_upload_geometry" : "ufe_ssa_upload") + ": null argument"); return UFE_BAD_ARG; }
   if (!in->Hi || !in->Hb || !in->SL || !in->dHs_dx_shelf || !in->dHs_dy_shelf || !in->A_flow_mean ||
       !in->mask_sheet || !in->Hi_Ac || !in->Hb_Ac || !in->SL_Ac || !in->dHs_dx_shelf_Ac ||
       !in->dHs_dy_shelf_Ac || !in->A_flow_mean_Ac || !io->U_SSA || !io->V_SSA || !io->Ux_SSA_Ac || !io->Uy_SSA_Ac) {
-    set_error("ufe_ssa_upload: missing input array");
+    set_error(std::string(in_on_device ? "ufe_ssa_upload_geometry" : "ufe_ssa_upload") + ": missing input array");
     return UFE_BAD_ARG;
   }
   if (p->use_analytical_GL_flux && (!in->mask_gl_Ac || !in->dHi_dx_Ac || !in->dHi_dy_Ac || !in->dSL_dx_Ac ||
                                     !in->dSL_dy_Ac || !in->dHb_dx_Ac || !in->dHb_dy_Ac)) {
-    set_error("ufe_ssa_upload: use_analytical_GL_flux needs mask_gl_Ac and the Ac slopes of Hi, SL, Hb");
+    set_error(std::string(in_on_device ? "ufe_ssa_upload_geometry" : "ufe_ssa_upload") + ": use_analytical_GL_flux needs mask_gl_Ac and the Ac slopes of Hi, SL, Hb");
     return UFE_BAD_ARG;
   }
   if (p->use_analytical_GL_flux && p->sliding_law != UFE_SLIDING_COULOMB_REGULARISED) {
-    set_error("ufe_ssa_upload: the GL flux is implemented for the Coulomb_regularised law only (as in the reference)");
+    set_error(std::string(in_on_device ? "ufe_ssa_upload_geometry" : "ufe_ssa_upload") + ": the GL flux is implemented for the Coulomb_regularised law only (as in the reference)");
     return UFE_BAD_ARG;
   }
   int rc = ensure_work(h);
@@ -1502,12 +1506,16 @@ extern "C" int ufe_ssa_upload(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_i
   double *st = w->stage_in;
   const double *aa[6] = {in->Hi, in->Hb, in->SL, in->dHs_dx_shelf, in->dHs_dy_shelf, in->A_flow_mean};
   const double *ac[6] = {in->Hi_Ac, in->Hb_Ac, in->SL_Ac, in->dHs_dx_shelf_Ac, in->dHs_dy_shelf_Ac, in->A_flow_mean_Ac};
-  for (int k = 0; k < 6 && !rc; ++k) rc = h2d(st + k * nV, aa[k], nV, s);
-  for (int k = 0; k < 6 && !rc; ++k) rc = h2d(st + 6 * nV + k * nAc, ac[k], nAc, s);
+  const cudaMemcpyKind kin = in_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  auto cp = [&](double *dst, const double *src, size_t n) {
+    return cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(double), kin, s), "upload");
+  };
+  for (int k = 0; k < 6 && !rc; ++k) rc = cp(st + k * nV, aa[k], nV);
+  for (int k = 0; k < 6 && !rc; ++k) rc = cp(st + 6 * nV + k * nAc, ac[k], nAc);
   double *beta = st + 6 * nV + 6 * nAc;
   double *U = beta + nA, *V = U + nV, *Ux = V + nV, *Uy = Ux + nAc, *N = Uy + nAc;
   w->has_beta = in->beta_sq_AaAc != nullptr;
-  if (!rc && w->has_beta) rc = h2d(beta, in->beta_sq_AaAc, nA, s);
+  if (!rc && w->has_beta) rc = cp(beta, in->beta_sq_AaAc, nA);
   if (!rc) rc = h2d(U, io->U_SSA, nV, s);
   if (!rc) rc = h2d(V, io->V_SSA, nV, s);
   if (!rc) rc = h2d(Ux, io->Ux_SSA_Ac, nAc, s);
@@ -1516,17 +1524,32 @@ extern "C" int ufe_ssa_upload(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_i
   if (!rc && w->has_N) rc = h2d(N, io->N_AaAc, nA, s);
   w->gl = p->use_analytical_GL_flux != 0;
   if (!rc && w->gl) {
-    rc = cuda_status(cudaMemcpyAsync(w->gl_int, in->mask_gl_Ac, nAc * sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
-    if (!rc) rc = cuda_status(cudaMemcpyAsync(w->gl_int + nAc, in->mask_sheet, nV * sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
+    rc = cuda_status(cudaMemcpyAsync(w->gl_int, in->mask_gl_Ac, nAc * sizeof(int), kin, s), "upload");
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(w->gl_int + nAc, in->mask_sheet, nV * sizeof(int), kin, s), "upload");
     const double *gs[6] = {in->dHi_dx_Ac, in->dHi_dy_Ac, in->dSL_dx_Ac, in->dSL_dy_Ac, in->dHb_dx_Ac, in->dHb_dy_Ac};
-    for (int k = 0; k < 6 && !rc; ++k) rc = h2d(w->gl_dbl + k * nAc, gs[k], nAc, s);
+    for (int k = 0; k < 6 && !rc; ++k) rc = cp(w->gl_dbl + k * nAc, gs[k], nAc);
   }
   // Early-outs of solve_SSA (431-452): benchmark experiments without SSA, or no grounded ice.
-  long long sheet = 0;
-  for (size_t v = 0; v < nV; ++v) sheet += in->mask_sheet[v];
+  long long sheet = sheet_count;
+  if (!in_on_device)
+    for (size_t v = 0; v < nV; ++v) sheet += in->mask_sheet[v];
   w->zero = p->zero_velocities != 0 || sheet == 0;
   w->uploaded = rc == UFE_OK;
   return rc;
+}
+}  // namespace ufe
+
+namespace ufe {
+// Up_SSA_Ac of the last solve on this handle, on the device (caller order), or null.
+const double *ssa_device_Up(ufe_mesh_h h) {
+  const SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) return nullptr;
+  return w->stage_out + 2 * (size_t)w->nV + 2 * (size_t)w->nAc;
+}
+}  // namespace ufe
+
+extern "C" int ufe_ssa_upload(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, const ufe_ssa_inout *io) {
+  return ssa_upload_impl(h, p, in, io, false, 0);
 }
 
 namespace ufe {

@@ -152,3 +152,36 @@ def ensemble_member(n_vertices, seed):
     ssa, _ = prepare_inputs(mesh, Hi, Hb, SL)
     ssa["beta_sq_AaAc"] = np.exp(log_beta_field(mesh, std=1.0, ell=100e3, seed=int(seed) + 1))
     return base, mesh, ssa
+
+
+def areas_and_widths(base):
+    """Per-vertex cell areas A (nV) and connection widths Cw (nV, nC_mem) for the thickness
+    update, from the triangulation: A = a third of the adjacent triangle areas, Cw = the
+    distance between the centroids of the two triangles on either side of a connection (to
+    the edge midpoint on the domain boundary). Stand-ins for the reference's Voronoi cell
+    areas and circumcentre-to-circumcentre widths, with the same units and meaning."""
+    V = np.asarray(base.V, dtype=np.float64)
+    T = np.asarray(base.Tri, dtype=np.int64) - 1
+    p0, p1, p2 = V[T[:, 0]], V[T[:, 1]], V[T[:, 2]]
+    area = 0.5 * np.abs((p1[:, 0] - p0[:, 0]) * (p2[:, 1] - p0[:, 1]) - (p2[:, 0] - p0[:, 0]) * (p1[:, 1] - p0[:, 1]))
+    A = np.zeros(base.nV)
+    for k in range(3):
+        np.add.at(A, T[:, k], area / 3.0)
+    cen = (p0 + p1 + p2) / 3.0
+    edges = {}
+    for t in range(T.shape[0]):
+        for a, b in ((0, 1), (1, 2), (2, 0)):
+            key = (min(T[t, a], T[t, b]), max(T[t, a], T[t, b]))
+            edges.setdefault(key, []).append(t)
+    C = np.asarray(base.C, dtype=np.int64) - 1
+    nC = np.asarray(base.nC, dtype=np.int64)
+    Cw = np.zeros(C.shape, order="F")
+    for v in range(base.nV):
+        for c in range(nC[v]):
+            j = C[v, c]
+            ts = edges[(min(v, j), max(v, j))]
+            if len(ts) == 2:
+                Cw[v, c] = np.linalg.norm(cen[ts[0]] - cen[ts[1]])
+            else:
+                Cw[v, c] = np.linalg.norm(cen[ts[0]] - 0.5 * (V[v] + V[j]))
+    return A, Cw
