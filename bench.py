@@ -470,10 +470,10 @@ def adjoint_bench(args):
     p64 = api.default_params(precision=nat.UFE_FP64, **tight)
     p32 = api.default_params(precision=nat.UFE_MIXED, **tight)
 
-    def forward(lbeta, p):
+    def forward(lbeta, p, warm=None):
         f = dict(ssa)
         f["beta_sq_AaAc"] = np.exp(lbeta)
-        rc, out, st = dm.solve_ssa(f, p, check=False)
+        rc, out, st = dm.solve_ssa(f, p, warm=warm, check=False)
         U = np.concatenate([out["U_SSA"], out["Ux_SSA_Ac"]])
         V = np.concatenate([out["V_SSA"], out["Uy_SSA_Ac"]])
         return U, V, out, st
@@ -487,17 +487,21 @@ def adjoint_bench(args):
         rc, g, vs = dm.ssa_vjp(dJ, p, geom_mesh=mesh, tol=args.adj_tol, check=False)
         res[name] = dict(forward_ms=st["device_ms"], forward_sweeps=st["total_sweeps"],
                          picard=st["picard_iterations"], vjp_ms=vs["device_ms"], vjp_sweeps=vs["sweeps"],
-                         vjp_status=rc, vjp_rel_update=vs["last_rel_update"],
-                         vjp_over_forward=vs["device_ms"] / st["device_ms"], grad=g, U=U, V=V)
-    # finite differences with the mixed forward (converged to the FP64 fixed point)
+                         vjp_status=rc, vjp_rel_residual=vs["last_rel_update"],
+                         vjp_over_forward=vs["device_ms"] / st["device_ms"], grad=g, U=U, V=V, out=out)
+    # finite differences with the mixed forward (converged to the FP64 fixed point), each
+    # perturbed solve warm-started from the unperturbed solution and Picard state
     rng = np.random.default_rng(20261211)
     g = res["mixed"]["grad"]
+    base_out = res["mixed"]["out"]
+    warm = {k: base_out[k] for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")}
     J = lambda U, V: 0.5 * float(np.sum((U - Uo) ** 2 + (V - Vo) ** 2))
     fd = []
+    t_fd = time.time()
     for k in range(args.fd_directions):
         d = rng.normal(size=mesh.nVAaAc)
-        Up, Vp, _, _ = forward(lb + 1e-4 * d, p32)
-        Um, Vm, _, _ = forward(lb - 1e-4 * d, p32)
+        Up, Vp, _, _ = forward(lb + 1e-4 * d, p32, warm)
+        Um, Vm, _, _ = forward(lb - 1e-4 * d, p32, warm)
         f = (J(Up, Vp) - J(Um, Vm)) / 2e-4
         a = float(g["dJ_dlogbeta_sq_AaAc"] @ d)
         fd.append(abs(f - a) / abs(a))
@@ -512,9 +516,11 @@ def adjoint_bench(args):
         "vjp_over_forward_fp64": res["fp64"]["vjp_over_forward"],
         "vjp_over_forward_mixed": res["mixed"]["vjp_over_forward"],
         "forward": {k: {q: v[q] for q in ("forward_ms", "forward_sweeps", "picard", "vjp_ms", "vjp_sweeps",
-                                          "vjp_status", "vjp_rel_update")} for k, v in res.items()},
+                                          "vjp_status", "vjp_rel_residual")} for k, v in res.items()},
+        "vjp_method": "GMRES(100), 8 transposed sweeps per iteration",
         "gradient_fp64_vs_mixed_forward_rel_l2": agree,
         "fd_directions": args.fd_directions, "fd_rel_err_max": max(fd) if fd else None, "fd_rel_err": fd,
+        "fd_seconds": time.time() - t_fd,
     }
     print(json.dumps(line))
     dm.close()
@@ -534,7 +540,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-sample-sweeps", type=int, default=40)
     ap.add_argument("--adj-rn-tol", type=float, default=1e-10, help="adjoint: forward Picard tolerance")
-    ap.add_argument("--adj-tol", type=float, default=1e-13, help="adjoint: VJP relative update tolerance")
+    ap.add_argument("--adj-tol", type=float, default=1e-12, help="adjoint: VJP relative residual tolerance")
     ap.add_argument("--fd-directions", type=int, default=2)
     ap.add_argument("--workload", default="dome", choices=["dome", "ensemble", "marine", "adjoint"],
                     help="dome: the 200k-vertex single solve; ensemble: the batched ensemble")

@@ -259,10 +259,17 @@ int ufe_thickness_update(ufe_mesh_h mesh, const ufe_thickness_in *in, double *Hi
  * only; the grounding-line flux option is not differentiated. Output arrays may be NULL.
  * The forward solve should be converged well below the tolerances the gradient is wanted
  * to (the VJP differentiates the fixed point, not the truncated iteration). */
+enum { UFE_VJP_GMRES = 0, UFE_VJP_SOR = 1 };
 typedef struct ufe_vjp_params {
-  double tol;          /* stop when max |update| < tol * max |mu| (0: 1e-13) */
-  int32_t max_sweeps;  /* 0: 2000000 */
+  double tol;          /* GMRES: relative residual of the sweep-preconditioned system (0: 1e-12);
+                          SOR: stop when max |update| < tol * max |mu| (0: 1e-13) */
+  int32_t max_sweeps;  /* GMRES: iterations (0: 50000); SOR: sweeps (0: 2000000) */
   double omega;        /* 0: SSA_SOR_omega */
+  int32_t method;      /* UFE_VJP_GMRES (default): restarted GMRES on the fixed-point map of
+                          sweeps_per_iteration transposed sweeps (stops when a restart cycle
+                          gains less than 5 %); UFE_VJP_SOR: plain sweeps */
+  int32_t restart;     /* GMRES restart length (0: 100, at most 1000) */
+  int32_t sweeps_per_iteration;  /* GMRES: transposed sweeps per Krylov iteration (0: 8) */
 } ufe_vjp_params;
 typedef struct ufe_vjp_in {
   const double *dJ_dU, *dJ_dV;          /* (nV) */

@@ -47,13 +47,14 @@ def split(m, a):
     return a[:nV], a[nV:]
 
 
+@pytest.mark.parametrize("method", [nat.UFE_VJP_GMRES, nat.UFE_VJP_SOR])
 @pytest.mark.parametrize("name,kind", [("1k", "dome"), ("1k", "marine")])
-def test_vjp_matches_cpu_reference_and_finite_differences(name, kind):
+def test_vjp_matches_cpu_reference_and_finite_differences(name, kind, method):
     m, ssa, logb, dm, p, solve, U, V, f0, Uo, Vo = setup_case(name, kind)
     gU, gV = U - Uo, V - Vo
     dJ = dict(zip(("U_SSA", "Ux_SSA_Ac"), split(m, gU)))
     dJ.update(zip(("V_SSA", "Uy_SSA_Ac"), split(m, gV)))
-    rc, out, st = dm.ssa_vjp(dJ, p, geom_mesh=m)
+    rc, out, st = dm.ssa_vjp(dJ, p, geom_mesh=m, method=method)
     assert rc == nat.UFE_OK, st
     # CPU reference at the GPU's converged state
     lin = adj.Linearisation(m, f0, U, V)
@@ -120,7 +121,7 @@ def test_vjp_reports_divergence_and_recovers():
     gU, gV = U - Uo, V - Vo
     dJ = dict(zip(("U_SSA", "Ux_SSA_Ac"), split(m, gU)))
     dJ.update(zip(("V_SSA", "Uy_SSA_Ac"), split(m, gV)))
-    rc, out, st = dm.ssa_vjp(dJ, p, omega=1.99, max_sweeps=200000, check=False)
+    rc, out, st = dm.ssa_vjp(dJ, p, omega=1.99, max_sweeps=200000, check=False, method=nat.UFE_VJP_SOR)
     assert rc in (nat.UFE_DIVERGED, nat.UFE_OK, nat.UFE_NOT_CONVERGED)
     if rc == nat.UFE_OK:   # converged after all: the gradient must then be right
         lin = adj.Linearisation(m, f0, U, V)

@@ -103,8 +103,12 @@ class ThicknessOut(ct.Structure):
     _fields_ = [(n, P) for n in ("Hi_prev", "dHi_dt", "dVi_in")]
 
 
+UFE_VJP_GMRES, UFE_VJP_SOR = 0, 1
+
+
 class VjpParams(ct.Structure):
-    _fields_ = [("tol", F64), ("max_sweeps", I32), ("omega", F64)]
+    _fields_ = [("tol", F64), ("max_sweeps", I32), ("omega", F64), ("method", I32), ("restart", I32),
+                ("sweeps_per_iteration", I32)]
 
 
 class VjpIn(ct.Structure):

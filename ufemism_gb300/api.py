@@ -231,7 +231,8 @@ class DeviceMesh:
         return io
 
     def ssa_vjp(self, dJ: dict, params: dict, geom_mesh=None, tol: float = 0.0, max_sweeps: int = 0,
-                omega: float = 0.0, check: bool = True):
+                omega: float = 0.0, check: bool = True, method: int = 0, restart: int = 0,
+                sweeps_per_iteration: int = 0):
         """VJP of the last solve on this handle (ufe_ssa_vjp). ``dJ`` holds dJ/du as U_SSA,
         V_SSA (nV) and Ux_SSA_Ac, Uy_SSA_Ac (nAc). With ``geom_mesh`` (an AaAc mesh with the
         Aa and Ac derivative stencils) dJ/dHi on Aa is returned too. Returns (status,
@@ -253,7 +254,7 @@ class DeviceMesh:
             geom = nat.VjpGeom(*(_ptr(gk[k]) for k in ("nC", "C", "Nx", "Ny", "Aci", "Nx_Ac", "Ny_Ac")))
             out["dJ_dHi"] = np.zeros(self.nV)
         vo = nat.VjpOut(*(_ptr(out.get(k)) for k in nat.VJP_OUT_FIELDS))
-        vp = nat.VjpParams(tol, max_sweeps, omega)
+        vp = nat.VjpParams(tol, max_sweeps, omega, method, restart, sweeps_per_iteration)
         ps, _z = _params_struct(params)
         st = nat.VjpStats()
         rc = L.ufe_ssa_vjp(self._h, ct.byref(ps), ct.byref(vp), ct.byref(vin), ct.byref(geom) if geom else None,

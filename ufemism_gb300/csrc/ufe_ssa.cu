@@ -119,6 +119,7 @@ struct SsaArgs {
 constexpr unsigned int kBarrierError = 1u << 30;
 // Largest shared-memory mirror of a patch's rows (the rest of the 228 KB of an SM stays L1).
 constexpr size_t kLocalRowsMaxBytes = 160 * 1024;
+constexpr int kMaxKrylovRestart = 1000;   // largest GMRES restart length of the VJP
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
@@ -1061,6 +1062,56 @@ __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_adjoint_sor(const A
       return;
     }
   }
+}
+
+// ---- Krylov acceleration of the transposed SOR (GMRES on the sweep's fixed-point map) ----
+// One transposed sweep maps mu to S(mu; g) = G mu + M^-1 g. GMRES solves (I - G) mu = S(0; g)
+// with the operator x -> x - S(x; 0): one sweep per Krylov iteration, left-preconditioned by
+// the sweep itself. Vectors are the (mu_x, mu_y) pairs of the nP device rows.
+__global__ void k_krylov_load(int nP, const double2 *x, const double2 *alpha, double2 *mu, double *s) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nP) return;
+  const double2 v = x ? x[p] : make_double2(0.0, 0.0);
+  const double2 al = alpha[p];
+  mu[p] = v;
+  s[p] = fma(al.x, v.x, al.y * v.y);
+}
+
+// y = x - mu
+__global__ void k_krylov_sub(int n, const double *x, const double *mu, double *y) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) y[e] = x[e] - mu[e];
+}
+
+// Block partial sums of V_i . w: part[i * gridDim.x + block], i = blockIdx.y.
+__global__ void k_krylov_dots(int n, const double *V, size_t ld, const double *w, double *part) {
+  const double *v = V + (size_t)blockIdx.y * ld;
+  double acc = 0.0;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) acc = fma(v[e], w[e], acc);
+  __shared__ double sw[32];
+  acc = warp_sum(acc);
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) sw[wid] = acc;
+  __syncthreads();
+  if (wid == 0) {
+    double x = lane < (int)(blockDim.x >> 5) ? sw[lane] : 0.0;
+    x = warp_sum(x);
+    if (lane == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = x;
+  }
+}
+
+// w -= sum_i h_i V_i (i < nvec)
+__global__ void k_krylov_axpy(int n, int nvec, const double *V, size_t ld, const double *h, double *w) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  double acc = 0.0;
+  for (int i = 0; i < nvec; ++i) acc = fma(h[i], V[(size_t)i * ld + e], acc);
+  w[e] = w[e] - acc;
+}
+
+__global__ void k_krylov_scale(int n, const double *w, double f, double *v) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) v[e] = w[e] * f;
 }
 
 // Per-row set-up of the adjoint operator at the converged velocities: strain rates,
@@ -2417,15 +2468,21 @@ struct AdjWork {
   AdjCtl *ctl = nullptr;
   AdjCtl *ctl_host = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // Krylov work (allocated on first use): basis (restart + 1 vectors), w, x, c, zero rows,
+  // dot partials (device and pinned host), Givens coefficients on the device
+  double *kry = nullptr;
+  size_t kry_vectors = 0;
+  double *part = nullptr, *part_host = nullptr, *hdev = nullptr;
 };
 
 void adj_free(AdjWork *w) {
   if (!w) return;
   void *ptrs[] = {w->cT, w->kT, w->ee, w->kh, w->alpha, w->dinv, w->g, w->mu, w->c3, w->s, w->eta, w->fr,
-                  w->inv_nb, w->K, w->stage, w->geom_int, w->geom_dbl, w->prog, w->ctl};
+                  w->inv_nb, w->K, w->stage, w->geom_int, w->geom_dbl, w->prog, w->ctl, w->kry, w->part, w->hdev};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
+  if (w->part_host) cudaFreeHost(w->part_host);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   delete w;
@@ -2473,6 +2530,191 @@ int ensure_adj(ufe_mesh_h h) {
 }  // namespace
 }  // namespace ufe
 
+namespace ufe {
+namespace {
+
+constexpr int kKrylovBlocks = 304;
+
+struct Krylov {
+  int sweeps_per_apply = 1;
+  ufe_mesh_h h;
+  AdjWork *a;
+  AdjArgs aa;
+  cudaStream_t s;
+  int nP, n;          // rows, vector length (2 nP)
+  size_t ld;          // vector stride
+  double *V, *w, *x, *c;
+  double2 *zero;
+  int sweeps = 0;
+  int err = 0;
+};
+
+// One transposed sweep of mu (in place) with right-hand side g.
+int kry_sweep(Krylov &k, const double2 *g) {
+  int rc = cuda_status(cudaMemsetAsync(k.a->prog, 0, 32 * (size_t)k.h->m.n_patch * sizeof(unsigned int), k.s), "memset prog");
+  if (!rc) rc = cuda_status(cudaMemsetAsync(k.a->ctl, 0, sizeof(AdjCtl), k.s), "memset adj ctl");
+  AdjArgs aa = k.aa;
+  aa.g = g;
+  aa.max_sweeps = k.sweeps_per_apply;
+  aa.tol = 0.0;
+  void *args[] = {(void *)&aa};
+  if (!rc)
+    rc = cuda_status(cudaLaunchCooperativeKernel((const void *)ssa_adjoint_sor, dim3(k.h->m.n_patch), dim3(kSsaBlock), args, 0, k.s),
+                     "ssa_adjoint_sor");
+  k.sweeps += k.sweeps_per_apply;
+  return rc;
+}
+
+// y = x - S(x; 0)
+int kry_apply(Krylov &k, const double *xin, double *y) {
+  const unsigned gp = (unsigned)((k.nP + 255) / 256), gn = (unsigned)((k.n + 255) / 256);
+  k_krylov_load<<<gp, 256, 0, k.s>>>(k.nP, reinterpret_cast<const double2 *>(xin), k.a->alpha, k.a->mu, k.a->s);
+  int rc = cuda_status(cudaGetLastError(), "k_krylov_load");
+  if (!rc) rc = kry_sweep(k, k.zero);
+  if (!rc) {
+    k_krylov_sub<<<gn, 256, 0, k.s>>>(k.n, xin, reinterpret_cast<const double *>(k.a->mu), y);
+    rc = cuda_status(cudaGetLastError(), "k_krylov_sub");
+  }
+  return rc;
+}
+
+// h[i] = V_i . wv for i < nvec (fixed-order sums: deterministic); also reads back the
+// sweep control block so that a failed wait is noticed.
+int kry_dots(Krylov &k, int nvec, const double *Vb, const double *wv, double *hout) {
+  k_krylov_dots<<<dim3(kKrylovBlocks, nvec), 256, 0, k.s>>>(k.n, Vb, k.ld, wv, k.a->part);
+  int rc = cuda_status(cudaGetLastError(), "k_krylov_dots");
+  if (!rc)
+    rc = cuda_status(cudaMemcpyAsync(k.a->part_host, k.a->part, (size_t)nvec * kKrylovBlocks * sizeof(double),
+                                     cudaMemcpyDeviceToHost, k.s), "dots D2H");
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(k.a->ctl_host, k.a->ctl, sizeof(AdjCtl), cudaMemcpyDeviceToHost, k.s), "ctl D2H");
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(k.s), "dots");
+  if (rc) return rc;
+  if (k.a->ctl_host->err) k.err = k.a->ctl_host->err;
+  for (int i = 0; i < nvec; ++i) {
+    double t = 0.0;
+    for (int b = 0; b < kKrylovBlocks; ++b) t += k.a->part_host[(size_t)i * kKrylovBlocks + b];
+    hout[i] = t;
+  }
+  return UFE_OK;
+}
+
+int kry_axpy(Krylov &k, int nvec, const double *Vb, const double *coef, double *wv) {
+  // A copy from pageable memory returns once the data is staged, so the caller may reuse
+  // the coefficient array at once.
+  int rc = cuda_status(cudaMemcpyAsync(k.a->hdev, coef, (size_t)nvec * sizeof(double), cudaMemcpyHostToDevice, k.s), "coef H2D");
+  if (!rc) {
+    k_krylov_axpy<<<(unsigned)((k.n + 255) / 256), 256, 0, k.s>>>(k.n, nvec, Vb, k.ld, k.a->hdev, wv);
+    rc = cuda_status(cudaGetLastError(), "k_krylov_axpy");
+  }
+  return rc;
+}
+
+// Restarted GMRES(m) on (I - G) mu = S(0; g); classical Gram-Schmidt applied twice.
+// Returns the relative residual of the preconditioned system in *rel; mu ends in a->mu.
+int adj_gmres(Krylov &k, int m, double tol, int max_iter, double *rel, int *iters) {
+  const unsigned gp = (unsigned)((k.nP + 255) / 256);
+  // c = S(0; g)
+  k_krylov_load<<<gp, 256, 0, k.s>>>(k.nP, nullptr, k.a->alpha, k.a->mu, k.a->s);
+  int rc = cuda_status(cudaGetLastError(), "k_krylov_load");
+  if (!rc) rc = kry_sweep(k, k.a->g);
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(k.c, k.a->mu, k.n * sizeof(double), cudaMemcpyDeviceToDevice, k.s), "copy c");
+  if (!rc) rc = cuda_status(cudaMemsetAsync(k.x, 0, k.n * sizeof(double), k.s), "memset x");
+  if (rc) return rc;
+  double beta0 = 0.0;
+  if ((rc = kry_dots(k, 1, k.c, k.c, &beta0))) return rc;
+  beta0 = std::sqrt(beta0);
+  *iters = 0;
+  *rel = 0.0;
+  if (beta0 == 0.0) {
+    k_krylov_load<<<gp, 256, 0, k.s>>>(k.nP, nullptr, k.a->alpha, k.a->mu, k.a->s);
+    return cuda_status(cudaGetLastError(), "k_krylov_load");
+  }
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), gv(m + 1), hcol(m + 1), h2(m + 1), y(m);
+  auto Hm = [&](int i, int j) -> double & { return H[(size_t)j * (m + 1) + i]; };
+  int total = 0;
+  double res = 1.0, cycle_start = 1.0;
+  while (total < max_iter) {
+    // r = c - A x (x = 0 on the first cycle)
+    double *V0 = k.V;
+    if (total == 0) {
+      rc = cuda_status(cudaMemcpyAsync(V0, k.c, k.n * sizeof(double), cudaMemcpyDeviceToDevice, k.s), "copy r");
+    } else {
+      rc = kry_apply(k, k.x, k.w);
+      if (!rc) {
+        k_krylov_sub<<<(unsigned)((k.n + 255) / 256), 256, 0, k.s>>>(k.n, k.c, k.w, V0);
+        rc = cuda_status(cudaGetLastError(), "k_krylov_sub");
+      }
+    }
+    if (rc) return rc;
+    double beta = 0.0;
+    if ((rc = kry_dots(k, 1, V0, V0, &beta))) return rc;
+    beta = std::sqrt(beta);
+    if (beta <= tol * beta0) { res = beta / beta0; break; }
+    k_krylov_scale<<<(unsigned)((k.n + 255) / 256), 256, 0, k.s>>>(k.n, V0, 1.0 / beta, V0);
+    if ((rc = cuda_status(cudaGetLastError(), "k_krylov_scale"))) return rc;
+    std::fill(gv.begin(), gv.end(), 0.0);
+    gv[0] = beta;
+    int j_end = 0;
+    for (int j = 0; j < m && total < max_iter; ++j) {
+      double *Vj = k.V + (size_t)j * k.ld;
+      if ((rc = kry_apply(k, Vj, k.w))) return rc;
+      if ((rc = kry_dots(k, j + 1, k.V, k.w, hcol.data()))) return rc;
+      if ((rc = kry_axpy(k, j + 1, k.V, hcol.data(), k.w))) return rc;
+      if ((rc = kry_dots(k, j + 1, k.V, k.w, h2.data()))) return rc;
+      if ((rc = kry_axpy(k, j + 1, k.V, h2.data(), k.w))) return rc;
+      for (int i = 0; i <= j; ++i) hcol[i] += h2[i];
+      double nw = 0.0;
+      if ((rc = kry_dots(k, 1, k.w, k.w, &nw))) return rc;
+      nw = std::sqrt(nw);
+      if (k.err) return k.err;
+      for (int i = 0; i <= j; ++i) Hm(i, j) = hcol[i];
+      Hm(j + 1, j) = nw;
+      if (nw > 0.0) {
+        k_krylov_scale<<<(unsigned)((k.n + 255) / 256), 256, 0, k.s>>>(k.n, k.w, 1.0 / nw, k.V + (size_t)(j + 1) * k.ld);
+        if ((rc = cuda_status(cudaGetLastError(), "k_krylov_scale"))) return rc;
+      }
+      // Givens rotations: apply the previous ones to the new column, then make a new one
+      for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * Hm(i, j) + sn[i] * Hm(i + 1, j);
+        Hm(i + 1, j) = -sn[i] * Hm(i, j) + cs[i] * Hm(i + 1, j);
+        Hm(i, j) = t;
+      }
+      const double r = std::hypot(Hm(j, j), Hm(j + 1, j));
+      cs[j] = r > 0.0 ? Hm(j, j) / r : 1.0;
+      sn[j] = r > 0.0 ? Hm(j + 1, j) / r : 0.0;
+      Hm(j, j) = r;
+      Hm(j + 1, j) = 0.0;
+      gv[j + 1] = -sn[j] * gv[j];
+      gv[j] = cs[j] * gv[j];
+      ++total;
+      j_end = j + 1;
+      res = std::fabs(gv[j + 1]) / beta0;
+      if (!std::isfinite(res)) return UFE_DIVERGED;
+      if (res <= tol || nw == 0.0) break;
+    }
+    // x += V y, H y = g (upper triangular)
+    for (int i = j_end - 1; i >= 0; --i) {
+      double t = gv[i];
+      for (int l = i + 1; l < j_end; ++l) t -= Hm(i, l) * y[l];
+      y[i] = t / Hm(i, i);
+    }
+    for (int i = 0; i < j_end; ++i) y[i] = -y[i];
+    if ((rc = kry_axpy(k, j_end, k.V, y.data(), k.x))) return rc;
+    if (res <= tol) break;
+    // a restart cycle that gains less than 5 % will not reach the tolerance: stop
+    if (res > 0.95 * cycle_start) break;
+    cycle_start = res;
+  }
+  *rel = res;
+  *iters = total;
+  // mu = x (and s consistent with it, for the gradient kernels that only read mu)
+  k_krylov_load<<<gp, 256, 0, k.s>>>(k.nP, reinterpret_cast<const double2 *>(k.x), k.a->alpha, k.a->mu, k.a->s);
+  return cuda_status(cudaGetLastError(), "k_krylov_load");
+}
+
+}  // namespace
+}  // namespace ufe
+
 extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_params *vp, const ufe_vjp_in *in,
                            const ufe_vjp_geom *geom, ufe_vjp_out *out, ufe_vjp_stats *stats) {
   if (!h || !p || !in || !out) { set_error("ufe_ssa_vjp: null argument"); return UFE_BAD_ARG; }
@@ -2495,9 +2737,11 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   const DevMesh &m = h->m;
   cudaStream_t s = h->stream;
   const size_t nV = m.nV, nAc = m.nAc, nA = m.nA, nP = m.nP, ncm = m.ncm;
-  // The error of a slowly contracting iteration is about its update / (1 - rate), so the
-  // default stops only when updates reach 1e-13 of the state.
-  const double tol = vp && vp->tol > 0 ? vp->tol : 1e-13;
+  // SOR: the error of a slowly contracting iteration is about its update / (1 - rate), so
+  // the default stops only when updates reach 1e-13 of the state. GMRES: relative residual
+  // of the sweep-preconditioned system.
+  const bool gmres_default = !vp || vp->method == UFE_VJP_GMRES;
+  const double tol = vp && vp->tol > 0 ? vp->tol : (gmres_default ? 1e-12 : 1e-13);
   const int max_sweeps = vp && vp->max_sweeps > 0 ? vp->max_sweeps : 2000000;
   const double omega = vp && vp->omega > 0 ? vp->omega : p->SSA_SOR_omega;
   double *st = a->stage;
@@ -2537,10 +2781,38 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   aa.prog = a->prog; aa.cT = a->cT; aa.kT = a->kT; aa.ee = a->ee; aa.c3 = a->c3; aa.kh = a->kh; aa.alpha = a->alpha;
   aa.dinv = a->dinv; aa.g = a->g; aa.mu = a->mu; aa.s = a->s; aa.ctl = a->ctl; aa.omega = omega; aa.tol = tol;
   aa.max_sweeps = max_sweeps; aa.timeout_ns = 20LL * 1000 * 1000 * 1000;
-  if (!rc) {
+  const bool krylov = !vp || vp->method == UFE_VJP_GMRES;
+  int k_iters = 0, k_err = 0;
+  double k_rel = 0.0;
+  if (!rc && !krylov) {
     void *args[] = {(void *)&aa};
     rc = cuda_status(cudaLaunchCooperativeKernel((const void *)ssa_adjoint_sor, dim3(m.n_patch), dim3(kSsaBlock), args, 0, s),
                      "ssa_adjoint_sor");
+  } else if (!rc) {
+    const int restart = std::min(kMaxKrylovRestart, vp && vp->restart > 0 ? vp->restart : 100);
+    const size_t n2 = 2 * nP;
+    const size_t need = (size_t)(restart + 1) + 4;   // basis, w, x, c, zero rows
+    if (a->kry_vectors < need) {
+      if (a->kry) { cudaFree(a->kry); a->kry = nullptr; }
+      rc = cuda_status(cudaMalloc(&a->kry, need * n2 * sizeof(double)), "krylov basis");
+      if (!rc) a->kry_vectors = need;
+    }
+    if (!rc && !a->part) rc = cuda_status(cudaMalloc(&a->part, (size_t)(kMaxKrylovRestart + 1) * kKrylovBlocks * sizeof(double)), "krylov dots");
+    if (!rc && !a->part_host) rc = cuda_status(cudaMallocHost(&a->part_host, (size_t)(kMaxKrylovRestart + 1) * kKrylovBlocks * sizeof(double)), "krylov dots host");
+    if (!rc && !a->hdev) rc = cuda_status(cudaMalloc(&a->hdev, (size_t)(kMaxKrylovRestart + 1) * sizeof(double)), "krylov coefficients");
+    if (!rc) {
+      Krylov k;
+      k.h = h; k.a = a; k.aa = aa; k.s = s; k.nP = (int)nP; k.n = (int)n2; k.ld = n2;
+      k.V = a->kry; k.w = k.V + (size_t)(restart + 1) * n2; k.x = k.w + n2; k.c = k.x + n2;
+      k.zero = reinterpret_cast<double2 *>(k.c + n2);
+      k.sweeps_per_apply = vp && vp->sweeps_per_iteration > 0 ? vp->sweeps_per_iteration : 8;
+      rc = cuda_status(cudaMemsetAsync(k.zero, 0, n2 * sizeof(double), s), "memset zero");
+      const int max_iter = vp && vp->max_sweeps > 0 ? vp->max_sweeps : 50000;
+      if (!rc) rc = adj_gmres(k, restart, tol, max_iter, &k_rel, &k_iters);
+      k_iters = k.sweeps;
+      k_err = k.err;
+      if (rc == UFE_DIVERGED) { rc = UFE_OK; k_rel = HUGE_VAL; k_err = UFE_DIVERGED; }
+    }
   }
   AdjGrad ag;
   ag.nP = (int)nP; ag.nV = (int)nV; ag.orig_of_dev = m.orig_of_dev; ag.deg = m.deg; ag.slice_g = m.slice_g;
@@ -2587,6 +2859,13 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   cudaEventElapsedTime(&ms, a->ev0, a->ev1);
   const AdjCtl &c = *a->ctl_host;
   int status = c.status;
+  if (krylov) {
+    status = k_err ? k_err : (k_rel <= tol ? UFE_OK : UFE_NOT_CONVERGED);
+    if (status == UFE_DIVERGED) set_error("ufe_ssa_vjp: GMRES produced a non-finite residual");
+    else if (status == UFE_NOT_CONVERGED) set_error("ufe_ssa_vjp: the GMRES iteration limit was reached before the tolerance");
+    a->ctl_host->sweeps = k_iters;
+    a->ctl_host->last_rel = k_rel;
+  }
   if (status == UFE_DIVERGED) set_error("ufe_ssa_vjp: the transposed SOR diverged (lower the relaxation factor)");
   else if (status == UFE_NOT_CONVERGED) set_error("ufe_ssa_vjp: max_sweeps reached before the tolerance");
   if (c.err) { status = c.err; set_error("ufe_ssa_vjp: a device-side bounded wait timed out"); }
