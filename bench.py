@@ -465,8 +465,10 @@ def adjoint_bench(args):
     torch.cuda.set_device(0)
     api.init(0)
     dm = api.DeviceMesh(mesh)
-    tight = dict(SSA_RN_tol=args.adj_rn_tol, SSA_max_residual_UV=args.adj_rn_tol / 10, SSA_max_outer_loops=400,
-                 SSA_max_inner_loops=2000000)
+    # The SOR tolerance is absolute (m/yr); below ~1e-10 it is under the FP64 floor of the
+    # defect for velocities of a few km/yr and would never be met.
+    tight = dict(SSA_RN_tol=args.adj_rn_tol, SSA_max_residual_UV=max(args.adj_rn_tol / 10, 1e-10),
+                 SSA_max_outer_loops=400, SSA_max_inner_loops=2000000)
     p64 = api.default_params(precision=nat.UFE_FP64, **tight)
     p32 = api.default_params(precision=nat.UFE_MIXED, **tight)
 
@@ -482,6 +484,9 @@ def adjoint_bench(args):
     res = {}
     for name, p in (("fp64", p64), ("mixed", p32)):
         U, V, out, st = forward(lb, p)
+        print("forward %s: %.1f ms, %d Picard, %d sweeps, RN %.2e" % (name, st["device_ms"], st["picard_iterations"],
+                                                                       st["total_sweeps"], st["last_RN"]),
+              file=sys.stderr, flush=True)
         dJ = dict(U_SSA=out["U_SSA"] - Uo[:base.nV], V_SSA=out["V_SSA"] - Vo[:base.nV],
                   Ux_SSA_Ac=out["Ux_SSA_Ac"] - Uo[base.nV:], Uy_SSA_Ac=out["Uy_SSA_Ac"] - Vo[base.nV:])
         rc, g, vs = dm.ssa_vjp(dJ, p, geom_mesh=mesh, tol=args.adj_tol, check=False)
@@ -489,19 +494,24 @@ def adjoint_bench(args):
                          picard=st["picard_iterations"], vjp_ms=vs["device_ms"], vjp_sweeps=vs["sweeps"],
                          vjp_status=rc, vjp_rel_residual=vs["last_rel_update"],
                          vjp_over_forward=vs["device_ms"] / st["device_ms"], grad=g, U=U, V=V, out=out)
-    # finite differences with the mixed forward (converged to the FP64 fixed point), each
-    # perturbed solve warm-started from the unperturbed solution and Picard state
+    # finite differences with the mixed forward (converged to the FP64 fixed point), every
+    # perturbed solve from a cold start like the unperturbed one: the SOR's stopping rule
+    # (an absolute update below the tolerance) leaves an error of about tolerance / (1 - rate)
+    # in the slowest mode, which cancels in the difference only when both solves follow the
+    # same path (warm starts from the unperturbed solution measured 1e-4 disagreement).
     rng = np.random.default_rng(20261211)
     g = res["mixed"]["grad"]
-    base_out = res["mixed"]["out"]
-    warm = {k: base_out[k] for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")}
+    warm = None
     J = lambda U, V: 0.5 * float(np.sum((U - Uo) ** 2 + (V - Vo) ** 2))
     fd = []
     t_fd = time.time()
     for k in range(args.fd_directions):
         d = rng.normal(size=mesh.nVAaAc)
-        Up, Vp, _, _ = forward(lb + 1e-4 * d, p32, warm)
-        Um, Vm, _, _ = forward(lb - 1e-4 * d, p32, warm)
+        Up, Vp, _, stp = forward(lb + 1e-4 * d, p32, warm)
+        Um, Vm, _, stm = forward(lb - 1e-4 * d, p32, warm)
+        print("fd direction %d: %.1f + %.1f ms, %d + %d sweeps" % (k, stp["device_ms"], stm["device_ms"],
+                                                                   stp["total_sweeps"], stm["total_sweeps"]),
+              file=sys.stderr, flush=True)
         f = (J(Up, Vp) - J(Um, Vm)) / 2e-4
         a = float(g["dJ_dlogbeta_sq_AaAc"] @ d)
         fd.append(abs(f - a) / abs(a))
