@@ -227,6 +227,10 @@ int ufe_geometry_update(ufe_mesh_h mesh, const double *Hi, const double *Hb, con
 int ufe_ssa_upload_geometry(ufe_mesh_h mesh, const ufe_params *params, const double *Hi, const double *Hb,
                             const double *SL, const double *A_flow_mean, const double *A_flow_mean_Ac,
                             const double *beta_sq_AaAc, const ufe_ssa_inout *inout);
+/* solve_SIA on the device geometry of the last ufe_geometry_update / ufe_ssa_upload_geometry
+ * (mask_sheet_Ac, Hi_Ac and the Ac surface slopes never leave the device); A_flow_Ac (nAc,nZ)
+ * from the host. */
+int ufe_sia_solve_geometry(ufe_mesh_h mesh, const ufe_params *params, const double *A_flow_Ac, ufe_sia_out *out);
 
 /* calculate_ice_thickness_change (ice_dynamics_module.f90:31-237) on the device: upwind ice
  * volume fluxes across every Aa connection from Up_SIA_Ac + Up_SSA_Ac, the outflux rescale

@@ -113,3 +113,34 @@ def test_thickness_update_from_device_velocities():
     ref = orc.thickness_change(m, A, Cw, so["Up_SIA_Ac"], o["Up_SSA_Ac"], smb, bmb, 5.0, ssa["Hi"])
     assert np.array_equal(got[0], ref[0])
     dm.close()
+
+
+def test_device_time_step_geometry_sia_ssa_thickness():
+    """A whole velocity-and-thickness step on the device from Hi, Hb, SL: geometry, SIA and
+    SSA solves on it, thickness update from the velocities the solves left on the device —
+    identical to the same step fed with the oracle's host-prepared fields."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, "marine")
+    A, Cw = wl.areas_and_widths(m.base)
+    rng = np.random.default_rng(2)
+    smb = rng.normal(size=m.base.nV) * 0.5
+    bmb = -np.abs(rng.normal(size=m.base.nV)) * 5.0 * (ssa["Hi"] > 0)
+    p = api.default_params()
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    dm.ssa_upload_geometry(ssa["Hi"], ssa["Hb"], ssa["SL"], ssa["A_flow_mean"], ssa["A_flow_mean_Ac"], p)
+    rc, st = dm.ssa_run(p, check=False)
+    o_dev = dm.ssa_download()
+    s_dev = dm.solve_sia_geometry(sia["A_flow_Ac"], p)
+    H_dev = dm.thickness_update(ssa["Hi"], A, Cw, smb, bmb, 10.0)[0]
+    dm2 = api.DeviceMesh(m)
+    rc2, o_host, st2 = dm2.solve_ssa(ssa, p, check=False)
+    s_host = dm2.solve_sia(sia, p)
+    for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "Up_SSA_Ac"):
+        assert np.array_equal(o_dev[k], o_host[k]), k
+    for k in ("D_SIA_3D_Ac", "Up_SIA_Ac", "U_SIA", "V_SIA"):
+        assert np.array_equal(s_dev[k], s_host[k]), k
+    ref = orc.thickness_change(m, A, Cw, s_host["Up_SIA_Ac"], o_host["Up_SSA_Ac"], smb, bmb, 10.0, ssa["Hi"])
+    assert np.array_equal(H_dev, ref[0])
+    dm.close()
+    dm2.close()

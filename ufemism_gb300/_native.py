@@ -181,6 +181,7 @@ PROTOTYPES = {
     "ufe_geometry_attach": (I32, [P, ct.POINTER(GeometryMesh)]),
     "ufe_geometry_update": (I32, [P, P, P, P, ct.POINTER(GeometryOut)]),
     "ufe_ssa_upload_geometry": (I32, [P, ct.POINTER(Params), P, P, P, P, P, P, ct.POINTER(SsaInout)]),
+    "ufe_sia_solve_geometry": (I32, [P, ct.POINTER(Params), P, ct.POINTER(SiaOut)]),
     "ufe_thickness_update": (I32, [P, ct.POINTER(ThicknessIn), P, ct.POINTER(ThicknessOut)]),
     "ufe_ssa_vjp": (I32, [P, ct.POINTER(Params), ct.POINTER(VjpParams), ct.POINTER(VjpIn), ct.POINTER(VjpGeom),
                           ct.POINTER(VjpOut), ct.POINTER(VjpStats)]),

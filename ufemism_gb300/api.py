@@ -305,6 +305,24 @@ class DeviceMesh:
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_ssa_upload_geometry")
 
+    def solve_sia_geometry(self, A_flow_Ac, params: dict):
+        """ufe_sia_solve_geometry: the SIA on the device geometry of the last geometry update."""
+        L = nat.load()
+        nZ = len(params["zeta"])
+        A = np.asfortranarray(A_flow_Ac, dtype=np.float64)
+        out = dict(D_SIA_3D_Ac=np.zeros((self.nAc, nZ), order="F"))
+        for k in ("D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac", "Uo_SIA_Ac"):
+            out[k] = np.zeros(self.nAc)
+        for k in ("U_SIA", "V_SIA", "D_SIA"):
+            out[k] = np.zeros(self.nV)
+        so = nat.SiaOut(*(_ptr(out[k]) for k in ("D_SIA_3D_Ac", "D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac",
+                                                  "Uo_SIA_Ac", "U_SIA", "V_SIA", "D_SIA")))
+        ps, _z = _params_struct(params)
+        rc = L.ufe_sia_solve_geometry(self._h, ct.byref(ps), A.ctypes.data, ct.byref(so))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_sia_solve_geometry")
+        return out
+
     def thickness_update(self, Hi, A, Cw, SMB_year, BMB, dt, Up_SIA_Ac=None, Up_SSA_Ac=None, mask_noice=None,
                          zero_edges=True):
         """calculate_ice_thickness_change on the device (ufe_thickness_update). Velocities left

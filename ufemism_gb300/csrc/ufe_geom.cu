@@ -348,6 +348,22 @@ extern "C" int ufe_ssa_upload_geometry(ufe_mesh_h h, const ufe_params *p, const 
   return ssa_upload_impl(h, p, &in, io, true, sheet);
 }
 
+extern "C" int ufe_sia_solve_geometry(ufe_mesh_h h, const ufe_params *p, const double *A_flow_Ac, ufe_sia_out *out) {
+  if (!h || !p || !A_flow_Ac || !out) { set_error("ufe_sia_solve_geometry: null argument"); return UFE_BAD_ARG; }
+  if (!h->geom || !h->geom->computed) {
+    set_error("ufe_sia_solve_geometry: no device geometry (ufe_geometry_update or ufe_ssa_upload_geometry first)");
+    return UFE_BAD_ARG;
+  }
+  GeomArgs a = args_of(h->geom);
+  ufe_sia_in in;
+  in.mask_sheet_Ac = ACM(a, MC_SHEET);
+  in.Hi_Ac = ACF(a, C_HI);
+  in.dHs_dx_Ac = ACF(a, C_DHS_DX); in.dHs_dy_Ac = ACF(a, C_DHS_DY);
+  in.dHs_dp_Ac = ACF(a, C_DHS_DP); in.dHs_do_Ac = ACF(a, C_DHS_DO);
+  in.A_flow_Ac = A_flow_Ac;
+  return sia_solve_impl(h, p, &in, out, true);
+}
+
 // ---------------------------------------------------------------------------------------
 // Ice thickness update: calculate_ice_thickness_change (ice_dynamics_module.f90:31-237).
 //

@@ -127,7 +127,10 @@ const double *sia_device_Up(ufe_mesh_h h) {
 }
 }  // namespace ufe
 
-extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out) {
+namespace ufe {
+// ufe_sia_solve; with fields_on_device the mask and the five Ac fields of `in` are device
+// arrays of this device (the device geometry preparation), A_flow_Ac stays a host array.
+int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out, bool fields_on_device) {
   if (!h || !p || !in || !out) { set_error("ufe_sia_solve: null argument"); return UFE_BAD_ARG; }
   if (!in->mask_sheet_Ac || !in->Hi_Ac || !in->dHs_dx_Ac || !in->dHs_dy_Ac || !in->dHs_dp_Ac ||
       !in->dHs_do_Ac || !in->A_flow_Ac || !p->zeta) {
@@ -157,10 +160,11 @@ extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in
   const size_t na = nAc;
   double *H = w->in, *sx = H + na, *sy = sx + na, *sp = sy + na, *so = sp + na, *A = so + na;
   rc = cuda_status(cudaMemcpyAsync(w->zc, zc.data(), zc.size() * sizeof(double), cudaMemcpyHostToDevice, s), "H2D zeta");
-  if (!rc) rc = cuda_status(cudaMemcpyAsync(w->mask, in->mask_sheet_Ac, na * sizeof(int), cudaMemcpyHostToDevice, s), "H2D");
+  const cudaMemcpyKind kin = fields_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(w->mask, in->mask_sheet_Ac, na * sizeof(int), kin, s), "sia input");
   const double *src[5] = {in->Hi_Ac, in->dHs_dx_Ac, in->dHs_dy_Ac, in->dHs_dp_Ac, in->dHs_do_Ac};
   for (int k = 0; k < 5 && !rc; ++k)
-    rc = cuda_status(cudaMemcpyAsync(w->in + k * na, src[k], na * sizeof(double), cudaMemcpyHostToDevice, s), "H2D");
+    rc = cuda_status(cudaMemcpyAsync(w->in + k * na, src[k], na * sizeof(double), kin, s), "sia input");
   if (!rc) rc = cuda_status(cudaMemcpyAsync(A, in->A_flow_Ac, na * nZ * sizeof(double), cudaMemcpyHostToDevice, s), "H2D A_flow");
   double *D3 = w->out, *D = D3 + na * nZ, *Ux = D + na, *Uy = Ux + na, *Up = Uy + na, *Uo = Up + na;
   double *Ua = Uo + na, *Va = Ua + nV, *Da = Va + nV;
@@ -192,6 +196,11 @@ extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "sia solve");
   w->solved = rc == UFE_OK;
   return rc;
+}
+}  // namespace ufe
+
+extern "C" int ufe_sia_solve(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out) {
+  return sia_solve_impl(h, p, in, out, false);
 }
 
 // ---------------------------------------------------------------------------------------
