@@ -412,7 +412,7 @@ static void basal_yield_stress(const or_base *b, const or_aaac *m, const or_ssa_
 /* calculate_GL_flux, ice_dynamics_module.f90:848-949 (Coulomb_regularised / Tsai et al. 2015) */
 static int gl_flux(const or_base *b, const or_aaac *m, const or_params *p, or_ssa_fields *f,
                    const double *phi_fric_AaAc) {
-  const int nV = b->nV, nAc = m->nAc;
+  const int nAc = m->nAc;
   const double Q0 = 0.61;
   if (p->sliding_law != 0) return OR_ERR_BAD_ARG; /* reference: only Coulomb_regularised */
   for (int aci = 1; aci <= nAc; aci++) {
