@@ -153,3 +153,37 @@ def test_autotune_picks_a_tried_candidate(ensemble):
     fastest = min(tried, key=lambda e: e["device_ms"])
     assert (best["rows_per_cta"], best["block"]) == (fastest["rows_per_cta"], fastest["block"])
     assert all(e["device_ms"] > 0 for e in tried)
+
+
+def test_batch_with_early_out_member_and_coulomb_gl_members():
+    """A member without grounded ice takes the early-out (zero velocities, not queued); the
+    Coulomb law with the grounding-line flux rows runs batched exactly as single solves."""
+    from conftest import oracle_aaac, oracle_inputs
+    api.init(0)
+    m1 = oracle_aaac("1k")
+    ssa_m, _, _ = oracle_inputs(m1, "marine")
+    ssa_d, _, _ = oracle_inputs(m1, "dome")
+    empty = dict(ssa_d, Hi=np.zeros_like(ssa_d["Hi"]), mask_sheet=np.zeros_like(ssa_d["mask_sheet"]))
+    p = api.default_params(precision=nat.UFE_MIXED, sliding_law=nat.UFE_SLIDING_COULOMB_REGULARISED,
+                           use_analytical_GL_flux=1)
+    members = [ssa_m, empty, ssa_m, ssa_d]
+    single = []
+    for f in members:
+        dm = api.DeviceMesh(m1)
+        single.append(dm.solve_ssa(f, p, check=False))
+        dm.close()
+    b = api.Batch([m1] * len(members), rows_per_cta=2048)
+    try:
+        for i, f in enumerate(members):
+            b.upload(i, f, p)
+        rc, stats, timing = b.run(p, check=False)
+        assert timing["n_active"] == len(members) - 1
+        outs = [b.download(i) for i in range(b.n)]
+        assert np.all(outs[1]["U_SSA"] == 0.0) and np.all(outs[1]["Ux_SSA_Ac"] == 0.0)
+        for i in (0, 2, 3):
+            rc1, o1, s1 = single[i]
+            assert stats[i]["sweeps"] == s1["sweeps"], i
+            for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac"):
+                assert rel_l2(outs[i][k], o1[k]) <= TOL, (i, k)
+    finally:
+        b.close()
