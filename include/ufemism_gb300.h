@@ -180,6 +180,11 @@ int ufe_ssa_upload(ufe_mesh_h mesh, const ufe_params *params, const ufe_ssa_in *
 int ufe_ssa_run(ufe_mesh_h mesh, const ufe_params *params, ufe_ssa_stats *stats);
 int ufe_ssa_download(ufe_mesh_h mesh, ufe_ssa_inout *inout, ufe_ssa_out *out);
 
+/* bottom_frictional_heating (thermodynamics_module.f90:281-311) from the last solve on this
+ * handle: on vertices with mask_sheet == 1, tau_c (U^2 + V^2) (delta_v^2 + U^2 + V^2)^((q-1)/2)
+ * / u_threshold^q with the solve's own U_SSA, V_SSA and tau_c_AaAc; 0 elsewhere. (nV) arrays. */
+int ufe_ssa_frictional_heating(ufe_mesh_h mesh, const int32_t *mask_sheet, double *frictional_heating);
+
 /* solve_SIA, ice_dynamics_module.f90:240-314 with map_Ac_to_Aa (mesh_ArakawaC_module.f90:770-791). */
 int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
                   ufe_sia_out *out);

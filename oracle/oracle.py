@@ -339,3 +339,12 @@ def thickness_change(m: AaAcMesh, A, Cw, Up_SIA_Ac, Up_SSA_Ac, SMB_year, BMB, dt
     if rc != OR_OK:
         raise RuntimeError("or_thickness_change failed: %d" % rc)
     return Hi_new, Hi_prev, dHi_dt, dVi_in
+
+
+def frictional_heating(mask_sheet, tau_c_AaAc, U, V):
+    """bottom_frictional_heating on the Aa vertices (U, V, mask_sheet of length nV)."""
+    nV = len(U)
+    out = np.zeros(nV)
+    keep = [_i32(mask_sheet), _f64(tau_c_AaAc), _f64(U), _f64(V)]
+    lib().or_frictional_heating(ct.c_int(nV), *(_vp(k) for k in keep), _vp(out))
+    return out

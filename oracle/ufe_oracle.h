@@ -189,6 +189,10 @@ int or_thickness_change(const or_base *b, const or_aaac *m, const double *A, con
                         const double *BMB, const int32_t *mask_noice, double dt, int zero_edges,
                         double *Hi, double *Hi_prev, double *dHi_dt, double *dVi_in);
 
+/* bottom_frictional_heating (thermodynamics_module.f90:281-311) on the Aa vertices. */
+void or_frictional_heating(int nV, const int32_t *mask_sheet, const double *tau_c_AaAc, const double *U,
+                           const double *V, double *heating);
+
 /* Primitive operators, for tests. */
 void or_map_Aa_to_Ac(const or_aaac *m, int nV, const double *d_Aa, double *d_Ac);
 void or_map_Ac_to_Aa(const or_base *b, const or_aaac *m, const double *d_Ac, double *d_Aa);

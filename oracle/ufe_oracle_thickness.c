@@ -6,8 +6,10 @@
  * (66-106), the outflux rescale against the available ice plus SMB/BMB (108-169, a
  * sequential loop over the vertices as the reference runs it on one rank), dHi/dt
  * (171-181), the zero-time-step rule (183-185), the thickness update (187-190), the domain-
- * edge rule (192-230) and the no-ice mask (232-236).
+ * edge rule (192-230) and the no-ice mask (232-236); and bottom_frictional_heating,
+ * thermodynamics_module.f90:281-311.
  */
+#include <math.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -83,4 +85,21 @@ int or_thickness_change(const or_base *b, const or_aaac *m, const double *A, con
       if (A1(mask_noice, vi) == 1) A1(Hi, vi) = 0.0;
   free(Vi_SMB);
   return OR_OK;
+}
+
+/* bottom_frictional_heating, thermodynamics_module.f90:281-311: on grounded-ice vertices,
+ * beta_base = tau_c * (delta_v^2 + U^2 + V^2)^(0.5 (q - 1)) / u_threshold^q and the heating
+ * beta_base * (U^2 + V^2); zero elsewhere. */
+void or_frictional_heating(int nV, const int32_t *mask_sheet, const double *tau_c_AaAc, const double *U,
+                           const double *V, double *heating) {
+  const double delta_v = 1e-3, q_plastic = 0.30, u_threshold = 100.0;
+  for (int vi = 1; vi <= nV; vi++) {
+    A1(heating, vi) = 0.0;
+    if (A1(mask_sheet, vi) == 1) {
+      const double u = A1(U, vi), v = A1(V, vi);
+      const double beta_base = (A1(tau_c_AaAc, vi) * pow((delta_v * delta_v + u * u) + v * v, 0.5 * (q_plastic - 1.0))) /
+                               pow(u_threshold, q_plastic);
+      A1(heating, vi) = beta_base * (u * u + v * v);
+    }
+  }
 }

@@ -144,3 +144,21 @@ def test_device_time_step_geometry_sia_ssa_thickness():
     assert np.array_equal(H_dev, ref[0])
     dm.close()
     dm2.close()
+
+
+def test_frictional_heating_matches_oracle():
+    """bottom_frictional_heating from the device solve's own U, V and tau_c against the
+    oracle's restatement applied to the downloaded fields (CUDA's pow vs the C library's:
+    1e-14 relative)."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, "marine")
+    p = api.default_params(sliding_law=nat.UFE_SLIDING_COULOMB_REGULARISED)
+    dm = api.DeviceMesh(m)
+    rc, o, st = dm.solve_ssa(ssa, p, check=False)
+    got = dm.frictional_heating(ssa["mask_sheet"])
+    nV = m.base.nV
+    ref = orc.frictional_heating(ssa["mask_sheet"], o["tau_c_AaAc"][:nV], o["U_SSA"], o["V_SSA"])
+    assert np.count_nonzero(ref) > 0
+    assert np.allclose(got, ref, rtol=1e-14, atol=0.0)
+    assert np.all(got[ssa["mask_sheet"] == 0] == 0.0)
+    dm.close()

@@ -177,6 +177,7 @@ PROTOTYPES = {
     "ufe_ssa_run": (I32, [P, ct.POINTER(Params), ct.POINTER(SsaStats)]),
     "ufe_ssa_download": (I32, [P, ct.POINTER(SsaInout), ct.POINTER(SsaOut)]),
     "ufe_sia_solve": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
+    "ufe_ssa_frictional_heating": (I32, [P, P, P]),
     "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_geometry_attach": (I32, [P, ct.POINTER(GeometryMesh)]),
     "ufe_geometry_update": (I32, [P, P, P, P, ct.POINTER(GeometryOut)]),

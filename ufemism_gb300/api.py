@@ -264,6 +264,16 @@ class DeviceMesh:
         return rc, out, dict(status=st.status, sweeps=st.sweeps, last_rel_update=st.last_rel_update,
                              device_ms=st.device_ms)
 
+    def frictional_heating(self, mask_sheet):
+        """bottom_frictional_heating from the last solve (ufe_ssa_frictional_heating)."""
+        L = nat.load()
+        m = np.ascontiguousarray(mask_sheet, dtype=np.int32)
+        out = np.zeros(self.nV)
+        rc = L.ufe_ssa_frictional_heating(self._h, m.ctypes.data, out.ctypes.data)
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_ssa_frictional_heating")
+        return out
+
     # ---------------------------------------------------------------- geometry on the device
     def geometry_attach(self, mesh):
         """Upload the Aa and Ac derivative stencils of ``mesh`` (ufe_geometry_attach)."""

@@ -1487,6 +1487,7 @@ struct SsaWork {
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   unsigned int *prog = nullptr;
+  double *fh = nullptr;          // frictional heating out (nV) + mask (nV ints), on first use
   SsaCtl *ctl = nullptr;
   SsaCtl *ctl_host = nullptr;    // pinned
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -1501,7 +1502,7 @@ struct SsaWork {
 void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
-                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl};
+                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -1879,6 +1880,50 @@ extern "C" int ufe_ssa_download(ufe_mesh_h h, ufe_ssa_inout *io, ufe_ssa_out *ou
     if (!rc) rc = d2h(out->phi_fric_AaAc, ab + 4 * nA, nA, s);
   }
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa download");
+  return rc;
+}
+
+namespace ufe {
+namespace {
+// bottom_frictional_heating (thermodynamics_module.f90:281-311) on the Aa vertices, from the
+// velocities and yield stress the last solve left in the staging buffer (caller order).
+__global__ void k_frictional_heating(int nV, const int *mask_sheet, const double *tau, const double *U,
+                                     const double *V, double *heating) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nV) return;
+  double h = 0.0;
+  if (mask_sheet[v] == 1) {
+    const double delta_v = 1e-3, q_plastic = 0.30, u_threshold = 100.0;
+    const double u = U[v], w = V[v];
+    const double beta_base = (tau[v] * pow((delta_v * delta_v + u * u) + w * w, 0.5 * (q_plastic - 1.0))) /
+                             pow(u_threshold, q_plastic);
+    h = beta_base * (u * u + w * w);
+  }
+  heating[v] = h;
+}
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_ssa_frictional_heating(ufe_mesh_h h, const int32_t *mask_sheet, double *heating) {
+  if (!h || !mask_sheet || !heating) { set_error("ufe_ssa_frictional_heating: null argument"); return UFE_BAD_ARG; }
+  SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) { set_error("ufe_ssa_frictional_heating: no solve on this handle"); return UFE_BAD_ARG; }
+  const size_t nV = w->nV, nAc = w->nAc, nA = w->nA;
+  cudaStream_t s = h->stream;
+  const double *so = w->stage_out;
+  const double *tau = so + 2 * nV + 4 * nAc + 3 * nA;
+  int rc = UFE_OK;
+  if (!w->fh) rc = cuda_status(cudaMalloc(&w->fh, nV * (sizeof(double) + sizeof(int))), "frictional heating");
+  if (rc) return rc;
+  double *out = w->fh;
+  int *mask = reinterpret_cast<int *>(w->fh + nV);
+  rc = cuda_status(cudaMemcpyAsync(mask, mask_sheet, nV * sizeof(int), cudaMemcpyHostToDevice, s), "mask H2D");
+  if (!rc) {
+    k_frictional_heating<<<(unsigned)((nV + 255) / 256), 256, 0, s>>>((int)nV, mask, tau, so, so + nV, out);
+    rc = cuda_status(cudaGetLastError(), "k_frictional_heating");
+  }
+  if (!rc) rc = d2h(heating, out, nV, s);
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "frictional heating");
   return rc;
 }
 
