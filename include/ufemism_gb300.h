@@ -237,6 +237,17 @@ int ufe_ssa_upload_geometry(ufe_mesh_h mesh, const ufe_params *params, const dou
  * from the host. */
 int ufe_sia_solve_geometry(ufe_mesh_h mesh, const ufe_params *params, const double *A_flow_Ac, ufe_sia_out *out);
 
+/* solve_SIA_3D (ice_dynamics_module.f90:317-405) on the device geometry of the last
+ * ufe_geometry_update / ufe_ssa_upload_geometry and the U_SSA, V_SSA of the last solve on the
+ * handle (zero without one): U_3D, V_3D = SIA deformation velocities plus the SSA basal ones on
+ * grounded vertices, Neumann rule on the domain edge, W_3D by vertical integration of the
+ * divergence. A_flow (nV,nZ), dHb_dt (nV) host arrays; outputs (nV,nZ), each may be NULL. */
+typedef struct ufe_sia3d_out {
+  double *U_3D, *V_3D, *W_3D;
+} ufe_sia3d_out;
+int ufe_sia3d_solve(ufe_mesh_h mesh, const ufe_params *params, const double *A_flow, const double *dHb_dt,
+                    ufe_sia3d_out *out);
+
 /* calculate_ice_thickness_change (ice_dynamics_module.f90:31-237) on the device: upwind ice
  * volume fluxes across every Aa connection from Up_SIA_Ac + Up_SSA_Ac, the outflux rescale
  * against the available ice plus SMB and BMB, dHi/dt, the update of Hi (in place), the

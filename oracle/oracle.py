@@ -27,7 +27,8 @@ ZETA_DEFAULT = np.array([0.00, 0.10, 0.20, 0.30, 0.40, 0.50, 0.60, 0.70, 0.80, 0
 def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB) or any(
             os.path.getmtime(os.path.join(_HERE, f)) > os.path.getmtime(_LIB)
-            for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle_thickness.c", "ufe_oracle.h")):
+            for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle_thickness.c", "ufe_oracle_sia3d.c",
+                      "ufe_oracle.h")):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
 
@@ -348,3 +349,22 @@ def frictional_heating(mask_sheet, tau_c_AaAc, U, V):
     keep = [_i32(mask_sheet), _f64(tau_c_AaAc), _f64(U), _f64(V)]
     lib().or_frictional_heating(ct.c_int(nV), *(_vp(k) for k in keep), _vp(out))
     return out
+
+
+def solve_sia_3d(m: AaAcMesh, g: dict, A_flow, dHb_dt, U_SSA, V_SSA, zeta=None, m_enh_sia=1.0):
+    """solve_SIA_3D with the geometry fields of update_geometry. Returns (U_3D, V_3D, W_3D),
+    each (nV, nZ)."""
+    base = m.base
+    nV = base.nV
+    z = np.ascontiguousarray(ZETA_DEFAULT if zeta is None else zeta, dtype=np.float64)
+    nZ = z.size
+    outs = [np.zeros((nV, nZ), order="F") for _ in range(3)]
+    keep = [_f64(g["Hi"]), _i32(g["mask_shelf"]), _i32(g["mask_sheet"]), _f64(g["dHs_dx"]), _f64(g["dHs_dy"]),
+            _f64(g["dHi_dx"]), _f64(g["dHi_dy"]), _f64(A_flow), _f64(dHb_dt), _f64(U_SSA), _f64(V_SSA)]
+    bs, bkeep = _base_struct(base)
+    ms = _aaac_struct(m)
+    rc = lib().or_solve_SIA_3D(ct.byref(bs), ct.byref(ms), _vp(z), ct.c_int(nZ), ct.c_double(m_enh_sia),
+                               *(_vp(k) for k in keep), *(_vp(o) for o in outs))
+    if rc != OR_OK:
+        raise RuntimeError("or_solve_SIA_3D failed: %d" % rc)
+    return tuple(outs)

@@ -189,6 +189,13 @@ int or_thickness_change(const or_base *b, const or_aaac *m, const double *A, con
                         const double *BMB, const int32_t *mask_noice, double dt, int zero_edges,
                         double *Hi, double *Hi_prev, double *dHi_dt, double *dVi_in);
 
+/* solve_SIA_3D (ice_dynamics_module.f90:317-405); A_flow and the outputs are (nV, nZ). */
+int or_solve_SIA_3D(const or_base *b, const or_aaac *m, const double *zeta, int nZ, double m_enh_sia,
+                    const double *Hi, const int32_t *mask_shelf, const int32_t *mask_sheet, const double *dHs_dx,
+                    const double *dHs_dy, const double *dHi_dx, const double *dHi_dy, const double *A_flow,
+                    const double *dHb_dt, const double *U_SSA, const double *V_SSA, double *U_3D, double *V_3D,
+                    double *W_3D);
+
 /* bottom_frictional_heating (thermodynamics_module.f90:281-311) on the Aa vertices. */
 void or_frictional_heating(int nV, const int32_t *mask_sheet, const double *tau_c_AaAc, const double *U,
                            const double *V, double *heating);

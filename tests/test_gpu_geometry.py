@@ -4,7 +4,7 @@ geometry identical to one fed by host-prepared fields."""
 import numpy as np
 import pytest
 
-from conftest import oracle_aaac, oracle_inputs
+from conftest import oracle_aaac, oracle_inputs, rel_l2
 
 import oracle as orc
 from ufemism_gb300 import _native as nat
@@ -161,4 +161,28 @@ def test_frictional_heating_matches_oracle():
     assert np.count_nonzero(ref) > 0
     assert np.allclose(got, ref, rtol=1e-14, atol=0.0)
     assert np.all(got[ssa["mask_sheet"] == 0] == 0.0)
+    dm.close()
+
+
+@pytest.mark.parametrize("kind", ["dome", "marine"])
+def test_sia3d_matches_oracle(kind):
+    """solve_SIA_3D on the device geometry and the device SSA solution against the oracle's
+    restatement fed with the same fields (CUDA's pow vs the C library's: 1e-12 relative)."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, kind)
+    nV = m.base.nV
+    rng = np.random.default_rng(4)
+    A3 = np.asfortranarray(np.full((nV, 15), 1e-16) * (1.0 + 0.5 * rng.uniform(size=(nV, 1))))
+    dHb_dt = rng.normal(size=nV) * 1e-3
+    p = api.default_params()
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    dm.ssa_upload_geometry(ssa["Hi"], ssa["Hb"], ssa["SL"], ssa["A_flow_mean"], ssa["A_flow_mean_Ac"], p)
+    dm.ssa_run(p, check=False)
+    o = dm.ssa_download()
+    U3, V3, W3 = dm.solve_sia_3d(A3, dHb_dt, p)
+    rU, rV, rW = orc.solve_sia_3d(m, g, A3, dHb_dt, o["U_SSA"], o["V_SSA"])
+    for a, b, name in ((U3, rU, "U"), (V3, rV, "V"), (W3, rW, "W")):
+        assert rel_l2(a, b) <= 1e-12, name
+    assert np.all(W3[m.base.edge_index == 0][g["mask_sheet"][m.base.edge_index == 0] == 0] == 0.0)
     dm.close()

@@ -94,6 +94,10 @@ class GeometryOut(ct.Structure):
     _fields_ = [(n, P) for n in GEOM_OUT_FIELDS]
 
 
+class Sia3dOut(ct.Structure):
+    _fields_ = [(n, P) for n in ("U_3D", "V_3D", "W_3D")]
+
+
 class ThicknessIn(ct.Structure):
     _fields_ = [(n, P) for n in ("A", "Cw", "Up_SIA_Ac", "Up_SSA_Ac", "SMB_year", "BMB", "mask_noice")] + \
                [("dt", F64), ("zero_edges", I32)]
@@ -183,6 +187,7 @@ PROTOTYPES = {
     "ufe_geometry_update": (I32, [P, P, P, P, ct.POINTER(GeometryOut)]),
     "ufe_ssa_upload_geometry": (I32, [P, ct.POINTER(Params), P, P, P, P, P, P, ct.POINTER(SsaInout)]),
     "ufe_sia_solve_geometry": (I32, [P, ct.POINTER(Params), P, ct.POINTER(SiaOut)]),
+    "ufe_sia3d_solve": (I32, [P, ct.POINTER(Params), P, P, ct.POINTER(Sia3dOut)]),
     "ufe_thickness_update": (I32, [P, ct.POINTER(ThicknessIn), P, ct.POINTER(ThicknessOut)]),
     "ufe_ssa_vjp": (I32, [P, ct.POINTER(Params), ct.POINTER(VjpParams), ct.POINTER(VjpIn), ct.POINTER(VjpGeom),
                           ct.POINTER(VjpOut), ct.POINTER(VjpStats)]),

@@ -333,6 +333,20 @@ class DeviceMesh:
             raise nat.UfeError(rc, "ufe_sia_solve_geometry")
         return out
 
+    def solve_sia_3d(self, A_flow, dHb_dt, params: dict):
+        """ufe_sia3d_solve: 3-D velocities on the device geometry. Returns (U_3D, V_3D, W_3D)."""
+        L = nat.load()
+        nZ = len(params["zeta"])
+        A = np.asfortranarray(A_flow, dtype=np.float64)
+        d = np.ascontiguousarray(dHb_dt, dtype=np.float64)
+        outs = [np.zeros((self.nV, nZ), order="F") for _ in range(3)]
+        so = nat.Sia3dOut(*(o.ctypes.data for o in outs))
+        ps, _z = _params_struct(params)
+        rc = L.ufe_sia3d_solve(self._h, ct.byref(ps), A.ctypes.data, d.ctypes.data, ct.byref(so))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_sia3d_solve")
+        return tuple(outs)
+
     def thickness_update(self, Hi, A, Cw, SMB_year, BMB, dt, Up_SIA_Ac=None, Up_SSA_Ac=None, mask_noice=None,
                          zero_edges=True):
         """calculate_ice_thickness_change on the device (ufe_thickness_update). Velocities left

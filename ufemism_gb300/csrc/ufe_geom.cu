@@ -29,12 +29,14 @@ struct GeomWork {
   double *beta = nullptr;      // (nV + nAc), allocated on first use
   double *thk = nullptr;       // thickness-update work, allocated on first use
   int *thk_int = nullptr;
+  double *sia3d = nullptr;     // 3-D SIA work (A_flow, dHb_dt, U, V, W), allocated on first use
+  int sia3d_nZ = 0;
   bool computed = false;
 };
 
 void geom_free(GeomWork *w) {
   if (!w) return;
-  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int};
+  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int, w->sia3d};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete w;
@@ -547,5 +549,199 @@ extern "C" int ufe_thickness_update(ufe_mesh_h h, const ufe_thickness_in *in, do
     dn(out->dVi_in, Cw, nV * ncm);
   }
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "thickness update");
+  return rc;
+}
+
+// ---------------------------------------------------------------------------------------
+// 3-D SIA velocities: solve_SIA_3D (ice_dynamics_module.f90:317-405) on the device geometry,
+// with apply_Neumann_boundary_3D (mesh_derivatives_module.f90:541-597) and the level
+// derivatives of get_mesh_derivatives_vertex_3D (372-391). Fields (nV, nZ) column-major.
+// ---------------------------------------------------------------------------------------
+namespace ufe {
+namespace {
+
+constexpr int kMaxZ3 = 64;
+
+struct Sia3dArgs {
+  int nV, nZ, ncm;
+  const int *nC, *C;
+  const double *Nx, *Ny;
+  const int *dev_of_orig;
+  const uint8_t *slice_g;
+  const double *Hi, *dHs_dx, *dHs_dy, *dHi_dx, *dHi_dy;
+  const int *mask_shelf, *mask_sheet;
+  const double *A, *dHb_dt, *U_SSA, *V_SSA;   // U_SSA/V_SSA may be null (no SSA solve: zero)
+  double m_enh;
+  double zeta[kMaxZ3], zeta3[kMaxZ3];
+  double *U3, *V3, *W3;
+};
+
+__device__ __forceinline__ bool aa_edge(const Sia3dArgs &a, int v) {
+  return a.slice_g[a.dev_of_orig[v] / kSlice] == 5;
+}
+
+__global__ void k_sia3d_uv(const Sia3dArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const size_t ld = a.nV;
+  const double us = a.U_SSA ? a.U_SSA[v] : 0.0, vs = a.V_SSA ? a.V_SSA[v] : 0.0;
+  const double h = a.Hi[v];
+  if (a.mask_shelf[v] == 1 || h == 0.0) {
+    for (int k = 0; k < a.nZ; ++k) { a.U3[v + k * ld] = us; a.V3[v + k * ld] = vs; }
+    return;
+  }
+  const double sx = a.dHs_dx[v], sy = a.dHs_dy[v];
+  const double D0 = pow((kIceDensity * kGrav) * h, 3.0) * pow(sx * sx + sy * sy, 1.0);
+  double dd[kMaxZ3];
+  const int nZ = a.nZ;
+  double f_hi = (a.m_enh * a.A[v + (size_t)(nZ - 1) * ld]) * a.zeta3[nZ - 1];
+  double acc = 0.0;
+  dd[nZ - 1] = 0.0;
+  for (int k = nZ - 2; k >= 0; --k) {
+    const double f_lo = (a.m_enh * a.A[v + (size_t)k * ld]) * a.zeta3[k];
+    acc = acc - (0.5 * (f_hi + f_lo)) * (a.zeta[k + 1] - a.zeta[k]);
+    dd[k] = acc;
+    f_hi = f_lo;
+  }
+  for (int k = 0; k < nZ; ++k) {
+    double D = D0 * ((2.0 * h) * dd[k]);
+    if (D < -1e5) D = -1e5;
+    a.U3[v + k * ld] = D * sx + us;
+    a.V3[v + k * ld] = D * sy + vs;
+  }
+}
+
+// Edge vertices (not the corners) from their non-edge neighbours, every level.
+__global__ void k_neumann3d_edges(const Sia3dArgs a, double *d) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < 4 || v >= a.nV || !aa_edge(a, v)) return;
+  const size_t ld = a.nV;
+  const int n = a.nC[v];
+  for (int k = 0; k < a.nZ; ++k) {
+    double s = 0.0;
+    int nvals = 0;
+    for (int c = 0; c < n; ++c) {
+      const int j = a.C[v + (size_t)c * ld] - 1;
+      if (aa_edge(a, j)) continue;
+      ++nvals;
+      s = s + d[j + k * ld];
+    }
+    if (nvals < a.ncm) s = s + 0.0;
+    d[v + k * ld] = s / (double)nvals;
+  }
+}
+
+// The four corners from all their neighbours (after the edges).
+__global__ void k_neumann3d_corners(const Sia3dArgs a, double *d) {
+  const int v = threadIdx.x;
+  if (v >= 4) return;
+  const size_t ld = a.nV;
+  const int n = a.nC[v];
+  for (int k = 0; k < a.nZ; ++k) {
+    double s = 0.0;
+    for (int c = 0; c < n; ++c) s = s + d[(a.C[v + (size_t)c * ld] - 1) + k * ld];
+    if (n < a.ncm) s = s + 0.0;
+    d[v + k * ld] = s / (double)n;
+  }
+}
+
+__device__ __forceinline__ void ddxy3(const Sia3dArgs &a, const double *d, int v, int k, double *dx, double *dy) {
+  const size_t ld = a.nV;
+  const int n = a.nC[v];
+  double x = a.Nx[v + (size_t)n * ld] * d[v + k * ld];
+  double y = a.Ny[v + (size_t)n * ld] * d[v + k * ld];
+  for (int c = 0; c < n; ++c) {
+    const int j = a.C[v + (size_t)c * ld] - 1;
+    x = x + a.Nx[v + (size_t)c * ld] * d[j + k * ld];
+    y = y + a.Ny[v + (size_t)c * ld] * d[j + k * ld];
+  }
+  *dx = x;
+  *dy = y;
+}
+
+__global__ void k_sia3d_w(const Sia3dArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const size_t ld = a.nV;
+  const int nZ = a.nZ;
+  for (int k = 0; k < nZ; ++k) a.W3[v + k * ld] = 0.0;
+  if (aa_edge(a, v) || a.mask_sheet[v] == 0) return;
+  const double bx = a.dHs_dx[v] - a.dHi_dx[v];
+  const double by = a.dHs_dy[v] - a.dHi_dy[v];
+  double w = (a.dHb_dt[v] + a.U3[v + (nZ - 1) * ld] * bx) + a.V3[v + (nZ - 1) * ld] * by;
+  a.W3[v + (nZ - 1) * ld] = w;
+  const double h = a.Hi[v];
+  const double mH = h > 0.1 ? h : 0.1;
+  for (int k = nZ - 2; k >= 0; --k) {
+    double ux0, uy0, ux1, uy1, vx0, vy0, vx1, vy1;
+    ddxy3(a, a.U3, v, k, &ux0, &uy0);
+    ddxy3(a, a.U3, v, k + 1, &ux1, &uy1);
+    ddxy3(a, a.V3, v, k, &vx0, &vy0);
+    ddxy3(a, a.V3, v, k + 1, &vx1, &vy1);
+    const double w1 = (ux0 + ux1) / 2.0;
+    const double w2 = (vy0 + vy1) / 2.0;
+    const double dz = a.zeta[k + 1] - a.zeta[k];
+    const double zm = 0.5 * (a.zeta[k + 1] + a.zeta[k]);
+    const double w3 = ((a.dHs_dx[v] - zm * a.dHi_dx[v]) / mH) * ((a.U3[v + (k + 1) * ld] - a.U3[v + k * ld]) / dz);
+    const double w4 = ((a.dHs_dy[v] - zm * a.dHi_dy[v]) / mH) * ((a.V3[v + (k + 1) * ld] - a.V3[v + k * ld]) / dz);
+    w = w - (h * (((w1 + w2) + w3) + w4)) * dz;
+    a.W3[v + k * ld] = w;
+  }
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_sia3d_solve(ufe_mesh_h h, const ufe_params *p, const double *A_flow, const double *dHb_dt,
+                               ufe_sia3d_out *out) {
+  if (!h || !p || !A_flow || !dHb_dt || !out || !p->zeta) { set_error("ufe_sia3d_solve: null argument"); return UFE_BAD_ARG; }
+  if (p->nZ < 2 || p->nZ > kMaxZ3) { set_error("ufe_sia3d_solve: nZ must be in [2, 64]"); return UFE_BAD_ARG; }
+  if (!h->geom || !h->geom->computed) {
+    set_error("ufe_sia3d_solve: no device geometry (ufe_geometry_update or ufe_ssa_upload_geometry first)");
+    return UFE_BAD_ARG;
+  }
+  GeomWork *g = h->geom;
+  const DevMesh &m = h->m;
+  GeomArgs ga = args_of(g);
+  const size_t nV = m.nV, nZ = p->nZ;
+  cudaStream_t s = h->stream;
+  if (g->sia3d_nZ != (int)nZ) {
+    if (g->sia3d) { cudaFree(g->sia3d); g->sia3d = nullptr; }
+    int rc = cuda_status(cudaMalloc(&g->sia3d, (4 * nV * nZ + nV) * sizeof(double)), "sia3d work");
+    if (rc) return rc;
+    g->sia3d_nZ = (int)nZ;
+  }
+  Sia3dArgs a;
+  a.nV = (int)nV; a.nZ = (int)nZ; a.ncm = m.ncm; a.nC = g->nC; a.C = g->C; a.Nx = g->Nx; a.Ny = g->Ny;
+  a.dev_of_orig = m.dev_of_orig; a.slice_g = m.slice_g;
+  a.Hi = AAF(ga, A_HI); a.dHs_dx = AAF(ga, A_DHS_DX); a.dHs_dy = AAF(ga, A_DHS_DY);
+  a.dHi_dx = AAF(ga, A_DHI_DX); a.dHi_dy = AAF(ga, A_DHI_DY);
+  a.mask_shelf = AAM(ga, M_SHELF); a.mask_sheet = AAM(ga, M_SHEET);
+  double *A = g->sia3d, *dhb = A + nV * nZ;
+  a.U3 = dhb + nV; a.V3 = a.U3 + nV * nZ; a.W3 = a.V3 + nV * nZ;
+  a.A = A; a.dHb_dt = dhb;
+  const double *uv = ssa_device_UV(h);
+  a.U_SSA = uv; a.V_SSA = uv ? uv + nV : nullptr;
+  a.m_enh = p->m_enh_sia;
+  for (size_t k = 0; k < nZ; ++k) { a.zeta[k] = p->zeta[k]; a.zeta3[k] = std::pow(p->zeta[k], 3.0); }
+  int rc = up(A, A_flow, nV * nZ, s);
+  if (!rc) rc = up(dhb, dHb_dt, nV, s);
+  const unsigned gv = (unsigned)((nV + 127) / 128);
+  if (!rc) { k_sia3d_uv<<<gv, 128, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_sia3d_uv"); }
+  for (double *d : {a.U3, a.V3}) {
+    if (!rc) { k_neumann3d_edges<<<gv, 128, 0, s>>>(a, d); rc = cuda_status(cudaGetLastError(), "k_neumann3d_edges"); }
+    if (!rc) { k_neumann3d_corners<<<1, 32, 0, s>>>(a, d); rc = cuda_status(cudaGetLastError(), "k_neumann3d_corners"); }
+  }
+  if (!rc) { k_sia3d_w<<<gv, 128, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_sia3d_w"); }
+  if (!rc) { k_neumann3d_edges<<<gv, 128, 0, s>>>(a, a.W3); rc = cuda_status(cudaGetLastError(), "k_neumann3d_edges"); }
+  if (!rc) { k_neumann3d_corners<<<1, 32, 0, s>>>(a, a.W3); rc = cuda_status(cudaGetLastError(), "k_neumann3d_corners"); }
+  auto dn = [&](double *dst, const double *src) {
+    if (!dst || rc) return;
+    rc = cuda_status(cudaMemcpyAsync(dst, src, nV * nZ * sizeof(double), cudaMemcpyDeviceToHost, s), "sia3d D2H");
+  };
+  dn(out->U_3D, a.U3);
+  dn(out->V_3D, a.V3);
+  dn(out->W_3D, a.W3);
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "sia3d solve");
   return rc;
 }

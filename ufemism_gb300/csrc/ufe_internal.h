@@ -129,6 +129,7 @@ void geom_free(GeomWork *w);
 int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out, bool fields_on_device);
 // Velocities of the last solves on a handle, on the device (caller order), or null.
 const double *ssa_device_Up(ufe_mesh_h h);
+const double *ssa_device_UV(ufe_mesh_h h);
 const double *sia_device_Up(ufe_mesh_h h);
 // ufe_ssa_upload from device arrays of this device (sheet_count: grounded-ice vertices).
 int ssa_upload_impl(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, const ufe_ssa_inout *io,

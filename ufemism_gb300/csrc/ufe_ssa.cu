@@ -1640,6 +1640,12 @@ int ssa_upload_impl(ufe_mesh_h h, const ufe_params *p, const ufe_ssa_in *in, con
 }  // namespace ufe
 
 namespace ufe {
+// U_SSA then V_SSA (nV each) of the last solve on this handle, on the device, or null.
+const double *ssa_device_UV(ufe_mesh_h h) {
+  const SsaWork *w = h->ssa;
+  if (!w || !w->uploaded) return nullptr;
+  return w->stage_out;
+}
 // Up_SSA_Ac of the last solve on this handle, on the device (caller order), or null.
 const double *ssa_device_Up(ufe_mesh_h h) {
   const SsaWork *w = h->ssa;
