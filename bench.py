@@ -537,6 +537,104 @@ def adjoint_bench(args):
     return 0
 
 
+def step_bench(args):
+    """One time step of the velocity path through the C-ABI, every input and output a host array:
+    device geometry preparation from Hi, Hb, SL (update_general_ice_model_data) and the SSA
+    upload -> SSA solve (mixed) -> SIA on the device geometry -> 3-D SIA -> frictional heating ->
+    thickness update from the velocities left on the device. Each call is timed on the host
+    (each returns after its device work); beside them the oracle's C restatements of the
+    non-SSA steps timed on one host thread (the cpu_baseline leg)."""
+    import torch
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api, workloads
+    from ufemism_gb300.meshgen import dome_mesh
+    size = args.size
+    base = dome_mesh(size)
+    mesh = api.build_aaac(base)
+    Hi, Hb, SL = workloads.dome_geometry(base)
+    ssa, sia = workloads.prepare_inputs(mesh, Hi, Hb, SL)
+    nV, nAc = base.nV, mesh.nAc
+    Aw, Cw = workloads.areas_and_widths(base)
+    A3 = np.full((nV, 15), workloads.A_FLOW, order="F")
+    dHb_dt = np.zeros(nV)
+    smb = np.full(nV, 0.3)
+    bmb = np.zeros(nV)
+    torch.cuda.set_device(0)
+    api.init(0)
+    dm = api.DeviceMesh(mesh)
+    dm.geometry_attach(mesh)
+    p = api.default_params(precision=nat.UFE_MIXED)
+    names = ("geometry+upload", "ssa_solve", "ssa_download", "sia", "sia_3d", "frictional_heating", "thickness")
+
+    def one_step():
+        t = {}
+        t0 = time.perf_counter()
+        dm.ssa_upload_geometry(Hi, Hb, SL, ssa["A_flow_mean"], ssa["A_flow_mean_Ac"], p)
+        t["geometry+upload"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rc, st = dm.ssa_run(p, check=False)
+        t["ssa_solve"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        dm.ssa_download()
+        t["ssa_download"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        dm.solve_sia_geometry(sia["A_flow_Ac"], p)
+        t["sia"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        dm.solve_sia_3d(A3, dHb_dt, p)
+        t["sia_3d"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        dm.frictional_heating(ssa["mask_sheet"])
+        t["frictional_heating"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        dm.thickness_update(Hi, Aw, Cw, smb, bmb, 10.0)
+        t["thickness"] = time.perf_counter() - t0
+        return t, st
+
+    for _ in range(args.warmup):
+        one_step()
+    rows = []
+    for _ in range(args.steps):
+        t, st = one_step()
+        rows.append(t)
+    gpu_ms = {k: 1e3 * float(np.median([r[k] for r in rows])) for k in names}
+    line = {
+        "metric": "velocity time step through the C-ABI (ms)", "value": sum(gpu_ms.values()), "unit": "ms",
+        "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "dtype": "f64 (SSA mixed)", "data": "synthetic (seeded dome geometry and mesh)",
+        "config": {"workload": "%s-vertex dome, one velocity and thickness step" % size, "nV": int(nV),
+                   "nAc": int(nAc), "ssa_sweeps": st["total_sweeps"]},
+        "components_ms": gpu_ms,
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+        om = orc.build_aaac(base)
+        cpu = {}
+        t0 = time.perf_counter(); g = orc.update_geometry(om, Hi, Hb, SL); cpu["geometry"] = time.perf_counter() - t0
+        sia_o = dict(sia)
+        t0 = time.perf_counter(); so = orc.solve_sia(om, sia_o, orc.default_params()); cpu["sia"] = time.perf_counter() - t0
+        o = dm.ssa_download()
+        t0 = time.perf_counter()
+        orc.solve_sia_3d(om, g, A3, dHb_dt, o["U_SSA"], o["V_SSA"])
+        cpu["sia_3d"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.frictional_heating(ssa["mask_sheet"], o["tau_c_AaAc"][:nV], o["U_SSA"], o["V_SSA"])
+        cpu["frictional_heating"] = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.thickness_change(om, Aw, Cw, so["Up_SIA_Ac"], o["Up_SSA_Ac"], smb, bmb, 10.0, Hi)
+        cpu["thickness"] = time.perf_counter() - t0
+        cpu_ms = {k: 1e3 * v for k, v in cpu.items()}
+        line["cpu_baseline"] = {"components_ms": cpu_ms, "cores": 1, "kind": "port",
+                                "sample": "the oracle's C restatements of the non-SSA steps, one call each"}
+        gpu_cmp = {"geometry": gpu_ms["geometry+upload"], "sia": gpu_ms["sia"], "sia_3d": gpu_ms["sia_3d"],
+                   "frictional_heating": gpu_ms["frictional_heating"], "thickness": gpu_ms["thickness"]}
+        line["speedup_vs_cpu"] = {k: cpu_ms[k] / gpu_cmp[k] for k in cpu_ms}
+    print(json.dumps(line))
+    dm.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--profile-case", choices=["mixed", "fp64", "exact"], default=None,
@@ -552,7 +650,7 @@ def main():
     ap.add_argument("--adj-rn-tol", type=float, default=1e-10, help="adjoint: forward Picard tolerance")
     ap.add_argument("--adj-tol", type=float, default=1e-12, help="adjoint: VJP relative residual tolerance")
     ap.add_argument("--fd-directions", type=int, default=2)
-    ap.add_argument("--workload", default="dome", choices=["dome", "ensemble", "marine", "adjoint"],
+    ap.add_argument("--workload", default="dome", choices=["dome", "ensemble", "marine", "adjoint", "step"],
                     help="dome: the 200k-vertex single solve; ensemble: the batched ensemble")
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--autotune", action="store_true", help="ensemble: run the autotuner first")
@@ -567,6 +665,8 @@ def main():
         return ensemble_bench(args)
     if args.workload == "marine":
         return marine_bench(args)
+    if args.workload == "step":
+        return step_bench(args)
     if args.workload == "adjoint":
         return adjoint_bench(args)
 

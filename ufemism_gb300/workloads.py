@@ -168,20 +168,27 @@ def areas_and_widths(base):
     for k in range(3):
         np.add.at(A, T[:, k], area / 3.0)
     cen = (p0 + p1 + p2) / 3.0
-    edges = {}
-    for t in range(T.shape[0]):
-        for a, b in ((0, 1), (1, 2), (2, 0)):
-            key = (min(T[t, a], T[t, b]), max(T[t, a], T[t, b]))
-            edges.setdefault(key, []).append(t)
+    nV = base.nV
+    # every triangle side as a sorted vertex pair key, with its triangle
+    ea = np.concatenate([T[:, 0], T[:, 1], T[:, 2]])
+    eb = np.concatenate([T[:, 1], T[:, 2], T[:, 0]])
+    key = np.minimum(ea, eb) * nV + np.maximum(ea, eb)
+    tri = np.tile(np.arange(T.shape[0]), 3)
+    order = np.argsort(key, kind="stable")
+    key, tri = key[order], tri[order]
     C = np.asarray(base.C, dtype=np.int64) - 1
     nC = np.asarray(base.nC, dtype=np.int64)
     Cw = np.zeros(C.shape, order="F")
-    for v in range(base.nV):
-        for c in range(nC[v]):
-            j = C[v, c]
-            ts = edges[(min(v, j), max(v, j))]
-            if len(ts) == 2:
-                Cw[v, c] = np.linalg.norm(cen[ts[0]] - cen[ts[1]])
-            else:
-                Cw[v, c] = np.linalg.norm(cen[ts[0]] - 0.5 * (V[v] + V[j]))
+    slot = np.arange(C.shape[1])[None, :]
+    valid = slot < nC[:, None]
+    vv = np.repeat(np.arange(nV), C.shape[1]).reshape(C.shape)[valid]
+    jj = C[valid]
+    k = np.minimum(vv, jj) * nV + np.maximum(vv, jj)
+    i0 = np.searchsorted(key, k, side="left")
+    i1 = np.searchsorted(key, k, side="right")
+    t0 = tri[i0]
+    two = (i1 - i0) == 2
+    t1 = np.where(two, tri[np.minimum(i0 + 1, key.size - 1)], t0)
+    far = np.where(two[:, None], cen[t1], 0.5 * (V[vv] + V[jj]))
+    Cw[valid] = np.linalg.norm(cen[t0] - far, axis=1)
     return A, Cw
