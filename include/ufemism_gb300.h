@@ -248,6 +248,30 @@ typedef struct ufe_sia3d_out {
 int ufe_sia3d_solve(ufe_mesh_h mesh, const ufe_params *params, const double *A_flow, const double *dHb_dt,
                     ufe_sia3d_out *out);
 
+/* ice_physical_properties (general_ice_model_data_module.f90:298-462) on the device, the last
+ * step of update_general_ice_model_data: from the ice temperature Ti (nV,nZ) and the Hi,
+ * mask_sheet, mask_sheet_Ac of the last ufe_geometry_update / ufe_ssa_upload_geometry.
+ *   UFE_FLOW_ARRHENIUS: Ti_Ac = map_Aa_to_Ac_3D(Ti); Ti_pmp, A_flow (Arrhenius law, two
+ *     branches at 263.15 K), Cpi, Ki on Aa; A_flow_Ac on Ac; A_flow_mean(_Ac) = the vertical
+ *     average under grounded ice, else the Arrhenius law at (Ti(:,1) + SMT) / 2.
+ *   UFE_FLOW_EISMINT (the EISMINT_1..6, Halfar, Bueler, mesh_generation_test benchmarks):
+ *     A = 1e-16 everywhere, Ki = 2.1 sec_per_year, Cpi = 2009, Ti_pmp from Hi; Ti not read,
+ *     Ti_Ac not written.
+ *   UFE_FLOW_MISMIP_MOD: A = 1e-16, 1e-17 or 1e-16 for time < 25,000, < 50,000, < 75,000
+ *     years, else 1e-16; only the four A fields are written.
+ * The results stay on the device: ufe_ssa_upload_geometry with both A_flow_mean arrays NULL,
+ * ufe_sia_solve_geometry with A_flow_Ac NULL and ufe_sia3d_solve with A_flow NULL take them
+ * from there. Each output host array may be NULL. */
+enum { UFE_FLOW_ARRHENIUS = 0, UFE_FLOW_EISMINT = 1, UFE_FLOW_MISMIP_MOD = 2 };
+typedef struct ufe_physprop_out {
+  double *A_flow, *Ti_pmp, *Cpi, *Ki;   /* (nV,nZ) */
+  double *A_flow_mean;                  /* (nV) */
+  double *A_flow_Ac, *Ti_Ac;            /* (nAc,nZ) */
+  double *A_flow_mean_Ac;               /* (nAc) */
+} ufe_physprop_out;
+int ufe_ice_physical_properties(ufe_mesh_h mesh, const ufe_params *params, int flow_law, double time,
+                                const double *Ti, ufe_physprop_out *out);
+
 /* calculate_ice_thickness_change (ice_dynamics_module.f90:31-237) on the device: upwind ice
  * volume fluxes across every Aa connection from Up_SIA_Ac + Up_SSA_Ac, the outflux rescale
  * against the available ice plus SMB and BMB, dHi/dt, the update of Hi (in place), the

@@ -28,7 +28,7 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB) or any(
             os.path.getmtime(os.path.join(_HERE, f)) > os.path.getmtime(_LIB)
             for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle_thickness.c", "ufe_oracle_sia3d.c",
-                      "ufe_oracle.h")):
+                      "ufe_oracle_physprop.c", "ufe_oracle.h")):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
 
@@ -368,3 +368,24 @@ def solve_sia_3d(m: AaAcMesh, g: dict, A_flow, dHb_dt, U_SSA, V_SSA, zeta=None, 
     if rc != OR_OK:
         raise RuntimeError("or_solve_SIA_3D failed: %d" % rc)
     return tuple(outs)
+
+
+def ice_physical_properties(m: AaAcMesh, Hi, mask_sheet, mask_sheet_Ac, Ti=None, flow_law=0, time=0.0, zeta=None):
+    """ice_physical_properties (flow_law 0: Arrhenius from Ti, 1: EISMINT-type constants,
+    2: MISMIP_mod). Returns a dict of A_flow, Ti_pmp, Cpi, Ki (nV, nZ), A_flow_mean (nV),
+    A_flow_Ac, Ti_Ac (nAc, nZ), A_flow_mean_Ac (nAc); the fields a law does not write stay NaN."""
+    nV, nAc = m.base.nV, m.nAc
+    z = np.ascontiguousarray(ZETA_DEFAULT if zeta is None else zeta, dtype=np.float64)
+    nZ = z.size
+    out = {k: np.full((nV, nZ), np.nan, order="F") for k in ("A_flow", "Ti_pmp", "Cpi", "Ki")}
+    out.update(A_flow_Ac=np.full((nAc, nZ), np.nan, order="F"), Ti_Ac=np.full((nAc, nZ), np.nan, order="F"),
+               A_flow_mean=np.full(nV, np.nan), A_flow_mean_Ac=np.full(nAc, np.nan))
+    keep = [_f64(Hi), _i32(mask_sheet), _i32(mask_sheet_Ac), None if Ti is None else _f64(Ti), _i32(m.Aci)]
+    rc = lib().or_ice_physical_properties(
+        ct.c_int(nV), ct.c_int(nAc), ct.c_int(nZ), _vp(z), _vp(keep[4]), ct.c_int(flow_law), ct.c_double(time),
+        _vp(keep[0]), _vp(keep[1]), _vp(keep[2]), None if keep[3] is None else _vp(keep[3]),
+        *(_vp(out[k]) for k in ("A_flow", "A_flow_Ac", "A_flow_mean", "A_flow_mean_Ac", "Ti_pmp", "Cpi", "Ki",
+                                "Ti_Ac")))
+    if rc != OR_OK:
+        raise RuntimeError("or_ice_physical_properties failed: %d" % rc)
+    return out

@@ -200,6 +200,16 @@ int or_solve_SIA_3D(const or_base *b, const or_aaac *m, const double *zeta, int 
 void or_frictional_heating(int nV, const int32_t *mask_sheet, const double *tau_c_AaAc, const double *U,
                            const double *V, double *heating);
 
+/* ice_physical_properties (general_ice_model_data_module.f90:298-462). flow_law 0: the
+ * Arrhenius law from Ti (nV, nZ), Ti_Ac = map_Aa_to_Ac_3D(Ti); 1: the EISMINT-type benchmarks
+ * (constant A, Ki, Cpi; Ti not read); 2: MISMIP_mod (A from the time; only the A fields
+ * written). 2-D arrays are (nV, nZ) and (nAc, nZ), column-major. */
+int or_ice_physical_properties(int nV, int nAc, int nZ, const double *zeta, const int32_t *Aci, int flow_law,
+                               double time, const double *Hi, const int32_t *mask_sheet,
+                               const int32_t *mask_sheet_Ac, const double *Ti, double *A_flow, double *A_flow_Ac,
+                               double *A_flow_mean, double *A_flow_mean_Ac, double *Ti_pmp, double *Cpi, double *Ki,
+                               double *Ti_Ac);
+
 /* Primitive operators, for tests. */
 void or_map_Aa_to_Ac(const or_aaac *m, int nV, const double *d_Aa, double *d_Ac);
 void or_map_Ac_to_Aa(const or_base *b, const or_aaac *m, const double *d_Ac, double *d_Aa);

@@ -186,3 +186,68 @@ def test_sia3d_matches_oracle(kind):
         assert rel_l2(a, b) <= 1e-12, name
     assert np.all(W3[m.base.edge_index == 0][g["mask_sheet"][m.base.edge_index == 0] == 0] == 0.0)
     dm.close()
+
+
+@pytest.mark.parametrize("law", [nat.UFE_FLOW_ARRHENIUS, nat.UFE_FLOW_EISMINT, nat.UFE_FLOW_MISMIP_MOD])
+def test_physical_properties_match_oracle(law):
+    """ice_physical_properties on the device against the oracle: the fields without a
+    transcendental function bit-identical, the rest within CUDA's exp against the C library's."""
+    m = oracle_aaac("1k")
+    Hi, Hb, SL = wl.marine_geometry(m.base, seed=20261206)
+    g = orc.update_geometry(m, Hi, Hb, SL)
+    rng = np.random.default_rng(12)
+    Ti = np.asfortranarray(240.0 + 30.0 * rng.random((m.base.nV, 15)))
+    T = Ti if law == nat.UFE_FLOW_ARRHENIUS else None
+    p = api.default_params()
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    dm.geometry_update(Hi, Hb, SL)
+    got = dm.ice_physical_properties(p, T, flow_law=law, time=30000.0)
+    ref = orc.ice_physical_properties(m, Hi, g["mask_sheet"], g["mask_sheet_Ac"], T, flow_law=law, time=30000.0)
+    assert set(got) == {k for k, v in ref.items() if not np.all(np.isnan(v))}
+    for k, v in got.items():
+        if k in ("Ti_Ac", "Ti_pmp", "Cpi") or law != nat.UFE_FLOW_ARRHENIUS:
+            assert np.array_equal(v, ref[k]), k
+        else:
+            assert np.allclose(v, ref[k], rtol=1e-14, atol=0.0), k
+    dm.close()
+
+
+def test_physical_properties_feed_the_solves():
+    """SSA, SIA and 3-D SIA fed by the flow factors left on the device equal the same solves
+    fed by those values from the host; before any physical properties the NULL forms fail."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, "dome")
+    Hi, Hb, SL = ssa["Hi"], ssa["Hb"], ssa["SL"]
+    nV = m.base.nV
+    rng = np.random.default_rng(13)
+    Ti = np.asfortranarray(250.0 + 15.0 * rng.random((nV, 15)))
+    dHb_dt = rng.normal(size=nV) * 1e-3
+    p = api.default_params(precision=nat.UFE_FP64)
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    dm.geometry_update(Hi, Hb, SL)
+    with pytest.raises(nat.UfeError):
+        dm.ssa_upload_geometry(Hi, Hb, SL, None, None, p)
+    with pytest.raises(nat.UfeError):
+        dm.solve_sia_3d(None, dHb_dt, p)
+    props = dm.ice_physical_properties(p, Ti)
+    runs = []
+    for A in (None, props):
+        dm.ssa_upload_geometry(Hi, Hb, SL, None if A is None else A["A_flow_mean"],
+                               None if A is None else A["A_flow_mean_Ac"], p)
+        rc, st = dm.ssa_run(p, check=False)
+        o = dm.ssa_download()
+        s = dm.solve_sia_geometry(None if A is None else A["A_flow_Ac"], p)
+        u = dm.solve_sia_3d(None if A is None else A["A_flow"], dHb_dt, p)
+        runs.append((rc, st["sweeps"], o, s, u))
+    (rc1, sw1, o1, s1, u1), (rc2, sw2, o2, s2, u2) = runs
+    assert rc1 == rc2 and sw1 == sw2
+    for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac"):
+        assert np.array_equal(o1[k], o2[k]), k
+    for k in ("Ux_SIA_Ac", "Uy_SIA_Ac", "D_SIA_3D_Ac", "U_SIA"):
+        assert np.array_equal(s1[k], s2[k]), k
+    for a, b in zip(u1, u2):
+        assert np.array_equal(a, b)
+    assert np.count_nonzero(o1["U_SSA"]) > 0
+    dm.close()

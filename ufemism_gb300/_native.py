@@ -98,6 +98,14 @@ class Sia3dOut(ct.Structure):
     _fields_ = [(n, P) for n in ("U_3D", "V_3D", "W_3D")]
 
 
+UFE_FLOW_ARRHENIUS, UFE_FLOW_EISMINT, UFE_FLOW_MISMIP_MOD = 0, 1, 2
+PHYSPROP_OUT_FIELDS = ("A_flow", "Ti_pmp", "Cpi", "Ki", "A_flow_mean", "A_flow_Ac", "Ti_Ac", "A_flow_mean_Ac")
+
+
+class PhyspropOut(ct.Structure):
+    _fields_ = [(n, P) for n in PHYSPROP_OUT_FIELDS]
+
+
 class ThicknessIn(ct.Structure):
     _fields_ = [(n, P) for n in ("A", "Cw", "Up_SIA_Ac", "Up_SSA_Ac", "SMB_year", "BMB", "mask_noice")] + \
                [("dt", F64), ("zero_edges", I32)]
@@ -188,6 +196,7 @@ PROTOTYPES = {
     "ufe_ssa_upload_geometry": (I32, [P, ct.POINTER(Params), P, P, P, P, P, P, ct.POINTER(SsaInout)]),
     "ufe_sia_solve_geometry": (I32, [P, ct.POINTER(Params), P, ct.POINTER(SiaOut)]),
     "ufe_sia3d_solve": (I32, [P, ct.POINTER(Params), P, P, ct.POINTER(Sia3dOut)]),
+    "ufe_ice_physical_properties": (I32, [P, ct.POINTER(Params), I32, ct.c_double, P, ct.POINTER(PhyspropOut)]),
     "ufe_thickness_update": (I32, [P, ct.POINTER(ThicknessIn), P, ct.POINTER(ThicknessOut)]),
     "ufe_ssa_vjp": (I32, [P, ct.POINTER(Params), ct.POINTER(VjpParams), ct.POINTER(VjpIn), ct.POINTER(VjpGeom),
                           ct.POINTER(VjpOut), ct.POINTER(VjpStats)]),

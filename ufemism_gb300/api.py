@@ -305,21 +305,25 @@ class DeviceMesh:
 
     def ssa_upload_geometry(self, Hi, Hb, SL, A_flow_mean, A_flow_mean_Ac, params: dict, beta=None,
                             warm: dict | None = None):
-        """ufe_ssa_upload_geometry: the solve's inputs derived on the device from Hi, Hb, SL."""
+        """ufe_ssa_upload_geometry: the solve's inputs derived on the device from Hi, Hb, SL.
+        A_flow_mean and A_flow_mean_Ac both None: the flow factors already on the device
+        (ice_physical_properties)."""
         L = nat.load()
         _, sio, io, _ = self._ssa_structs({}, warm)
-        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (Hi, Hb, SL, A_flow_mean, A_flow_mean_Ac)]
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+                for a in (Hi, Hb, SL, A_flow_mean, A_flow_mean_Ac)]
         b = None if beta is None else np.ascontiguousarray(beta, dtype=np.float64)
         ps, _z = _params_struct(params)
-        rc = L.ufe_ssa_upload_geometry(self._h, ct.byref(ps), *(a.ctypes.data for a in arrs), _ptr(b), ct.byref(sio))
+        rc = L.ufe_ssa_upload_geometry(self._h, ct.byref(ps), *(_ptr(a) for a in arrs), _ptr(b), ct.byref(sio))
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_ssa_upload_geometry")
 
     def solve_sia_geometry(self, A_flow_Ac, params: dict):
-        """ufe_sia_solve_geometry: the SIA on the device geometry of the last geometry update."""
+        """ufe_sia_solve_geometry: the SIA on the device geometry of the last geometry update
+        (A_flow_Ac None: the device's from ice_physical_properties)."""
         L = nat.load()
         nZ = len(params["zeta"])
-        A = np.asfortranarray(A_flow_Ac, dtype=np.float64)
+        A = None if A_flow_Ac is None else np.asfortranarray(A_flow_Ac, dtype=np.float64)
         out = dict(D_SIA_3D_Ac=np.zeros((self.nAc, nZ), order="F"))
         for k in ("D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac", "Uo_SIA_Ac"):
             out[k] = np.zeros(self.nAc)
@@ -328,24 +332,51 @@ class DeviceMesh:
         so = nat.SiaOut(*(_ptr(out[k]) for k in ("D_SIA_3D_Ac", "D_SIA_Ac", "Ux_SIA_Ac", "Uy_SIA_Ac", "Up_SIA_Ac",
                                                   "Uo_SIA_Ac", "U_SIA", "V_SIA", "D_SIA")))
         ps, _z = _params_struct(params)
-        rc = L.ufe_sia_solve_geometry(self._h, ct.byref(ps), A.ctypes.data, ct.byref(so))
+        rc = L.ufe_sia_solve_geometry(self._h, ct.byref(ps), _ptr(A), ct.byref(so))
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_sia_solve_geometry")
         return out
 
     def solve_sia_3d(self, A_flow, dHb_dt, params: dict):
-        """ufe_sia3d_solve: 3-D velocities on the device geometry. Returns (U_3D, V_3D, W_3D)."""
+        """ufe_sia3d_solve: 3-D velocities on the device geometry (A_flow None: the device's
+        from ice_physical_properties). Returns (U_3D, V_3D, W_3D)."""
         L = nat.load()
         nZ = len(params["zeta"])
-        A = np.asfortranarray(A_flow, dtype=np.float64)
+        A = None if A_flow is None else np.asfortranarray(A_flow, dtype=np.float64)
         d = np.ascontiguousarray(dHb_dt, dtype=np.float64)
         outs = [np.zeros((self.nV, nZ), order="F") for _ in range(3)]
         so = nat.Sia3dOut(*(o.ctypes.data for o in outs))
         ps, _z = _params_struct(params)
-        rc = L.ufe_sia3d_solve(self._h, ct.byref(ps), A.ctypes.data, d.ctypes.data, ct.byref(so))
+        rc = L.ufe_sia3d_solve(self._h, ct.byref(ps), _ptr(A), d.ctypes.data, ct.byref(so))
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_sia3d_solve")
         return tuple(outs)
+
+    def ice_physical_properties(self, params: dict, Ti=None, flow_law: int = nat.UFE_FLOW_ARRHENIUS,
+                                time: float = 0.0) -> dict:
+        """ufe_ice_physical_properties on the device geometry of the last geometry update. Returns
+        the fields the law writes: A_flow, Ti_pmp, Cpi, Ki (nV, nZ), A_flow_mean (nV), A_flow_Ac,
+        Ti_Ac (nAc, nZ), A_flow_mean_Ac (nAc)."""
+        L = nat.load()
+        nZ = len(params["zeta"])
+        shapes = dict(A_flow=(self.nV, nZ), Ti_pmp=(self.nV, nZ), Cpi=(self.nV, nZ), Ki=(self.nV, nZ),
+                      A_flow_mean=(self.nV,), A_flow_Ac=(self.nAc, nZ), Ti_Ac=(self.nAc, nZ),
+                      A_flow_mean_Ac=(self.nAc,))
+        keys = ["A_flow", "A_flow_mean", "A_flow_Ac", "A_flow_mean_Ac"]
+        if flow_law != nat.UFE_FLOW_MISMIP_MOD:
+            keys += ["Ti_pmp", "Cpi", "Ki"]
+        if flow_law == nat.UFE_FLOW_ARRHENIUS:
+            keys.append("Ti_Ac")
+        out = {k: np.zeros(shapes[k], order="F") for k in keys}
+        po = nat.PhyspropOut(*(_ptr(out.get(k)) for k in nat.PHYSPROP_OUT_FIELDS))
+        T = None if Ti is None else np.asfortranarray(Ti, dtype=np.float64)
+        if T is not None and T.shape != (self.nV, nZ):
+            raise ValueError("Ti must be (nV, nZ)")
+        ps, _z = _params_struct(params)
+        rc = L.ufe_ice_physical_properties(self._h, ct.byref(ps), int(flow_law), float(time), _ptr(T), ct.byref(po))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_ice_physical_properties")
+        return out
 
     def thickness_update(self, Hi, A, Cw, SMB_year, BMB, dt, Up_SIA_Ac=None, Up_SSA_Ac=None, mask_noice=None,
                          zero_edges=True):

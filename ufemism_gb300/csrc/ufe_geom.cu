@@ -31,12 +31,17 @@ struct GeomWork {
   int *thk_int = nullptr;
   double *sia3d = nullptr;     // 3-D SIA work (A_flow, dHb_dt, U, V, W), allocated on first use
   int sia3d_nZ = 0;
+  // ice physical properties: Ti, A_flow, Ti_pmp, Cpi, Ki (nV x nZ each), A_flow_Ac, Ti_Ac (nAc x nZ each)
+  double *props = nullptr;
+  int props_nZ = 0;
+  int props_law = -1;          // flow law of the last ufe_ice_physical_properties, -1: none
+  bool af_set = false;         // A_flow_mean(_Ac) present on the device (physical properties or an upload)
   bool computed = false;
 };
 
 void geom_free(GeomWork *w) {
   if (!w) return;
-  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int, w->sia3d};
+  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int, w->sia3d, w->props};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete w;
@@ -204,10 +209,161 @@ int compute(ufe_mesh_h h, const double *Hi, const double *Hb, const double *SL) 
   return rc;
 }
 
+// ---------------------------------------------------------------------------------------
+// ice_physical_properties (general_ice_model_data_module.f90:298-462): the flow factor, the
+// pressure-melting point, the specific heat and the conductivity of the ice, one thread per
+// Aa vertex and one per Ac edge, each walking its nZ layers (column-major, so every layer is
+// a coalesced row across the warp). Constants from parameters_module.f90:10-21 and the
+// routine's own Arrhenius constants (318-322).
+// ---------------------------------------------------------------------------------------
+constexpr int kMaxZP = 64;
+constexpr double kT0 = 273.16, kCC = 8.7E-04, kSMT = 271.15, kSecPerYear = 31556943.36;
+constexpr double kALow = 1.14E-05, kAHigh = 5.47E+10, kQLow = 6.0E+04, kQHigh = 13.9E+04, kRGas = 8.314;
+
+struct PropArgs {
+  int nV, nAc, nZ, law;
+  double A_const;                     // the benchmark laws' flow factor
+  const int *Aci;                     // (nAc, 4), 1-based
+  const double *Hi;                   // (nV)
+  const int *mask_sheet, *mask_sheet_Ac;
+  const double *Ti;                   // (nV, nZ)
+  double *A_flow, *Ti_pmp, *Cpi, *Ki, *A_mean;   // Aa
+  double *A_flow_Ac, *Ti_Ac, *A_mean_Ac;         // Ac
+  double zeta[kMaxZP];
+};
+
+__device__ __forceinline__ double arrhenius(double T) {
+  return T < 263.15 ? kALow * exp(-kQLow / (kRGas * T)) : kAHigh * exp(-kQHigh / (kRGas * T));
+}
+
+__global__ void k_physprop_aa(const PropArgs a) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const size_t n = a.nV;
+  const double H = a.Hi[v];
+  if (a.law != UFE_FLOW_ARRHENIUS) {
+    for (int k = 0; k < a.nZ; ++k) a.A_flow[v + k * n] = a.A_const;
+    a.A_mean[v] = a.A_const;
+    if (a.law == UFE_FLOW_EISMINT)
+      for (int k = 0; k < a.nZ; ++k) {
+        a.Ki[v + k * n] = 2.1 * kSecPerYear;
+        a.Cpi[v + k * n] = 2009.0;
+        a.Ti_pmp[v + k * n] = kT0 - (a.zeta[k] * H * 8.7E-04);
+      }
+    return;
+  }
+  // the vertical average (zeta_module.f90:33-57) accumulates layer by layer, base upwards
+  double avg = 0.0, below = 0.0;
+  for (int k = 0; k < a.nZ; ++k) {
+    const double T = a.Ti[v + k * n];
+    a.Ti_pmp[v + k * n] = kT0 - kCC * H * a.zeta[k];
+    const double A = arrhenius(T);
+    a.A_flow[v + k * n] = A;
+    a.Cpi[v + k * n] = 2115.3 + 7.79293 * (T - kT0);
+    a.Ki[v + k * n] = 3.101E+08 * exp(-0.0057 * T);
+    if (k > 0) avg = avg + 0.5 * (A + below) * (a.zeta[k] - a.zeta[k - 1]);
+    below = A;
+  }
+  a.A_mean[v] = a.mask_sheet[v] == 1 ? avg : arrhenius((a.Ti[v] + kSMT) / 2.0);
+}
+
+__global__ void k_physprop_ac(const PropArgs a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nAc) return;
+  const size_t n = a.nAc, nv = a.nV;
+  if (a.law != UFE_FLOW_ARRHENIUS) {
+    for (int k = 0; k < a.nZ; ++k) a.A_flow_Ac[c + k * n] = a.A_const;
+    a.A_mean_Ac[c] = a.A_const;
+    return;
+  }
+  const int vi = a.Aci[c] - 1, vj = a.Aci[c + n] - 1;
+  double avg = 0.0, below = 0.0, T1 = 0.0;
+  for (int k = 0; k < a.nZ; ++k) {
+    const double T = (a.Ti[vi + k * nv] + a.Ti[vj + k * nv]) / 2.0;   // map_Aa_to_Ac_3D
+    a.Ti_Ac[c + k * n] = T;
+    if (k == 0) T1 = T;
+    const double A = arrhenius(T);
+    a.A_flow_Ac[c + k * n] = A;
+    if (k > 0) avg = avg + 0.5 * (A + below) * (a.zeta[k] - a.zeta[k - 1]);
+    below = A;
+  }
+  a.A_mean_Ac[c] = a.mask_sheet_Ac[c] == 1 ? avg : arrhenius((T1 + kSMT) / 2.0);
+}
+
+// Device copies of the last physical properties, or null when none match this nZ.
+const double *props_A_flow(const GeomWork *w, const ufe_params *p) {
+  return (w->props_law >= 0 && w->props_nZ == p->nZ) ? w->props + (size_t)w->nV * w->props_nZ : nullptr;
+}
+const double *props_A_flow_Ac(const GeomWork *w, const ufe_params *p) {
+  return (w->props_law >= 0 && w->props_nZ == p->nZ) ? w->props + 5 * (size_t)w->nV * w->props_nZ : nullptr;
+}
+
 }  // namespace
 }  // namespace ufe
 
 using namespace ufe;
+
+extern "C" int ufe_ice_physical_properties(ufe_mesh_h h, const ufe_params *p, int flow_law, double time,
+                                           const double *Ti, ufe_physprop_out *out) {
+  if (!h || !p || !p->zeta) { set_error("ufe_ice_physical_properties: null argument"); return UFE_BAD_ARG; }
+  if (flow_law < UFE_FLOW_ARRHENIUS || flow_law > UFE_FLOW_MISMIP_MOD) {
+    set_error("ufe_ice_physical_properties: unknown flow law");
+    return UFE_BAD_ARG;
+  }
+  if (flow_law == UFE_FLOW_ARRHENIUS && !Ti) { set_error("ufe_ice_physical_properties: Ti is required"); return UFE_BAD_ARG; }
+  if (p->nZ < 2 || p->nZ > kMaxZP) { set_error("ufe_ice_physical_properties: nZ must be in [2, 64]"); return UFE_BAD_ARG; }
+  if (!h->geom || !h->geom->computed) {
+    set_error("ufe_ice_physical_properties: no device geometry (ufe_geometry_update or ufe_ssa_upload_geometry first)");
+    return UFE_BAD_ARG;
+  }
+  GeomWork *w = h->geom;
+  const size_t nV = w->nV, nAc = w->nAc, nZ = p->nZ;
+  cudaStream_t s = h->stream;
+  int rc = UFE_OK;
+  if (w->props_nZ != (int)nZ) {
+    if (w->props) { cudaFree(w->props); w->props = nullptr; }
+    w->props_nZ = 0;
+    w->props_law = -1;
+    rc = cuda_status(cudaMalloc(&w->props, (5 * nV + 2 * nAc) * nZ * sizeof(double)), "physical properties");
+    if (rc) return rc;
+    w->props_nZ = (int)nZ;
+  }
+  GeomArgs ga = args_of(w);
+  PropArgs a;
+  a.nV = (int)nV; a.nAc = (int)nAc; a.nZ = (int)nZ; a.law = flow_law;
+  a.A_const = 1.0E-16;
+  if (flow_law == UFE_FLOW_MISMIP_MOD && time >= 25000.0 && time < 50000.0) a.A_const = 1.0E-17;
+  a.Aci = w->Aci; a.Hi = AAF(ga, A_HI); a.mask_sheet = AAM(ga, M_SHEET); a.mask_sheet_Ac = ACM(ga, MC_SHEET);
+  double *Ti_d = w->props;
+  a.Ti = Ti_d;
+  a.A_flow = Ti_d + nV * nZ; a.Ti_pmp = a.A_flow + nV * nZ; a.Cpi = a.Ti_pmp + nV * nZ; a.Ki = a.Cpi + nV * nZ;
+  a.A_flow_Ac = a.Ki + nV * nZ; a.Ti_Ac = a.A_flow_Ac + nAc * nZ;
+  a.A_mean = AAF(ga, A_AF); a.A_mean_Ac = ACF(ga, C_AF);
+  for (size_t k = 0; k < nZ; ++k) a.zeta[k] = p->zeta[k];
+  if (flow_law == UFE_FLOW_ARRHENIUS) rc = up(Ti_d, Ti, nV * nZ, s);
+  if (!rc) { k_physprop_aa<<<(unsigned)((nV + 127) / 128), 128, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_physprop_aa"); }
+  if (!rc) { k_physprop_ac<<<(unsigned)((nAc + 127) / 128), 128, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_physprop_ac"); }
+  // the A fields stay valid on the device whatever the copies back do
+  if (!rc) { w->props_law = flow_law; w->af_set = true; }
+  if (out) {
+    auto dn = [&](double *dst, const double *src, size_t n) {
+      if (!dst || rc) return;
+      rc = cuda_status(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, s), "physical properties D2H");
+    };
+    dn(out->A_flow, a.A_flow, nV * nZ);
+    dn(out->A_flow_mean, a.A_mean, nV);
+    dn(out->A_flow_Ac, a.A_flow_Ac, nAc * nZ);
+    dn(out->A_flow_mean_Ac, a.A_mean_Ac, nAc);
+    if (flow_law != UFE_FLOW_MISMIP_MOD) {
+      dn(out->Ti_pmp, a.Ti_pmp, nV * nZ);
+      dn(out->Cpi, a.Cpi, nV * nZ);
+      dn(out->Ki, a.Ki, nV * nZ);
+    }
+    if (flow_law == UFE_FLOW_ARRHENIUS) dn(out->Ti_Ac, a.Ti_Ac, nAc * nZ);
+  }
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "physical properties");
+  return rc;
+}
 
 extern "C" int ufe_geometry_attach(ufe_mesh_h h, const ufe_geometry_mesh *g) {
   if (!h || !g || !g->nC || !g->C || !g->Nx || !g->Ny || !g->Aci || !g->Nx_Ac || !g->Ny_Ac || !g->No_Ac || !g->Np_Ac) {
@@ -311,19 +467,26 @@ extern "C" int ufe_geometry_update(ufe_mesh_h h, const double *Hi, const double 
 extern "C" int ufe_ssa_upload_geometry(ufe_mesh_h h, const ufe_params *p, const double *Hi, const double *Hb,
                                        const double *SL, const double *A_flow_mean, const double *A_flow_mean_Ac,
                                        const double *beta_sq_AaAc, const ufe_ssa_inout *io) {
-  if (!h || !p || !Hi || !Hb || !SL || !A_flow_mean || !A_flow_mean_Ac || !io) {
+  if (!h || !p || !Hi || !Hb || !SL || !io || (!A_flow_mean) != (!A_flow_mean_Ac)) {
     set_error("ufe_ssa_upload_geometry: null argument");
     return UFE_BAD_ARG;
   }
   if (!h->geom) { set_error("ufe_ssa_upload_geometry: call ufe_geometry_attach first"); return UFE_BAD_ARG; }
+  if (!A_flow_mean && !h->geom->af_set) {
+    set_error("ufe_ssa_upload_geometry: no flow factor on the device (ufe_ice_physical_properties first)");
+    return UFE_BAD_ARG;
+  }
   int rc = compute(h, Hi, Hb, SL);
   if (rc) return rc;
   GeomWork *w = h->geom;
   GeomArgs a = args_of(w);
   cudaStream_t s = h->stream;
   const size_t nV = w->nV, nAc = w->nAc, nA = nV + nAc;
-  rc = up(AAF(a, A_AF), A_flow_mean, nV, s);
-  if (!rc) rc = up(ACF(a, C_AF), A_flow_mean_Ac, nAc, s);
+  if (A_flow_mean) {
+    rc = up(AAF(a, A_AF), A_flow_mean, nV, s);
+    if (!rc) rc = up(ACF(a, C_AF), A_flow_mean_Ac, nAc, s);
+    w->af_set = rc == UFE_OK;
+  }
   double *beta_dev = nullptr;
   if (!rc && beta_sq_AaAc) {
     if (!w->beta) rc = cuda_status(cudaMalloc(&w->beta, nA * sizeof(double)), "geometry beta");
@@ -351,9 +514,14 @@ extern "C" int ufe_ssa_upload_geometry(ufe_mesh_h h, const ufe_params *p, const 
 }
 
 extern "C" int ufe_sia_solve_geometry(ufe_mesh_h h, const ufe_params *p, const double *A_flow_Ac, ufe_sia_out *out) {
-  if (!h || !p || !A_flow_Ac || !out) { set_error("ufe_sia_solve_geometry: null argument"); return UFE_BAD_ARG; }
+  if (!h || !p || !out) { set_error("ufe_sia_solve_geometry: null argument"); return UFE_BAD_ARG; }
   if (!h->geom || !h->geom->computed) {
     set_error("ufe_sia_solve_geometry: no device geometry (ufe_geometry_update or ufe_ssa_upload_geometry first)");
+    return UFE_BAD_ARG;
+  }
+  const double *A_dev = A_flow_Ac ? nullptr : props_A_flow_Ac(h->geom, p);
+  if (!A_flow_Ac && !A_dev) {
+    set_error("ufe_sia_solve_geometry: no A_flow_Ac on the device for this nZ (ufe_ice_physical_properties first)");
     return UFE_BAD_ARG;
   }
   GeomArgs a = args_of(h->geom);
@@ -362,8 +530,8 @@ extern "C" int ufe_sia_solve_geometry(ufe_mesh_h h, const ufe_params *p, const d
   in.Hi_Ac = ACF(a, C_HI);
   in.dHs_dx_Ac = ACF(a, C_DHS_DX); in.dHs_dy_Ac = ACF(a, C_DHS_DY);
   in.dHs_dp_Ac = ACF(a, C_DHS_DP); in.dHs_do_Ac = ACF(a, C_DHS_DO);
-  in.A_flow_Ac = A_flow_Ac;
-  return sia_solve_impl(h, p, &in, out, true);
+  in.A_flow_Ac = A_flow_Ac ? A_flow_Ac : A_dev;
+  return sia_solve_impl(h, p, &in, out, true, A_dev != nullptr);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -694,13 +862,18 @@ __global__ void k_sia3d_w(const Sia3dArgs a) {
 
 extern "C" int ufe_sia3d_solve(ufe_mesh_h h, const ufe_params *p, const double *A_flow, const double *dHb_dt,
                                ufe_sia3d_out *out) {
-  if (!h || !p || !A_flow || !dHb_dt || !out || !p->zeta) { set_error("ufe_sia3d_solve: null argument"); return UFE_BAD_ARG; }
+  if (!h || !p || !dHb_dt || !out || !p->zeta) { set_error("ufe_sia3d_solve: null argument"); return UFE_BAD_ARG; }
   if (p->nZ < 2 || p->nZ > kMaxZ3) { set_error("ufe_sia3d_solve: nZ must be in [2, 64]"); return UFE_BAD_ARG; }
   if (!h->geom || !h->geom->computed) {
     set_error("ufe_sia3d_solve: no device geometry (ufe_geometry_update or ufe_ssa_upload_geometry first)");
     return UFE_BAD_ARG;
   }
   GeomWork *g = h->geom;
+  const double *A_dev = A_flow ? nullptr : props_A_flow(g, p);
+  if (!A_flow && !A_dev) {
+    set_error("ufe_sia3d_solve: no A_flow on the device for this nZ (ufe_ice_physical_properties first)");
+    return UFE_BAD_ARG;
+  }
   const DevMesh &m = h->m;
   GeomArgs ga = args_of(g);
   const size_t nV = m.nV, nZ = p->nZ;
@@ -719,12 +892,12 @@ extern "C" int ufe_sia3d_solve(ufe_mesh_h h, const ufe_params *p, const double *
   a.mask_shelf = AAM(ga, M_SHELF); a.mask_sheet = AAM(ga, M_SHEET);
   double *A = g->sia3d, *dhb = A + nV * nZ;
   a.U3 = dhb + nV; a.V3 = a.U3 + nV * nZ; a.W3 = a.V3 + nV * nZ;
-  a.A = A; a.dHb_dt = dhb;
+  a.A = A_dev ? A_dev : A; a.dHb_dt = dhb;
   const double *uv = ssa_device_UV(h);
   a.U_SSA = uv; a.V_SSA = uv ? uv + nV : nullptr;
   a.m_enh = p->m_enh_sia;
   for (size_t k = 0; k < nZ; ++k) { a.zeta[k] = p->zeta[k]; a.zeta3[k] = std::pow(p->zeta[k], 3.0); }
-  int rc = up(A, A_flow, nV * nZ, s);
+  int rc = A_dev ? UFE_OK : up(A, A_flow, nV * nZ, s);
   if (!rc) rc = up(dhb, dHb_dt, nV, s);
   const unsigned gv = (unsigned)((nV + 127) / 128);
   if (!rc) { k_sia3d_uv<<<gv, 128, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_sia3d_uv"); }

@@ -126,7 +126,8 @@ void sia_free(SiaWork *w);
 void adj_free(AdjWork *w);
 void geom_free(GeomWork *w);
 // ufe_sia_solve with the mask and Ac fields of `in` on the device (A_flow_Ac on the host).
-int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out, bool fields_on_device);
+int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out, bool fields_on_device,
+                   bool A_on_device = false);
 // Velocities of the last solves on a handle, on the device (caller order), or null.
 const double *ssa_device_Up(ufe_mesh_h h);
 const double *ssa_device_UV(ufe_mesh_h h);

@@ -129,8 +129,10 @@ const double *sia_device_Up(ufe_mesh_h h) {
 
 namespace ufe {
 // ufe_sia_solve; with fields_on_device the mask and the five Ac fields of `in` are device
-// arrays of this device (the device geometry preparation), A_flow_Ac stays a host array.
-int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out, bool fields_on_device) {
+// arrays of this device (the device geometry preparation), and with A_on_device A_flow_Ac is
+// too (the device physical properties); otherwise A_flow_Ac is a host array.
+int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_sia_out *out, bool fields_on_device,
+                   bool A_on_device) {
   if (!h || !p || !in || !out) { set_error("ufe_sia_solve: null argument"); return UFE_BAD_ARG; }
   if (!in->mask_sheet_Ac || !in->Hi_Ac || !in->dHs_dx_Ac || !in->dHs_dy_Ac || !in->dHs_dp_Ac ||
       !in->dHs_do_Ac || !in->A_flow_Ac || !p->zeta) {
@@ -165,7 +167,9 @@ int sia_solve_impl(ufe_mesh_h h, const ufe_params *p, const ufe_sia_in *in, ufe_
   const double *src[5] = {in->Hi_Ac, in->dHs_dx_Ac, in->dHs_dy_Ac, in->dHs_dp_Ac, in->dHs_do_Ac};
   for (int k = 0; k < 5 && !rc; ++k)
     rc = cuda_status(cudaMemcpyAsync(w->in + k * na, src[k], na * sizeof(double), kin, s), "sia input");
-  if (!rc) rc = cuda_status(cudaMemcpyAsync(A, in->A_flow_Ac, na * nZ * sizeof(double), cudaMemcpyHostToDevice, s), "H2D A_flow");
+  if (!rc)
+    rc = cuda_status(cudaMemcpyAsync(A, in->A_flow_Ac, na * nZ * sizeof(double),
+                                     A_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s), "A_flow input");
   double *D3 = w->out, *D = D3 + na * nZ, *Ux = D + na, *Uy = Ux + na, *Up = Uy + na, *Uo = Up + na;
   double *Ua = Uo + na, *Va = Ua + nV, *Da = Va + nV;
   if (!rc) {
