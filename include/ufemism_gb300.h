@@ -272,6 +272,28 @@ typedef struct ufe_physprop_out {
 int ufe_ice_physical_properties(ufe_mesh_h mesh, const ufe_params *params, int flow_law, double time,
                                 const double *Ti, ufe_physprop_out *out);
 
+/* Upwind derivatives for the thermodynamics: get_upwind_derivative_vertex_3D
+ * (mesh_derivatives_module.f90:434-483) for every vertex and layer on the device. Where the
+ * wind (U_3D, V_3D) is below 1e-10 in both components, the Aa neighbour-function derivative;
+ * otherwise the derivative on the first triangle around the vertex (iTri order) that holds the
+ * point V(vi) - (U,V) R(vi) / (4 |(U,V)|) (is_in_triangle, mesh_help_functions_module.f90:646-672,
+ * tolerance 1e-8). ufe_triangles_attach (after ufe_geometry_attach) uploads the reference's
+ * triangle data once per mesh. U_3D and V_3D both NULL: those of the last ufe_sia3d_solve on the
+ * device; d NULL: the Ti of the last ufe_ice_physical_properties (UFE_FLOW_ARRHENIUS). All 2-D
+ * arrays are (nV,nZ). A pair (vertex, layer) with no upwind triangle gets 0 and is counted in
+ * *no_upwind (may be NULL); the reference reports it and reads outside NxTri there. */
+typedef struct ufe_triangle_mesh {
+  int32_t nTri;
+  const double *V;                      /* (nV,2) vertex coordinates */
+  const double *R;                      /* (nV) mesh%R, the distance to the nearest neighbour */
+  const int32_t *niTri, *iTri;          /* (nV), (nV,nC_mem) */
+  const int32_t *Tri;                   /* (nTri,3) */
+  const double *NxTri, *NyTri;          /* (nTri,3) */
+} ufe_triangle_mesh;
+int ufe_triangles_attach(ufe_mesh_h mesh, const ufe_triangle_mesh *triangles);
+int ufe_upwind_derivatives_3d(ufe_mesh_h mesh, const ufe_params *params, const double *U_3D, const double *V_3D,
+                              const double *d, double *ddx, double *ddy, int64_t *no_upwind);
+
 /* calculate_ice_thickness_change (ice_dynamics_module.f90:31-237) on the device: upwind ice
  * volume fluxes across every Aa connection from Up_SIA_Ac + Up_SSA_Ac, the outflux rescale
  * against the available ice plus SMB and BMB, dHi/dt, the update of Hi (in place), the

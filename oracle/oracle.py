@@ -28,7 +28,7 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB) or any(
             os.path.getmtime(os.path.join(_HERE, f)) > os.path.getmtime(_LIB)
             for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle_thickness.c", "ufe_oracle_sia3d.c",
-                      "ufe_oracle_physprop.c", "ufe_oracle.h")):
+                      "ufe_oracle_physprop.c", "ufe_oracle_upwind.c", "ufe_oracle.h")):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
 
@@ -389,3 +389,38 @@ def ice_physical_properties(m: AaAcMesh, Hi, mask_sheet, mask_sheet_Ac, Ti=None,
     if rc != OR_OK:
         raise RuntimeError("or_ice_physical_properties failed: %d" % rc)
     return out
+
+
+def triangle_functions(base):
+    """NxTri, NyTri (nTri, 3) of get_neighbour_functions."""
+    NxT = np.zeros((base.nTri, 3), order="F")
+    NyT = np.zeros((base.nTri, 3), order="F")
+    bs, bkeep = _base_struct(base)
+    lib().or_triangle_functions(ct.byref(bs), _vp(NxT), _vp(NyT))
+    return NxT, NyT
+
+
+def vertex_resolution(base, domain_width=None):
+    """mesh%R: the distance from each vertex to its nearest neighbour."""
+    V = np.asarray(base.V)
+    w = float(V[:, 0].max() - V[:, 0].min()) if domain_width is None else float(domain_width)
+    R = np.zeros(base.nV)
+    bs, bkeep = _base_struct(base)
+    lib().or_vertex_resolution(ct.byref(bs), ct.c_double(w), _vp(R))
+    return R
+
+
+def upwind_derivatives_3d(m: AaAcMesh, R, NxTri, NyTri, U, V, d):
+    """get_upwind_derivative_vertex_3D for every vertex and layer. Returns (ddx, ddy,
+    number of pairs without an upwind triangle)."""
+    base = m.base
+    keep = [_f64(R), _f64(NxTri), _f64(NyTri), _f64(U), _f64(V), _f64(d)]
+    nV, nZ = keep[3].shape
+    ddx = np.zeros((nV, nZ), order="F")
+    ddy = np.zeros((nV, nZ), order="F")
+    bs, bkeep = _base_struct(base)
+    ms = _aaac_struct(m)
+    f = lib().or_upwind_derivatives_3d
+    f.restype = ct.c_longlong
+    missing = f(ct.byref(bs), ct.byref(ms), ct.c_int(nZ), *(_vp(k) for k in keep), _vp(ddx), _vp(ddy))
+    return ddx, ddy, int(missing)

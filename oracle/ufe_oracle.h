@@ -210,6 +210,18 @@ int or_ice_physical_properties(int nV, int nAc, int nZ, const double *zeta, cons
                                double *A_flow_mean, double *A_flow_mean_Ac, double *Ti_pmp, double *Cpi, double *Ki,
                                double *Ti_Ac);
 
+/* The triangle functions NxTri/NyTri (nTri,3) of get_neighbour_functions
+ * (mesh_derivatives_module.f90:30-47) and the vertex resolution mesh%R
+ * (mesh_help_functions_module.f90:195-211; domain_width = xmax - xmin). */
+void or_triangle_functions(const or_base *b, double *NxTri, double *NyTri);
+void or_vertex_resolution(const or_base *b, double domain_width, double *R);
+/* get_upwind_derivative_vertex_3D (mesh_derivatives_module.f90:434-483) for every vertex and
+ * layer; U, V, d, ddx, ddy are (nV, nZ). Returns the number of (vertex, layer) pairs without an
+ * upwind triangle (their derivatives are 0 here; the reference reads outside NxTri there). */
+long long or_upwind_derivatives_3d(const or_base *b, const or_aaac *m, int nZ, const double *R, const double *NxTri,
+                                   const double *NyTri, const double *U, const double *V, const double *d,
+                                   double *ddx, double *ddy);
+
 /* Primitive operators, for tests. */
 void or_map_Aa_to_Ac(const or_aaac *m, int nV, const double *d_Aa, double *d_Ac);
 void or_map_Ac_to_Aa(const or_base *b, const or_aaac *m, const double *d_Ac, double *d_Aa);

@@ -251,3 +251,60 @@ def test_physical_properties_feed_the_solves():
         assert np.array_equal(a, b)
     assert np.count_nonzero(o1["U_SSA"]) > 0
     dm.close()
+
+
+def _triangles(m, dm):
+    NxT, NyT = orc.triangle_functions(m.base)
+    R = orc.vertex_resolution(m.base)
+    dm.triangles_attach(m.base, R, NxT, NyT)
+    return R, NxT, NyT
+
+
+def test_upwind_derivatives_match_oracle():
+    """get_upwind_derivative_vertex_3D on the device: bit-identical to the oracle (same
+    triangle decisions, separately rounded arithmetic), including the windless layer and the
+    count of edge pairs without an upwind triangle."""
+    m = oracle_aaac("4k")
+    nV, nZ = m.base.nV, 15
+    rng = np.random.default_rng(21)
+    U = rng.normal(size=(nV, nZ)) * 200.0
+    V = rng.normal(size=(nV, nZ)) * 200.0
+    U[:, 3] = 0.0
+    V[:, 3] = 0.0
+    U, V = np.asfortranarray(U), np.asfortranarray(V)
+    d = np.asfortranarray(250.0 + 20.0 * rng.random((nV, nZ)))
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    R, NxT, NyT = _triangles(m, dm)
+    p = api.default_params()
+    gx, gy, gmiss = dm.upwind_derivatives_3d(p, U, V, d)
+    rx, ry, rmiss = orc.upwind_derivatives_3d(m, R, NxT, NyT, U, V, d)
+    assert np.array_equal(gx, rx) and np.array_equal(gy, ry)
+    assert gmiss == rmiss and 0 < rmiss < nV * nZ // 20
+    dm.close()
+
+
+def test_upwind_derivatives_of_the_device_step():
+    """Ti -> physical properties -> SSA -> 3-D SIA -> upwind derivatives of Ti with every field
+    left on the device, equal to the same call given those fields from the host."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, "dome")
+    nV = m.base.nV
+    rng = np.random.default_rng(22)
+    Ti = np.asfortranarray(250.0 + 15.0 * rng.random((nV, 15)))
+    p = api.default_params(precision=nat.UFE_FP64)
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    _triangles(m, dm)
+    dm.geometry_update(ssa["Hi"], ssa["Hb"], ssa["SL"])
+    with pytest.raises(nat.UfeError):
+        dm.upwind_derivatives_3d(p)          # no 3-D velocities yet
+    dm.ice_physical_properties(p, Ti)
+    dm.ssa_upload_geometry(ssa["Hi"], ssa["Hb"], ssa["SL"], None, None, p)
+    dm.ssa_run(p, check=False)
+    U3, V3, _ = dm.solve_sia_3d(None, np.zeros(nV), p)
+    gx, gy, gm = dm.upwind_derivatives_3d(p)
+    hx, hy, hm = dm.upwind_derivatives_3d(p, U3, V3, Ti)
+    assert np.array_equal(gx, hx) and np.array_equal(gy, hy) and gm == hm
+    assert np.count_nonzero(gx) > 0
+    dm.close()

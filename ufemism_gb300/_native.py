@@ -106,6 +106,10 @@ class PhyspropOut(ct.Structure):
     _fields_ = [(n, P) for n in PHYSPROP_OUT_FIELDS]
 
 
+class TriangleMesh(ct.Structure):
+    _fields_ = [("nTri", I32)] + [(n, P) for n in ("V", "R", "niTri", "iTri", "Tri", "NxTri", "NyTri")]
+
+
 class ThicknessIn(ct.Structure):
     _fields_ = [(n, P) for n in ("A", "Cw", "Up_SIA_Ac", "Up_SSA_Ac", "SMB_year", "BMB", "mask_noice")] + \
                [("dt", F64), ("zero_edges", I32)]
@@ -197,6 +201,8 @@ PROTOTYPES = {
     "ufe_sia_solve_geometry": (I32, [P, ct.POINTER(Params), P, ct.POINTER(SiaOut)]),
     "ufe_sia3d_solve": (I32, [P, ct.POINTER(Params), P, P, ct.POINTER(Sia3dOut)]),
     "ufe_ice_physical_properties": (I32, [P, ct.POINTER(Params), I32, ct.c_double, P, ct.POINTER(PhyspropOut)]),
+    "ufe_triangles_attach": (I32, [P, ct.POINTER(TriangleMesh)]),
+    "ufe_upwind_derivatives_3d": (I32, [P, ct.POINTER(Params), P, P, P, P, P, ct.POINTER(ct.c_int64)]),
     "ufe_thickness_update": (I32, [P, ct.POINTER(ThicknessIn), P, ct.POINTER(ThicknessOut)]),
     "ufe_ssa_vjp": (I32, [P, ct.POINTER(Params), ct.POINTER(VjpParams), ct.POINTER(VjpIn), ct.POINTER(VjpGeom),
                           ct.POINTER(VjpOut), ct.POINTER(VjpStats)]),

@@ -378,6 +378,40 @@ class DeviceMesh:
             raise nat.UfeError(rc, "ufe_ice_physical_properties")
         return out
 
+    def triangles_attach(self, base, R, NxTri, NyTri):
+        """Upload the triangle data of the upwind derivatives (ufe_triangles_attach): the base
+        mesh's V, niTri, iTri, Tri, and mesh%R, NxTri, NyTri."""
+        L = nat.load()
+        k = dict(V=_f64(base.V), R=_f64(R), niTri=_i32(base.niTri), iTri=_i32(base.iTri), Tri=_i32(base.Tri),
+                 NxTri=_f64(NxTri), NyTri=_f64(NyTri))
+        nTri = k["Tri"].shape[0]
+        if k["V"].shape != (self.nV, 2) or k["R"].shape != (self.nV,) or k["NxTri"].shape != (nTri, 3) or \
+                k["NyTri"].shape != (nTri, 3) or k["Tri"].shape != (nTri, 3):
+            raise ValueError("triangle arrays do not match this mesh")
+        t = nat.TriangleMesh(nTri, *(_ptr(k[n]) for n in ("V", "R", "niTri", "iTri", "Tri", "NxTri", "NyTri")))
+        rc = L.ufe_triangles_attach(self._h, ct.byref(t))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_triangles_attach")
+
+    def upwind_derivatives_3d(self, params: dict, U_3D=None, V_3D=None, d=None):
+        """ufe_upwind_derivatives_3d. U_3D, V_3D None: the device's last 3-D SIA velocities; d
+        None: the device's Ti. Returns (ddx, ddy, pairs without an upwind triangle)."""
+        L = nat.load()
+        nZ = len(params["zeta"])
+        arrs = [None if a is None else np.asfortranarray(a, dtype=np.float64) for a in (U_3D, V_3D, d)]
+        for a in arrs:
+            if a is not None and a.shape != (self.nV, nZ):
+                raise ValueError("fields must be (nV, nZ)")
+        ddx = np.zeros((self.nV, nZ), order="F")
+        ddy = np.zeros((self.nV, nZ), order="F")
+        miss = ct.c_int64(0)
+        ps, _z = _params_struct(params)
+        rc = L.ufe_upwind_derivatives_3d(self._h, ct.byref(ps), *(_ptr(a) for a in arrs), ddx.ctypes.data,
+                                         ddy.ctypes.data, ct.byref(miss))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_upwind_derivatives_3d")
+        return ddx, ddy, int(miss.value)
+
     def thickness_update(self, Hi, A, Cw, SMB_year, BMB, dt, Up_SIA_Ac=None, Up_SSA_Ac=None, mask_noice=None,
                          zero_edges=True):
         """calculate_ice_thickness_change on the device (ufe_thickness_update). Velocities left

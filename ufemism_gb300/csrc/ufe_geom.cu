@@ -36,12 +36,21 @@ struct GeomWork {
   int props_nZ = 0;
   int props_law = -1;          // flow law of the last ufe_ice_physical_properties, -1: none
   bool af_set = false;         // A_flow_mean(_Ac) present on the device (physical properties or an upload)
+  bool sia3d_done = false;     // U_3D, V_3D, W_3D of a successful ufe_sia3d_solve in sia3d
+  // triangles (ufe_triangles_attach) and the upwind-derivative work
+  int nTri = 0;
+  double *tV = nullptr, *tR = nullptr, *NxTri = nullptr, *NyTri = nullptr;
+  int *niTri = nullptr, *iTri = nullptr, *Tri = nullptr;
+  double *upw = nullptr;       // U, V, d in; ddx, ddy out (nV x nZ each)
+  int upw_nZ = 0;
+  unsigned long long *upw_missing = nullptr;
   bool computed = false;
 };
 
 void geom_free(GeomWork *w) {
   if (!w) return;
-  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int, w->sia3d, w->props};
+  void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int, w->sia3d, w->props,
+                   w->tV, w->tR, w->NxTri, w->NyTri, w->niTri, w->iTri, w->Tri, w->upw, w->upw_missing};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete w;
@@ -878,8 +887,10 @@ extern "C" int ufe_sia3d_solve(ufe_mesh_h h, const ufe_params *p, const double *
   GeomArgs ga = args_of(g);
   const size_t nV = m.nV, nZ = p->nZ;
   cudaStream_t s = h->stream;
+  g->sia3d_done = false;
   if (g->sia3d_nZ != (int)nZ) {
     if (g->sia3d) { cudaFree(g->sia3d); g->sia3d = nullptr; }
+    g->sia3d_nZ = 0;
     int rc = cuda_status(cudaMalloc(&g->sia3d, (4 * nV * nZ + nV) * sizeof(double)), "sia3d work");
     if (rc) return rc;
     g->sia3d_nZ = (int)nZ;
@@ -916,5 +927,200 @@ extern "C" int ufe_sia3d_solve(ufe_mesh_h h, const ufe_params *p, const double *
   dn(out->V_3D, a.V3);
   dn(out->W_3D, a.W3);
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "sia3d solve");
+  g->sia3d_done = rc == UFE_OK;
+  return rc;
+}
+
+// ---------------------------------------------------------------------------------------
+// Upwind derivatives for the thermodynamics: get_upwind_derivative_vertex_3D
+// (mesh_derivatives_module.f90:434-483) with is_in_triangle (mesh_help_functions_module.f90:
+// 646-672). One thread per (vertex, layer), vertex fastest, so the wind and the field are read
+// coalesced and only the triangle search gathers. Separately rounded products (no FMA) and
+// IEEE sqrt/division: the search takes the same decisions as the reference's arithmetic.
+// ---------------------------------------------------------------------------------------
+namespace ufe {
+namespace {
+
+struct UpwArgs {
+  int nV, nZ, nTri;
+  const int *nC, *C;                    // (nV), (nV, ncm), 1-based
+  const double *Nx, *Ny;                // (nV, ncm + 1), home at column nC + 1
+  const double *V, *R;                  // (nV, 2), (nV)
+  const int *niTri, *iTri, *Tri;        // (nV), (nV, ncm), (nTri, 3), 1-based
+  const double *NxTri, *NyTri;          // (nTri, 3)
+  const double *U, *Vw, *d;             // (nV, nZ)
+  double *ddx, *ddy;                    // (nV, nZ)
+  unsigned long long *missing;
+};
+
+__device__ __forceinline__ bool in_triangle(double pax, double pay, double pbx, double pby, double pcx, double pcy,
+                                            double px, double py) {
+  const double tol = 1E-8;
+  const double as_x = px - pax, as_y = py - pay;
+  const double s1 = ((pbx - pax) * as_y - (pby - pay) * as_x);
+  const double s2 = ((pcx - pax) * as_y - (pcy - pay) * as_x);
+  const double s3 = ((pcx - pbx) * (py - pby) - (pcy - pby) * (px - pbx));
+  return s1 > -tol && s2 < tol && s3 > -tol;
+}
+
+__global__ void k_upwind(const UpwArgs a) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n = a.nV, nt = a.nTri;
+  if (i >= n * a.nZ) return;
+  const int vi = (int)(i % n);
+  const size_t kof = i - vi;            // k * nV
+  const double u = a.U[i], v = a.Vw[i];
+  double dx = 0.0, dy = 0.0;
+  if (fabs(u) < 1E-10 && fabs(v) < 1E-10) {
+    // get_mesh_derivatives_vertex_3D (372-392): home term first
+    const int nc = a.nC[vi];
+    dx = a.Nx[vi + nc * n] * a.d[i];
+    dy = a.Ny[vi + nc * n] * a.d[i];
+    for (int c = 0; c < nc; ++c) {
+      const double dc = a.d[(a.C[vi + c * n] - 1) + kof];
+      dx = dx + a.Nx[vi + c * n] * dc;
+      dy = dy + a.Ny[vi + c * n] * dc;
+    }
+  } else {
+    const double s = 4.0 * sqrt(u * u + v * v);
+    const double r = a.R[vi];
+    const double px = a.V[vi] - u * r / s, py = a.V[vi + n] - v * r / s;
+    int tup = -1, ta = 0, tb = 0, tc = 0;
+    const int ni = a.niTri[vi];
+    for (int it = 0; it < ni; ++it) {
+      const int ti = a.iTri[vi + it * n] - 1;
+      const int qa = a.Tri[ti] - 1, qb = a.Tri[ti + nt] - 1, qc = a.Tri[ti + 2 * nt] - 1;
+      if (in_triangle(a.V[qa], a.V[qa + n], a.V[qb], a.V[qb + n], a.V[qc], a.V[qc + n], px, py)) {
+        tup = ti; ta = qa; tb = qb; tc = qc;
+        break;
+      }
+    }
+    if (tup < 0) {
+      atomicAdd(a.missing, 1ull);
+    } else {
+      const double da = a.d[ta + kof], db = a.d[tb + kof], dc = a.d[tc + kof];
+      dx = a.NxTri[tup] * da + a.NxTri[tup + nt] * db + a.NxTri[tup + 2 * nt] * dc;
+      dy = a.NyTri[tup] * da + a.NyTri[tup + nt] * db + a.NyTri[tup + 2 * nt] * dc;
+    }
+  }
+  a.ddx[i] = dx;
+  a.ddy[i] = dy;
+}
+
+}  // namespace
+}  // namespace ufe
+
+extern "C" int ufe_triangles_attach(ufe_mesh_h h, const ufe_triangle_mesh *t) {
+  if (!h || !t || !t->V || !t->R || !t->niTri || !t->iTri || !t->Tri || !t->NxTri || !t->NyTri) {
+    set_error("ufe_triangles_attach: missing array");
+    return UFE_BAD_ARG;
+  }
+  if (!h->geom) { set_error("ufe_triangles_attach: call ufe_geometry_attach first"); return UFE_BAD_ARG; }
+  GeomWork *w = h->geom;
+  const int nV = w->nV, ncm = w->ncm, nTri = t->nTri;
+  if (nTri < 1) { set_error("ufe_triangles_attach: nTri must be positive"); return UFE_BAD_MESH; }
+  // validate the index arrays on the host before any kernel reads them
+  for (size_t k = 0; k < 3 * (size_t)nTri; ++k)
+    if (t->Tri[k] < 1 || t->Tri[k] > nV) { set_error("ufe_triangles_attach: Tri out of range"); return UFE_BAD_MESH; }
+  for (int v = 0; v < nV; ++v) {
+    if (t->niTri[v] < 0 || t->niTri[v] > ncm) { set_error("ufe_triangles_attach: niTri out of range"); return UFE_BAD_MESH; }
+    for (int c = 0; c < t->niTri[v]; ++c) {
+      const int ti = t->iTri[v + (size_t)c * nV];
+      if (ti < 1 || ti > nTri) { set_error("ufe_triangles_attach: iTri out of range"); return UFE_BAD_MESH; }
+    }
+  }
+  void *old[] = {w->tV, w->tR, w->NxTri, w->NyTri, w->niTri, w->iTri, w->Tri};
+  for (void *p : old)
+    if (p) cudaFree(p);
+  w->tV = w->tR = w->NxTri = w->NyTri = nullptr;
+  w->niTri = w->iTri = w->Tri = nullptr;
+  w->nTri = 0;
+  cudaStream_t s = h->stream;
+  const size_t nv = nV, nt = nTri, nc = ncm;
+  int rc = cuda_status(cudaMalloc(&w->tV, 2 * nv * sizeof(double)), "triangles");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->tR, nv * sizeof(double)), "triangles");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->NxTri, 3 * nt * sizeof(double)), "triangles");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->NyTri, 3 * nt * sizeof(double)), "triangles");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->niTri, nv * sizeof(int)), "triangles");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->iTri, nv * nc * sizeof(int)), "triangles");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->Tri, 3 * nt * sizeof(int)), "triangles");
+  if (!rc) rc = up(w->tV, t->V, 2 * nv, s);
+  if (!rc) rc = up(w->tR, t->R, nv, s);
+  if (!rc) rc = up(w->NxTri, t->NxTri, 3 * nt, s);
+  if (!rc) rc = up(w->NyTri, t->NyTri, 3 * nt, s);
+  if (!rc) rc = up(w->niTri, t->niTri, nv, s);
+  if (!rc) rc = up(w->iTri, t->iTri, nv * nc, s);
+  if (!rc) rc = up(w->Tri, t->Tri, 3 * nt, s);
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "triangles attach");
+  if (!rc) w->nTri = nTri;
+  return rc;
+}
+
+extern "C" int ufe_upwind_derivatives_3d(ufe_mesh_h h, const ufe_params *p, const double *U_3D, const double *V_3D,
+                                         const double *d, double *ddx, double *ddy, int64_t *no_upwind) {
+  if (!h || !p || !ddx || !ddy || (!U_3D) != (!V_3D)) {
+    set_error("ufe_upwind_derivatives_3d: null argument");
+    return UFE_BAD_ARG;
+  }
+  if (p->nZ < 1) { set_error("ufe_upwind_derivatives_3d: nZ must be positive"); return UFE_BAD_ARG; }
+  if (!h->geom || h->geom->nTri < 1) {
+    set_error("ufe_upwind_derivatives_3d: call ufe_geometry_attach and ufe_triangles_attach first");
+    return UFE_BAD_ARG;
+  }
+  GeomWork *w = h->geom;
+  const size_t nV = w->nV, nZ = p->nZ, nf = nV * nZ;
+  if (!U_3D && !(w->sia3d_done && w->sia3d_nZ == (int)nZ)) {
+    set_error("ufe_upwind_derivatives_3d: no 3-D velocities on the device for this nZ (ufe_sia3d_solve first)");
+    return UFE_BAD_ARG;
+  }
+  if (!d && !(w->props_law == UFE_FLOW_ARRHENIUS && w->props_nZ == (int)nZ)) {
+    set_error("ufe_upwind_derivatives_3d: no Ti on the device for this nZ (ufe_ice_physical_properties first)");
+    return UFE_BAD_ARG;
+  }
+  cudaStream_t s = h->stream;
+  int rc = UFE_OK;
+  if (w->upw_nZ != (int)nZ) {
+    if (w->upw) { cudaFree(w->upw); w->upw = nullptr; }
+    w->upw_nZ = 0;
+    rc = cuda_status(cudaMalloc(&w->upw, 5 * nf * sizeof(double)), "upwind work");
+    if (rc) return rc;
+    w->upw_nZ = (int)nZ;
+  }
+  if (!w->upw_missing) {
+    rc = cuda_status(cudaMalloc(&w->upw_missing, sizeof(unsigned long long)), "upwind work");
+    if (rc) return rc;
+  }
+  double *Ud = w->upw, *Vd = Ud + nf, *dd = Vd + nf, *ox = dd + nf, *oy = ox + nf;
+  UpwArgs a;
+  a.nV = (int)nV; a.nZ = (int)nZ; a.nTri = w->nTri;
+  a.nC = w->nC; a.C = w->C; a.Nx = w->Nx; a.Ny = w->Ny;
+  a.V = w->tV; a.R = w->tR; a.niTri = w->niTri; a.iTri = w->iTri; a.Tri = w->Tri;
+  a.NxTri = w->NxTri; a.NyTri = w->NyTri;
+  if (U_3D) {
+    a.U = Ud; a.Vw = Vd;
+    rc = up(Ud, U_3D, nf, s);
+    if (!rc) rc = up(Vd, V_3D, nf, s);
+  } else {
+    const double *u3 = w->sia3d + nf + nV;           // A_flow, dHb_dt, then U_3D, V_3D, W_3D
+    a.U = u3; a.Vw = u3 + nf;
+  }
+  if (d) {
+    a.d = dd;
+    if (!rc) rc = up(dd, d, nf, s);
+  } else {
+    a.d = w->props;                                   // Ti comes first in the properties block
+  }
+  a.ddx = ox; a.ddy = oy; a.missing = w->upw_missing;
+  if (!rc) rc = cuda_status(cudaMemsetAsync(w->upw_missing, 0, sizeof(unsigned long long), s), "upwind");
+  if (!rc) {
+    k_upwind<<<(unsigned)((nf + 255) / 256), 256, 0, s>>>(a);
+    rc = cuda_status(cudaGetLastError(), "k_upwind");
+  }
+  unsigned long long missing = 0;
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(ddx, ox, nf * sizeof(double), cudaMemcpyDeviceToHost, s), "upwind D2H");
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(ddy, oy, nf * sizeof(double), cudaMemcpyDeviceToHost, s), "upwind D2H");
+  if (!rc) rc = cuda_status(cudaMemcpyAsync(&missing, w->upw_missing, sizeof(missing), cudaMemcpyDeviceToHost, s), "upwind D2H");
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "upwind derivatives");
+  if (!rc && no_upwind) *no_upwind = (int64_t)missing;
   return rc;
 }
