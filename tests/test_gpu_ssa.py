@@ -179,6 +179,30 @@ def test_not_converged_warning():
     _check_solution(gout, oout, FP64_TOL)
 
 
+MIXED_LAG = 1   # the mixed sweeps decide convergence this many sweeps late (ufe_ssa.cu, kMixedLag)
+
+
+def test_mixed_lagged_decisions_cap_and_reset():
+    """The mixed sweeps decide convergence from the residual of the sweep `MIXED_LAG` earlier,
+    with no team barrier between sweeps, and decide exactly at the sweep cap: a capped solve
+    stops at the cap and warns like the reference, a converged one has done at least
+    MIXED_LAG + 1 sweeps and ends below the tolerance, and a diverging one resets once."""
+    kw = dict(SSA_max_inner_loops=20, SSA_max_outer_loops=3)
+    m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both("1k", precision=nat.UFE_MIXED, oracle_kw=kw, gpu_kw=kw)
+    assert rc_o == orc.OR_NOT_CONVERGED and rc_g == nat.UFE_NOT_CONVERGED
+    assert gst["sweeps"][0] == 20 and all(sw <= 20 for sw in gst["sweeps"])
+    m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both("4k", precision=nat.UFE_MIXED,
+                                                        gpu_kw=dict(mixed_refold_sweeps=8))
+    assert rc_g == rc_o == 0
+    _check_solution(gout, oout, MIXED_TOL)
+    assert all(sw >= MIXED_LAG + 1 for sw in gst["sweeps"])
+    assert gst["last_max_residual"] < api.default_params()["SSA_max_residual_UV"]
+    kw = dict(SSA_SOR_omega=2.5)
+    m, (rc_o, oout, ost), (rc_g, gout, gst) = _run_both("tiny", precision=nat.UFE_MIXED, oracle_kw=kw, gpu_kw=kw)
+    assert rc_o == orc.OR_RESET_ONCE and rc_g == nat.UFE_RESET_ONCE
+    assert gst["resets"] == 1 and np.all(gout["U_SSA"] == 0.0)
+
+
 def test_early_outs_zero_velocity():
     m = oracle_aaac("tiny")
     ssa, sia, g = oracle_inputs(m)

@@ -58,6 +58,9 @@ struct SsaCtl {
   double last_RN;
   double last_max_residual;
   int sweeps[64];
+  // lagged convergence decisions of the mixed sweeps (ring of kLagRing sweeps)
+  unsigned int lag_cnt[8];          // CTAs counted in per slot, monotonic within a launch
+  unsigned long long lag_res[8];    // (sweep + 1) << 32 | FP32 bits of the sweep's max |res|, rounded up
 };
 
 // Sweep arithmetic of the persistent solver.
@@ -117,6 +120,17 @@ struct SsaArgs {
 };
 
 constexpr unsigned int kBarrierError = 1u << 30;
+// Ring of the lagged decisions: a slot is reused kLagRing sweeps later, safe for lag <= 3
+// (the writer of sweep G + kLagRing has seen every CTA finish sweep G + kLagRing - 1 - lag,
+// after every reader of sweep G read it, when kLagRing > 2 lag + 1).
+constexpr int kLagRing = 8;
+constexpr int kMaxLag = 3;
+// Mixed sweeps decide convergence this many sweeps late (0: a team barrier after every sweep).
+#ifndef UFE_MIXED_LAG
+#define UFE_MIXED_LAG 1
+#endif
+constexpr int kMixedLag = UFE_MIXED_LAG;
+static_assert(kMixedLag >= 0 && kMixedLag <= kMaxLag, "lag out of range");
 // Largest shared-memory mirror of a patch's rows (the rest of the 228 KB of an SM stays L1).
 constexpr size_t kLocalRowsMaxBytes = 160 * 1024;
 constexpr int kMaxKrylovRestart = 1000;   // largest GMRES restart length of the VJP
@@ -691,6 +705,7 @@ __device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &
         if (ns < 64) ns <<= 1;
         v = ld_acquire_u32(q);
         if ((int)(v - target) >= 0) break;
+        if (*(volatile unsigned int *)team_bar & kBarrierError) break;   // another CTA failed
         if ((long long)(globaltimer_ns() - t0) > a.timeout_ns) {
           atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
           atomicOr(team_bar, kBarrierError);
@@ -700,6 +715,75 @@ __device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &
     }
   }
   __syncthreads();
+}
+
+// Lagged decisions (mixed sweeps). After its colour phases each CTA folds its maximum |res|
+// into the ring slot of sweep G (one atomicMax of a key that carries the sweep, so a slot needs
+// no reset) and counts itself in with a release; a CTA reads sweep G's maximum once the slot's
+// count says every CTA of the team is in. The residual travels as FP32 rounded up, so a
+// decision can only come later, never earlier, than the FP64 value would give.
+__device__ __forceinline__ void lag_arrive(SsaCtl *ctl, unsigned int G, unsigned long long mx_bits) {
+  __shared__ unsigned long long s_w[32];
+  unsigned long long v = warp_max_u64(mx_bits);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) s_w[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0ull;
+    x = warp_max_u64(x);
+    if (l == 0) {
+      const float r = __double2float_ru(__longlong_as_double((long long)x));
+      const unsigned long long key = ((unsigned long long)(G + 1u) << 32) | (unsigned long long)__float_as_uint(r);
+      atomicMax(&ctl->lag_res[G % kLagRing], key);
+      red_release_add_u32(&ctl->lag_cnt[G % kLagRing], 1u);   // orders the atomicMax before the count
+    }
+  }
+}
+
+// Sweep G's maximum |res| for the whole block. Bounded wait; false when it ran out, when the
+// team's error bit is set, or when the slot already holds a later sweep (cannot happen with
+// lag <= kMaxLag).
+template <class Team>
+__device__ __forceinline__ bool lag_residual(const SsaArgs &a, const Team &t, unsigned int G, double &res) {
+  __shared__ double s_res;
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    const unsigned int slot = G % kLagRing;
+    const unsigned int target = (unsigned)t.size() * (G / kLagRing + 1u);
+    const unsigned int *cnt = &a.ctl->lag_cnt[slot];
+    unsigned int v = ld_acquire_u32(cnt);
+    int ok = 1;
+    if ((int)(v - target) < 0) {
+      const unsigned long long t0 = globaltimer_ns();
+      unsigned int ns = 16;
+      for (;;) {
+        __nanosleep(ns);
+        if (ns < 64) ns <<= 1;
+        v = ld_acquire_u32(cnt);
+        if ((int)(v - target) >= 0) break;
+        if (*(volatile unsigned int *)t.bar() & kBarrierError) { ok = 0; break; }
+        if ((long long)(globaltimer_ns() - t0) > a.timeout_ns) {
+          atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
+          atomicOr(t.bar(), kBarrierError);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    if (ok) {
+      const unsigned long long key = *(volatile unsigned long long *)&a.ctl->lag_res[slot];
+      if ((unsigned int)(key >> 32) != G + 1u) {
+        atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
+        atomicOr(t.bar(), kBarrierError);
+        ok = 0;
+      }
+      s_res = (double)__uint_as_float((unsigned int)key);
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  res = s_res;
+  return s_ok != 0;
 }
 
 // Patch b's slice table, edge range and synchronisation set into shared memory.
@@ -748,6 +832,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
   double *N = a.Na, *Nprev = a.Nb;
   int did_reset_before = 0;
   int it = 0;
+  unsigned int gsweep = 0;   // sweeps of this launch (the lagged decisions' ring index)
   bool picard_done = false;
 #define UFE_GRID_SYNC()                                   \
   if (!team_barrier(t, &ctl->err, a.timeout_ns)) {        \
@@ -777,6 +862,73 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
     bool lin_done = false;
     int did_reset = 0;
     double maxres = 0.0;
+    if constexpr (kM && kMixedLag > 0) {
+      // Mixed sweeps with lagged decisions: the boundary phase is a counted phase and the next
+      // sweep's first colour waits for the neighbours' boundary rows, so no team barrier
+      // separates sweeps; sweep j's residual decides at the end of sweep j + lag (every CTA
+      // reads the same value, so every CTA takes the same decision and does the same
+      // sweeps). Refolds and the last allowed sweep are barriers, where the sweeps not yet
+      // decided are decided in order.
+      bool synced = true;        // a team barrier follows the previous phases of this CTA
+      int decided = 0;           // sweeps of this linear solve already decided
+      const unsigned int base = gsweep;
+      while (!lin_done && sweeps < a.max_inner) {
+        ++sweeps;
+        const unsigned int G = gsweep++;
+        unsigned long long mx = 0ull;
+        for (int g = 0; g < 5; ++g) {
+          if (g > 0 || !synced) wait_neighbours(a, ps, phases, t.bar());
+          const unsigned long long m = phase_sweep32(a, ps, g, lc);
+          mx = m > mx ? m : mx;
+          ++phases;
+          publish_progress(a, t, phases);
+        }
+        lag_arrive(ctl, G, mx);
+        wait_neighbours(a, ps, phases, t.bar());
+        phase_boundary<kM>(a, ps, lc);
+        ++phases;
+        publish_progress(a, t, phases);
+        synced = false;
+        const bool refold_now = a.refold > 0 && sweeps % a.refold == 0;
+        const bool sync_point = sweeps == a.max_inner || refold_now;
+        if (sync_point) {
+          UFE_GRID_SYNC();
+          synced = true;
+        }
+        const int upto = sync_point ? sweeps : sweeps - kMixedLag;
+        int act = 0;             // 1: converged, 2: diverged
+        while (decided < upto && act == 0) {
+          ++decided;
+          double r;
+          if (!lag_residual(a, t, base + (unsigned)(decided - 1), r)) {
+            if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu;
+            return false;
+          }
+          maxres = r;
+          if (r < a.tol) act = 1;
+          else if (r > 1e6) act = 2;
+        }
+        if (act == 1) {
+          lin_done = true;
+        } else if (act == 2) {
+          if (!synced) { UFE_GRID_SYNC(); synced = true; }
+          phase_zero_velocity(a, t, kM);
+          UFE_GRID_SYNC();
+          reload();
+          did_reset = 1;
+          lin_done = true;
+        } else if (sweeps == a.max_inner) {
+          if (leader) ctl->not_converged += 1;
+        } else if (refold_now) {
+          phase_fold(a, t);
+          UFE_GRID_SYNC();
+          reload();
+          phase_defect(a, t);
+          UFE_GRID_SYNC();
+        }
+      }
+      if (!synced) UFE_GRID_SYNC();
+    } else
     while (!lin_done && sweeps < a.max_inner) {
       ++sweeps;
       const int slot = sweeps % 3;
