@@ -106,3 +106,14 @@ def test_batch_entry_points_validate_arguments():
     assert L.ufe_batch_run(None, ct.byref(ps), None, None) == nat.UFE_BAD_ARG
     assert L.ufe_batch_upload(None, 0, ct.byref(ps), None, None) == nat.UFE_BAD_ARG
     assert L.ufe_batch_destroy(None) == nat.UFE_BAD_ARG
+
+
+def test_ssa_buffer_helpers():
+    from ufemism_gb300 import api
+    b = api.ssa_buffers(10, 30, 40)
+    assert set(b) == set(api.SSA_INOUT_FIELDS + api.SSA_OUT_FIELDS)
+    assert b["U_SSA"].shape == (10,) and b["Up_SSA_Ac"].shape == (30,) and b["N_AaAc"].shape == (40,)
+    api._check_buffers(b, 10, 30, 40)
+    for bad in (np.zeros(10, dtype=np.float32), np.zeros(11), np.zeros(20)[::2]):
+        with pytest.raises(ValueError):
+            api._check_buffers(dict(b, U_SSA=bad), 10, 30, 40)

@@ -187,3 +187,22 @@ def test_batch_with_early_out_member_and_coulomb_gl_members():
                 assert rel_l2(outs[i][k], o1[k]) <= TOL, (i, k)
     finally:
         b.close()
+
+
+def test_batch_into_reused_host_buffers(ensemble):
+    """upload/download with per-member host buffers (warm start read in place, results written
+    in place) give the members' single solves, twice from a reset of the same arrays."""
+    single = single_results(ensemble, nat.UFE_MIXED)
+    b = api.Batch([m for _, m, _ in ensemble])
+    p = api.default_params(precision=nat.UFE_MIXED, sliding_law=nat.UFE_SLIDING_LINEAR)
+    bufs = [api.ssa_buffers(base.nV, mesh.nAc, mesh.nVAaAc) for base, mesh, _ in ensemble]
+    for _ in range(2):
+        for i, (_, _, ssa) in enumerate(ensemble):
+            for k in api.SSA_INOUT_FIELDS:
+                bufs[i][k].fill(0.0)
+            b.upload(i, ssa, p, buffers=bufs[i])
+        rc, stats, timing = b.run(p)
+        outs = [b.download(i, buffers=bufs[i]) for i in range(b.n)]
+        assert all(o is bb for o, bb in zip(outs, bufs))
+        check_members(single, stats, outs)
+    b.close()

@@ -267,3 +267,24 @@ def test_full_size_mixed_vs_fp64_and_convergence():
     ur = (o64["U_SSA"][sel] * x[sel] + o64["V_SSA"][sel] * y[sel]) / r[sel]
     assert np.all(ur > 0)
     dm.close()
+
+
+def test_solve_into_reused_host_buffers():
+    """solve_ssa(buffers=...) reads the warm start from the caller's arrays and writes every
+    result into them in place; the same solve as the allocating form, repeated from a reset."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m)
+    dm = device_mesh("1k")
+    p = api.default_params(precision=nat.UFE_MIXED)
+    rc1, o1, s1 = dm.solve_ssa(ssa, p)
+    bufs = dm.ssa_buffers()
+    keep = {k: bufs[k] for k in bufs}
+    for _ in range(2):
+        for k in api.SSA_INOUT_FIELDS:
+            bufs[k].fill(0.0)
+        rc2, o2, s2 = dm.solve_ssa(ssa, p, buffers=bufs)
+        assert rc2 == rc1 and s2["sweeps"] == s1["sweeps"]
+        for k in api.SSA_INOUT_FIELDS + api.SSA_OUT_FIELDS:
+            assert o2[k] is keep[k] and np.array_equal(o2[k], o1[k]), k
+    with pytest.raises(ValueError):
+        dm.solve_ssa(ssa, p, buffers=dict(bufs, U_SSA=np.zeros(3)))

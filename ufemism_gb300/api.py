@@ -118,7 +118,7 @@ def _mesh_desc(mesh):
     return d, k
 
 
-def _ssa_structs(nV, nAc, nA, fields: dict, warm: dict | None):
+def _ssa_in(fields: dict):
     keep = {}
 
     def g(k, dt=np.float64):
@@ -130,7 +130,41 @@ def _ssa_structs(nV, nAc, nA, fields: dict, warm: dict | None):
         return a.ctypes.data
 
     ints = ("mask_sheet", "mask_gl_Ac")
-    si = nat.SsaIn(*(g(k, np.int32 if k in ints else np.float64) for k in nat.SSA_IN_FIELDS))
+    return nat.SsaIn(*(g(k, np.int32 if k in ints else np.float64) for k in nat.SSA_IN_FIELDS)), keep
+
+
+SSA_INOUT_FIELDS = ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac", "N_AaAc")
+SSA_OUT_FIELDS = ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")
+
+
+def _ssa_sizes(nV, nAc, nA) -> dict:
+    sizes = {k: nA for k in SSA_INOUT_FIELDS + SSA_OUT_FIELDS}
+    sizes.update(U_SSA=nV, V_SSA=nV, Ux_SSA_Ac=nAc, Uy_SSA_Ac=nAc, Up_SSA_Ac=nAc, Uo_SSA_Ac=nAc)
+    return sizes
+
+
+def ssa_buffers(nV, nAc, nA) -> dict:
+    """Host arrays for the buffers= forms, zero (a cold start): the warm start that a solve
+    overwrites with its solution (U_SSA, V_SSA, Ux_SSA_Ac, Uy_SSA_Ac, N_AaAc) and the other
+    outputs — the model's own state arrays, kept across time steps."""
+    return {k: np.zeros(n) for k, n in _ssa_sizes(nV, nAc, nA).items()}
+
+
+def _check_buffers(buffers: dict, nV, nAc, nA):
+    for k, n in _ssa_sizes(nV, nAc, nA).items():
+        b = buffers.get(k)
+        if not (isinstance(b, np.ndarray) and b.dtype == np.float64 and b.flags.c_contiguous and b.shape == (n,)):
+            raise ValueError("buffers[%r] must be a contiguous float64 array of %d" % (k, n))
+
+
+def _buffer_structs(buffers: dict):
+    sio = nat.SsaInout(*(buffers[k].ctypes.data for k in SSA_INOUT_FIELDS))
+    so = nat.SsaOut(*(buffers[k].ctypes.data for k in SSA_OUT_FIELDS))
+    return sio, so
+
+
+def _ssa_structs(nV, nAc, nA, fields: dict, warm: dict | None):
+    si, keep = _ssa_in(fields)
     warm = warm or {}
     io = {}
     for k, n in (("U_SSA", nV), ("V_SSA", nV), ("Ux_SSA_Ac", nAc), ("Uy_SSA_Ac", nAc)):
@@ -187,16 +221,31 @@ class DeviceMesh:
     def _ssa_structs(self, fields: dict, warm: dict | None):
         return _ssa_structs(self.nV, self.nAc, self.nVAaAc, fields, warm)
 
-    def solve_ssa(self, fields: dict, params: dict, warm: dict | None = None, check: bool = True):
+    def ssa_buffers(self) -> dict:
+        """Zeroed host arrays for solve_ssa(buffers=...) (see the module's ssa_buffers)."""
+        return ssa_buffers(self.nV, self.nAc, self.nVAaAc)
+
+    def solve_ssa(self, fields: dict, params: dict, warm: dict | None = None, check: bool = True,
+                  buffers: dict | None = None):
         """solve_SSA. Returns (status, outputs, stats). Outputs hold the solution U_SSA, V_SSA,
         Ux_SSA_Ac, Uy_SSA_Ac, N_AaAc and Up_SSA_Ac, Uo_SSA_Ac, eta_AaAc, S_AaAc, tau_c_AaAc,
-        phi_fric_AaAc."""
+        phi_fric_AaAc. With ``buffers`` (see ssa_buffers) the warm start is read from those
+        arrays and every result written into them in place, with no allocation; the returned
+        outputs are the same arrays."""
         L = nat.load()
-        si, sio, io, keep = self._ssa_structs(fields, warm)
-        out = {k: np.zeros(self.nAc) for k in ("Up_SSA_Ac", "Uo_SSA_Ac")}
-        out.update({k: np.zeros(self.nVAaAc) for k in ("eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")})
-        so = nat.SsaOut(*(out[k].ctypes.data for k in ("Up_SSA_Ac", "Uo_SSA_Ac", "eta_AaAc", "S_AaAc",
-                                                        "tau_c_AaAc", "phi_fric_AaAc")))
+        if buffers is None:
+            si, sio, io, keep = self._ssa_structs(fields, warm)
+            out = {k: np.zeros(self.nAc) for k in ("Up_SSA_Ac", "Uo_SSA_Ac")}
+            out.update({k: np.zeros(self.nVAaAc) for k in ("eta_AaAc", "S_AaAc", "tau_c_AaAc", "phi_fric_AaAc")})
+        else:
+            if warm is not None:
+                raise ValueError("with buffers the warm start is the buffers' content")
+            _check_buffers(buffers, self.nV, self.nAc, self.nVAaAc)
+            si, keep = _ssa_in(fields)
+            io = {k: buffers[k] for k in SSA_INOUT_FIELDS}
+            out = {k: buffers[k] for k in SSA_OUT_FIELDS}
+        sio = nat.SsaInout(*(io[k].ctypes.data for k in SSA_INOUT_FIELDS))
+        so = nat.SsaOut(*(out[k].ctypes.data for k in SSA_OUT_FIELDS))
         ps, _z = _params_struct(params)
         st = nat.SsaStats()
         rc = L.ufe_ssa_solve(self._h, ct.byref(ps), ct.byref(si), ct.byref(sio), ct.byref(so), ct.byref(st))
@@ -489,9 +538,18 @@ class Batch:
         self._h = h
         self.n = n
 
-    def upload(self, i: int, fields: dict, params: dict, warm: dict | None = None):
+    def upload(self, i: int, fields: dict, params: dict, warm: dict | None = None, buffers: dict | None = None):
+        """Member i's inputs; the warm start from ``warm`` or, in place, from ``buffers``
+        (see ssa_buffers)."""
         L = nat.load()
-        si, sio, io, keep = _ssa_structs(*self.sizes[i], fields, warm)
+        if buffers is None:
+            si, sio, io, keep = _ssa_structs(*self.sizes[i], fields, warm)
+        else:
+            if warm is not None:
+                raise ValueError("with buffers the warm start is the buffers' content")
+            _check_buffers(buffers, *self.sizes[i])
+            si, keep = _ssa_in(fields)
+            sio, _ = _buffer_structs(buffers)
         ps, _z = _params_struct(params)
         rc = L.ufe_batch_upload(self._h, i, ct.byref(ps), ct.byref(si), ct.byref(sio))
         if rc != nat.UFE_OK:
@@ -512,9 +570,15 @@ class Batch:
         timing["member_ms"] = member_ms
         return rc, [stats_dict(s) for s in st], timing
 
-    def download(self, i: int) -> dict:
+    def download(self, i: int, buffers: dict | None = None) -> dict:
+        """Member i's results, into new arrays or in place into ``buffers``."""
         L = nat.load()
-        io, sio, so = _download_structs(*self.sizes[i])
+        if buffers is None:
+            io, sio, so = _download_structs(*self.sizes[i])
+        else:
+            _check_buffers(buffers, *self.sizes[i])
+            io = buffers
+            sio, so = _buffer_structs(buffers)
         rc = L.ufe_batch_download(self._h, i, ct.byref(sio), ct.byref(so))
         if rc != nat.UFE_OK:
             raise nat.UfeError(rc, "ufe_batch_download")
