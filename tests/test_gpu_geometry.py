@@ -308,3 +308,38 @@ def test_upwind_derivatives_of_the_device_step():
     assert np.array_equal(gx, hx) and np.array_equal(gy, hy) and gm == hm
     assert np.count_nonzero(gx) > 0
     dm.close()
+
+
+def test_halfar_time_loop_on_the_device():
+    """The Halfar benchmark stepped on the device — geometry preparation, the SIA on the device
+    geometry, the thickness update taking the SIA velocities from the device — against the same
+    loop of the oracle (CUDA's pow in the SIA against the C library's: 1e-10 after 200 steps)."""
+    from test_oracle_halfar import halfar
+    m = oracle_aaac("4k")
+    base = m.base
+    x, y = base.V[:, 0], base.V[:, 1]
+    dt, steps = 2.0, 200
+    H0 = halfar(3000.0, 500e3, x, y, 0.0)
+    Hb, SL = np.zeros(base.nV), np.zeros(base.nV)
+    Aw, Cw = wl.areas_and_widths(base)
+    A = np.full((m.nAc, 15), 1e-16, order="F")
+    zac, zv = np.zeros(m.nAc), np.zeros(base.nV)
+    p = api.default_params()
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    Hd = H0.copy()
+    for _ in range(steps):
+        dm.geometry_update(Hd, Hb, SL)
+        dm.solve_sia_geometry(A, p)
+        Hd = dm.thickness_update(Hd, Aw, Cw, zv, zv, dt, Up_SSA_Ac=zac)[0]
+    dm.close()
+    Ho = H0.copy()
+    po = orc.default_params()
+    for _ in range(steps):
+        g = orc.update_geometry(m, Ho, Hb, SL)
+        sia = dict(mask_sheet_Ac=g["mask_sheet_Ac"], Hi_Ac=g["Hi_Ac"], dHs_dx_Ac=g["dHs_dx_Ac"],
+                   dHs_dy_Ac=g["dHs_dy_Ac"], dHs_dp_Ac=g["dHs_dp_Ac"], dHs_do_Ac=g["dHs_do_Ac"], A_flow_Ac=A)
+        up = orc.solve_sia(m, sia, po)["Up_SIA_Ac"]
+        Ho = orc.thickness_change(m, Aw, Cw, up, zac, zv, zv, dt, Ho)[0]
+    assert rel_l2(Hd, Ho) <= 1e-10
+    assert abs(np.sum(Aw * Hd) / np.sum(Aw * H0) - 1.0) < 1e-12
