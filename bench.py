@@ -34,7 +34,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "SSA solves/s mixed vs FP64 on GB300 @ rel-L2<=1e-6; sweep HBM GB/s; adjoint ms"
 UNIT = "solves/s"
-WORKLOAD = "200k-vertex dome SSA cold-start solve"
+WORKLOAD = "%s-vertex dome SSA cold-start solve"   # formatted with the mesh size (default 200k)
 
 
 def dist_info():
@@ -242,7 +242,7 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dome geometry and mesh)",
-        "config": {"workload": WORKLOAD, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc), "precision": "fp64",
+        "config": {"workload": WORKLOAD % args.size, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc), "precision": "fp64",
                    "l2": "n/a (CPU)"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
@@ -756,7 +756,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 sweeps / f64 defect", "data": "synthetic (seeded dome geometry and mesh)",
-        "config": {"workload": WORKLOAD, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc),
+        "config": {"workload": WORKLOAD % args.size, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc),
                    "nnz": counts["nnz_all"], "precision": "mixed", "sliding": "linear beta^2=1e3",
                    "picard_iterations": st32["picard_iterations"], "sor_sweeps": st32["total_sweeps"],
                    "l2": "inputs and coefficient arrays (> 300 MB) larger than L2; no flush",
