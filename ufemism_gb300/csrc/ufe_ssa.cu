@@ -26,7 +26,10 @@
 // in exact arithmetic, and the residual the sweep tests against SSA_max_residual_UV is that
 // of the FP64 iteration; FP32 rounding is relative to |d|, not |u|. Every `refold` sweeps
 // d is folded into u0 and the defect recomputed in FP64. The viscosity uses FP32 arithmetic
-// on FP64 differences u_j - u_i. Convergence norms (RN, max residual) are FP64.
+// on FP64 differences u_j - u_i. Convergence norms (RN, max residual) are FP64. The mixed
+// sweeps have no team barrier between sweeps: a sweep's maximum residual is read one sweep
+// later from a ring of per-sweep slots (lag_arrive / lag_residual), so a converged linear
+// solve ends one sweep after the sweep that met the tolerance.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -690,7 +693,8 @@ __device__ __forceinline__ void publish_progress(const Args &a, const Team &t, u
 }
 
 // Wait until every patch this patch synchronises with has completed `target` colour phases.
-// Bounded: after timeout_ns the CTA records UFE_TIMEOUT (the next grid barrier then fails).
+// Bounded: after timeout_ns the CTA records UFE_TIMEOUT and sets the team's error bit, which
+// ends every other wait of the team (and the next team barrier or lagged decision fails).
 template <class Args>
 __device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &ps, unsigned int target,
                                                 unsigned int *team_bar) {
