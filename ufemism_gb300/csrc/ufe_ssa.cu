@@ -1629,6 +1629,19 @@ __global__ void k_scatter(int nA, int nV, const int *dev_of_orig, const double2 
 // ---------------------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------------------
+
+// Limit of every device-side bounded wait (team barriers, neighbour progress waits, lagged
+// decisions): 20 s, or the positive integer in UFE_WAIT_TIMEOUT_NS. The tests set a few
+// nanoseconds to make the waits run out and check that the solve reports UFE_TIMEOUT and the
+// context stays usable; nothing else should set it.
+long long wait_timeout_ns() {
+  const char *env = std::getenv("UFE_WAIT_TIMEOUT_NS");
+  if (env && *env) {
+    const long long v = std::atoll(env);
+    if (v > 0) return v;
+  }
+  return 20LL * 1000 * 1000 * 1000;
+}
 struct SsaWork {
   int nP = 0, nV = 0, nAc = 0, nA = 0;
   // staging (original order)
@@ -1902,7 +1915,7 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->sliding_law = p->sliding_law; a->has_beta = w->has_beta;
   a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 32;
   a->fp32_visc = p->mixed_fp32_viscosity != 0;
-  a->timeout_ns = 20LL * 1000 * 1000 * 1000;
+  a->timeout_ns = wait_timeout_ns();
   return rc;
 }
 
@@ -2363,7 +2376,7 @@ int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
     ba.members = b->args_dev; ba.n_members = n_active;
     ba.team_of_cta = tcd; ba.team_info = tid; ba.class_range = reinterpret_cast<const int2 *>(tid + b->n_teams);
     ba.queue = queue; ba.team_bar = team_bar; ba.team_member = team_member;
-    ba.times = b->times_dev; ba.err = b->err_dev; ba.timeout_ns = 20LL * 1000 * 1000 * 1000;
+    ba.times = b->times_dev; ba.err = b->err_dev; ba.timeout_ns = wait_timeout_ns();
     if (!rc) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)pl.grid_ctas);
@@ -2987,7 +3000,7 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   aa.patch_slice = m.patch_slice; aa.patch_edge0 = m.patch_edge0; aa.sync_ptr = m.sync_ptr; aa.sync_list = m.sync_list;
   aa.prog = a->prog; aa.cT = a->cT; aa.kT = a->kT; aa.ee = a->ee; aa.c3 = a->c3; aa.kh = a->kh; aa.alpha = a->alpha;
   aa.dinv = a->dinv; aa.g = a->g; aa.mu = a->mu; aa.s = a->s; aa.ctl = a->ctl; aa.omega = omega; aa.tol = tol;
-  aa.max_sweeps = max_sweeps; aa.timeout_ns = 20LL * 1000 * 1000 * 1000;
+  aa.max_sweeps = max_sweeps; aa.timeout_ns = wait_timeout_ns();
   const bool krylov = !vp || vp->method == UFE_VJP_GMRES;
   int k_iters = 0, k_err = 0;
   double k_rel = 0.0;
