@@ -28,7 +28,7 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(_LIB) or any(
             os.path.getmtime(os.path.join(_HERE, f)) > os.path.getmtime(_LIB)
             for f in ("ufe_oracle_mesh.c", "ufe_oracle_solve.c", "ufe_oracle_thickness.c", "ufe_oracle_sia3d.c",
-                      "ufe_oracle_physprop.c", "ufe_oracle_upwind.c", "ufe_oracle.h")):
+                      "ufe_oracle_physprop.c", "ufe_oracle_upwind.c", "ufe_oracle_masks.c", "ufe_oracle.h")):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
 
@@ -424,3 +424,28 @@ def upwind_derivatives_3d(m: AaAcMesh, R, NxTri, NyTri, U, V, d):
     f.restype = ct.c_longlong
     missing = f(ct.byref(bs), ct.byref(ms), ct.c_int(nZ), *(_vp(k) for k in keep), _vp(ddx), _vp(ddy))
     return ddx, ddy, int(missing)
+
+
+MASK_NAMES = ("land", "ocean", "lake", "ice", "sheet", "shelf", "coast", "margin", "gl", "cf", "type")
+
+
+def determine_masks(m: AaAcMesh, Hi, Hb, SL) -> dict:
+    """determine_masks in full: mask_<name> (nV) and mask_<name>_Ac (nAc) for every name of
+    MASK_NAMES, "type" being the combined type mask."""
+    base = m.base
+    nV, nAc = base.nV, m.nAc
+    keep = [_f64(Hi), _f64(Hb), _f64(SL)]
+    ac_in = [np.zeros(nAc) for _ in range(3)]
+    for a, o in zip(keep, ac_in):
+        lib().or_map_Aa_to_Ac(ct.byref(_aaac_struct(m)), ct.c_int(nV), _vp(a), _vp(o))
+    aa = np.zeros((nV, len(MASK_NAMES)), dtype=np.int32, order="F")
+    ac = np.zeros((nAc, len(MASK_NAMES)), dtype=np.int32, order="F")
+    bs, bkeep = _base_struct(base)
+    ms = _aaac_struct(m)
+    lib().or_determine_masks(ct.byref(bs), ct.byref(ms), *(_vp(a) for a in keep), *(_vp(a) for a in ac_in),
+                             _vp(aa), _vp(ac))
+    out = {}
+    for k, name in enumerate(MASK_NAMES):
+        out["mask_" + name] = aa[:, k].copy()
+        out["mask_" + name + "_Ac"] = ac[:, k].copy()
+    return out

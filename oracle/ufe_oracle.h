@@ -222,6 +222,17 @@ long long or_upwind_derivatives_3d(const or_base *b, const or_aaac *m, int nZ, c
                                    const double *NyTri, const double *U, const double *V, const double *d,
                                    double *ddx, double *ddy);
 
+/* determine_masks in full (general_ice_model_data_module.f90:97-297). aa is (nV, OR_MASK_COUNT)
+ * and ac (nAc, OR_MASK_COUNT), column-major, columns in the order below; the TYPE column holds
+ * the combined type (0 land, 1 ocean, 2 lake, 3 sheet, 4 shelf, 5 coast, 6 margin, 7 grounding
+ * line, 8 calving front). Hi_Ac, Hb_Ac, SL_Ac are the Aa-to-Ac maps of Hi, Hb, SL. */
+enum {
+  OR_MASK_LAND = 0, OR_MASK_OCEAN, OR_MASK_LAKE, OR_MASK_ICE, OR_MASK_SHEET, OR_MASK_SHELF, OR_MASK_COAST,
+  OR_MASK_MARGIN, OR_MASK_GL, OR_MASK_CF, OR_MASK_TYPE, OR_MASK_COUNT
+};
+void or_determine_masks(const or_base *b, const or_aaac *m, const double *Hi, const double *Hb, const double *SL,
+                        const double *Hi_Ac, const double *Hb_Ac, const double *SL_Ac, int32_t *aa, int32_t *ac);
+
 /* Primitive operators, for tests. */
 void or_map_Aa_to_Ac(const or_aaac *m, int nV, const double *d_Aa, double *d_Ac);
 void or_map_Ac_to_Aa(const or_base *b, const or_aaac *m, const double *d_Ac, double *d_Aa);
