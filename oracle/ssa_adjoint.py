@@ -18,6 +18,14 @@ The discrete system at convergence, per AaAc row i (0-based here):
 * edge rows: u_e - mean(u over the non-edge neighbours) = 0; corners 1..4: u_c - mean(u over
   all neighbours) = 0 (apply_Neumann_boundary_AaAc, mesh_ArakawaC_module.f90:660-724).
 
+Sliding: linear (S = beta^2, the library's extension) or the reference's Coulomb_regularised
+law (SSA_sliding_term, ice_dynamics_module.f90:727-779), S = tau_c (dv^2 + U^2 + V^2)^e / u_t^q
+with e = (q - 1)/2, q = 0.3, dv = 1e-3, u_t = 100, which depends on the row's own velocity: its
+derivative adds a 2x2 block per grounded interior row, d(fr U)/dU = fr + 2 e fr U^2 / w,
+d(fr U)/dV = 2 e fr U V / w (w = dv^2 + U^2 + V^2), and likewise for V. tau_c (basal_yield_stress,
+780-844) is proportional to max(0.1, Hi), as is the denominator of fr, so under the Coulomb law the
+friction term does not depend on the thickness.
+
 Parameters: log(beta^2) on AaAc (linear sliding S = beta^2), and the ice thickness Hi on Aa,
 which enters through Hi_AaAc (Aa rows and the Ac average, map_Aa_to_Ac) and the driving-
 stress slopes hx, hy (get_mesh_derivatives on Aa, mesh_derivatives_module.f90:315-371,
@@ -36,6 +44,9 @@ RHO_SW = 1028.0
 GRAV = 9.81
 N_FLOW = 3.0
 EPS_SQ0 = 1e-12
+Q_PLASTIC = 0.30
+DELTA_V = 1e-3
+U_THRESHOLD = 100.0
 
 
 def _rows(m):
@@ -84,8 +95,11 @@ def derivative_ops(m):
 class Linearisation:
     """Everything the Jacobian needs at one velocity state (U, V on AaAc)."""
 
-    def __init__(self, m, f, U, V, m_enh=1.0):
+    def __init__(self, m, f, U, V, m_enh=1.0, tau_c=None):
+        """tau_c (AaAc, the solve's basal yield stress) selects the Coulomb_regularised law;
+        without it the sliding is linear with f's beta^2."""
         self.m = m
+        self.tau_c = None if tau_c is None else np.asarray(tau_c, dtype=np.float64)
         nA = m.nVAaAc
         self.nA = nA
         self.g = gather_fields(m, f)
@@ -118,7 +132,11 @@ class Linearisation:
         self.eps2 = ux * ux + vy * vy + ux * vy + 0.25 * t * t + EPS_SQ0
         self.eta = self.B * self.eps2 ** self.p
         self.K1, self.K2, self.K3 = 2 * ux + vy, 0.5 * t, 2 * vy + ux
-        S = self.g["beta"]
+        if self.tau_c is None:
+            S = self.g["beta"]
+        else:
+            self.w = DELTA_V ** 2 + U * U + V * V
+            S = self.tau_c * self.w ** (0.5 * (Q_PLASTIC - 1.0)) / U_THRESHOLD ** Q_PLASTIC
         self.fr = np.where(self.floating, 0.0, S / (self.mH * self.eta))
 
     def residual(self):
@@ -182,6 +200,14 @@ class Linearisation:
         add(hi, nA + hi, 3 * self.sNxy[hi] + ax[hi] * kV_h[hi])
         add(nA + hi, hi, 3 * self.sNxy[hi] + ay[hi] * kU_h[hi])
         add(nA + hi, nA + hi, self.hcv[hi] - self.fr[hi] + ay[hi] * kV_h[hi])
+        if self.tau_c is not None:
+            # the Coulomb law's S'(u): local to the row
+            cS = (Q_PLASTIC - 1.0) * self.fr[hi] / self.w[hi]
+            Uh, Vh = U[hi], V[hi]
+            add(hi, hi, -cS * Uh * Uh)
+            add(hi, nA + hi, -cS * Uh * Vh)
+            add(nA + hi, hi, -cS * Uh * Vh)
+            add(nA + hi, nA + hi, -cS * Vh * Vh)
         # boundary rows
         Bm = self.boundary_matrix().tocoo()
         be = home[self.edge]
@@ -195,6 +221,8 @@ class Linearisation:
     # ------------------------------------------------------------ parameter derivatives
     def dF_dlogbeta(self):
         """dF/d(log beta^2) (diagonal per row): -fr U on interior grounded rows."""
+        if self.tau_c is not None:
+            raise ValueError("log(beta^2) is a parameter of the linear law only")
         interior = ~self.edge
         return np.where(interior, -self.fr * self.U, 0.0), np.where(interior, -self.fr * self.V, 0.0)
 
@@ -204,6 +232,8 @@ class Linearisation:
         rg = RHO_I * GRAV
         dhx = np.where(interior, -rg / self.eta, 0.0)
         dH = np.where(interior & (self.g["Hi"] > 0.1), self.fr / self.mH, 0.0)   # d(-fr u)/dH = fr u / H
+        if self.tau_c is not None:
+            dH = np.zeros_like(dH)     # tau_c / max(0.1, H) does not depend on H
         return dhx, dH * self.U, dH * self.V
 
 
@@ -255,14 +285,16 @@ def geometry_matrix(m, Hi, Hb, SL):
 
 
 def adjoint_gradient(lin: Linearisation, gU, gV, G=None):
-    """Solve (dF/du)^T mu = dJ/du and return (mu_U, mu_V, dJ/dlogbeta2, dJ/dHi or None,
-    field sensitivities dict)."""
+    """Solve (dF/du)^T mu = dJ/du and return (mu_U, mu_V, dJ/dlogbeta2 (None under the
+    Coulomb law), dJ/dHi or None, field sensitivities dict)."""
     nA = lin.nA
     K = lin.jacobian()
     mu = spla.spsolve(K.T.tocsc(), np.concatenate([gU, gV]))
     mx, my = mu[:nA], mu[nA:]
-    bx, by = lin.dF_dlogbeta()
-    d_logbeta = -(mx * bx + my * by)
+    d_logbeta = None                  # the Coulomb law has no log(beta^2)
+    if lin.tau_c is None:
+        bx, by = lin.dF_dlogbeta()
+        d_logbeta = -(mx * bx + my * by)
     dhx, dHx, dHy = lin.dF_dfields()
     s_hx = -mx * dhx
     s_hy = -my * dhx

@@ -91,3 +91,83 @@ def test_gradients_match_finite_differences_and_tangent_linear(problem):
         du, dv = adj.tangent_linear(lin, d_Hi=d, G=G)
         assert abs(fd - an) <= 1e-5 * abs(an)
         assert abs(float(gU @ du + gV @ dv) - an) <= 1e-10 * abs(an)
+
+
+@pytest.fixture(scope="module")
+def coulomb():
+    """The marine 1k case under the reference's Coulomb_regularised law (floating shelf rows
+    without friction), solved tightly by the oracle."""
+    m = oracle_aaac("1k")
+    ssa, sia, g = oracle_inputs(m, "marine")
+    P = orc.default_params(sliding_law=0, **TIGHT)
+
+    def solve(fields):
+        rc, out, st = orc.solve_ssa(m, fields, P)
+        assert rc == 0 and st["last_RN"] < 1e-12
+        return adj.aaac_velocity(out), out
+
+    (U, V), out = solve(ssa)
+    return m, ssa, solve, U, V, out
+
+
+def test_coulomb_jacobian_matches_finite_differences(coulomb):
+    """With the velocity-dependent sliding term S(u) of the Coulomb law, the residual vanishes at
+    the oracle's converged state and the Jacobian, S'(u) blocks included, matches central finite
+    differences of the residual. The direction lives on the grounded interior rows, scaled by
+    each row's speed plus the regularisation dv (grounded rows here run as slow as 4e-5 m/yr,
+    below dv = 1e-3, where a uniform step would see S's curvature); on it the S'(u) blocks carry
+    a third of the Jacobian's action, so leaving them out fails the comparison."""
+    m, ssa, solve, U, V, out = coulomb
+    tau = out["tau_c_AaAc"]
+    lin = adj.Linearisation(m, ssa, U, V, tau_c=tau)
+    F = lin.residual()
+    interior = np.concatenate([~lin.edge, ~lin.edge])
+    scale = np.abs(adj.RHO_I * adj.GRAV * lin.g["hx"] / lin.eta).max()
+    assert np.abs(F[interior]).max() < 1e-9 * scale                      # momentum rows
+    assert np.abs(F[~interior]).max() < 1e-12 * np.abs(np.concatenate([U, V])).max()   # Neumann rows
+    assert np.any(lin.fr > 0) and np.any(lin.floating & ~lin.edge)
+    K = lin.jacobian()
+    nA = m.nVAaAc
+    rng = np.random.default_rng(3)
+    grounded = np.concatenate([lin.fr > 0, lin.fr > 0])
+    speed = np.hypot(U, V) + adj.DELTA_V
+    h = 1e-5
+    for _ in range(2):
+        d = np.where(grounded, np.concatenate([speed, speed]) * rng.normal(size=2 * nA), 0.0)
+        Fp = adj.Linearisation(m, ssa, U + h * d[:nA], V + h * d[nA:], tau_c=tau).residual()
+        Fm = adj.Linearisation(m, ssa, U - h * d[:nA], V - h * d[nA:], tau_c=tau).residual()
+        an = K @ d
+        assert np.linalg.norm((Fp - Fm) / (2 * h) - an) / np.linalg.norm(an) < 1e-8
+    # the same friction factor treated as a constant of u (no S'(u) blocks)
+    frozen = adj.Linearisation(m, ssa, U, V, tau_c=tau)
+    frozen.tau_c = None
+    frozen.g = dict(frozen.g, beta=tau * lin.w ** (0.5 * (adj.Q_PLASTIC - 1.0)) / adj.U_THRESHOLD ** adj.Q_PLASTIC)
+    frozen.update(U, V)
+    assert np.linalg.norm((frozen.jacobian() - K) @ d) > 0.1 * np.linalg.norm(K @ d)
+
+
+def test_coulomb_thickness_gradient_matches_finite_differences(coulomb):
+    """dJ/dHi under the Coulomb law against central finite differences of the oracle's forward
+    solve, on perturbations away from the floatation and ice-free thresholds (masks frozen)."""
+    m, ssa, solve, U, V, out = coulomb
+    H = np.asarray(ssa["Hi"], dtype=np.float64)
+    Hb, SL = ssa["Hb"], ssa["SL"]
+    rng = np.random.default_rng(12)
+    x, y = m.base.V[:, 0], m.base.V[:, 1]
+    bump = 20.0 * np.exp(-((x - 2e5) ** 2 + (y + 1e5) ** 2) / (2 * (1.5e5) ** 2))
+    (Uo, Vo), _ = solve(fields_for(m, ssa, np.where(H > 0, H + bump, H))[0])
+    lin = adj.Linearisation(m, ssa, U, V, tau_c=out["tau_c_AaAc"])
+    G = adj.geometry_matrix(m, H, Hb, SL)
+    gU, gV = U - Uo, V - Vo
+    mx, my, dlb, dHi, sens = adj.adjoint_gradient(lin, gU, gV, G)
+    assert dlb is None
+    flot = (SL - Hb) * adj.RHO_SW / adj.RHO_I
+    safe = (H > 50.0) & (np.abs(H - flot) > 50.0)
+    h = 1e-2
+    for _ in range(2):
+        d = np.where(safe, rng.normal(size=H.size), 0.0)
+        (Up, Vp), _ = solve(fields_for(m, ssa, H + h * d)[0])
+        (Um, Vm), _ = solve(fields_for(m, ssa, H - h * d)[0])
+        fd = (adj.misfit(Up, Vp, Uo, Vo) - adj.misfit(Um, Vm, Uo, Vo)) / (2 * h)
+        an = float(dHi @ d)
+        assert abs(fd - an) <= 1e-5 * abs(an), (fd, an)
