@@ -13,8 +13,11 @@ reference's stopping rules fire).
   roofline  the persistent SSA kernel: algorithmic bytes per launch / launch time vs HBM peak
 
 ``--impl reference`` times the reference algorithm on the host cores: the CPU oracle (a C
-restatement of the Fortran routines; the Fortran reference cannot be built on this image),
-on a bounded sample of the same solve, extrapolated to solves/s.
+restatement of the Fortran routines; the Fortran reference cannot be built on this image) runs
+full cold-start solves of the same workload, which it builds itself (mesh, neighbour functions,
+colouring, geometry) without loading this library. The K timed steps are K consecutive pieces
+(by SOR sweep count) of one full solve, so together they are exactly one solve and the value
+is measured, not extrapolated; the warm-up is one full solve before it.
 """
 from __future__ import annotations
 
@@ -25,6 +28,7 @@ import statistics
 import subprocess
 import sys
 import tempfile
+import threading
 import time
 
 import numpy as np
@@ -157,11 +161,16 @@ class ClockSampler:
         return out
 
 
+L2_FLUSH_BYTES = 256 << 20   # twice the GB300's L2
+
+
 def timed_runs(dm, params, steps, warmup, stream_ptr):
     """Device-resident solves: ufe_ssa_run on the uploaded inputs, timed with CUDA events
-    recorded on the handle's stream. Returns per-step ms and the stats of the last run."""
+    recorded on the handle's stream, with L2 flushed (a 256 MB write on the same stream)
+    before every timed step. Returns per-step ms and the stats of the last run."""
     import torch
     stream = torch.cuda.ExternalStream(stream_ptr)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
     st = None
     for _ in range(warmup):
         rc, st = dm.ssa_run(params)
@@ -170,6 +179,8 @@ def timed_runs(dm, params, steps, warmup, stream_ptr):
     for _ in range(steps):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
         e0.record(stream)
         rc, st = dm.ssa_run(params)
         e1.record(stream)
@@ -179,76 +190,107 @@ def timed_runs(dm, params, steps, warmup, stream_ptr):
     return times, st
 
 
-def cpu_baseline(mesh, ssa, gpu_stats, sample_sweeps=120, threads=None):
-    """The oracle (C restatement of the reference's FP64 solve) on the host cores: one
-    viscosity update and ``sample_sweeps`` SOR sweeps of the same workload (replay mode),
-    extrapolated with the full solve's sweep and Picard counts."""
+def oracle_workload(size: str):
+    """The benchmark workload built by the oracle alone: the seeded base mesh, the oracle's Ac
+    mesh, neighbour functions and five-colouring, and the geometry of
+    update_general_ice_model_data from its restatement. This library is not loaded."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
+    from ufemism_gb300 import workloads
+    from ufemism_gb300.meshgen import dome_mesh
+    base = dome_mesh(size)
+    om = orc.build_aaac(base)
+    Hi, Hb, SL = workloads.dome_geometry(base)
+    g = orc.update_geometry(om, Hi, Hb, SL)
+    A = workloads.A_FLOW
+    ssa = dict(Hi=Hi, Hb=Hb, SL=SL, dHs_dx_shelf=g["dHs_dx_shelf"], dHs_dy_shelf=g["dHs_dy_shelf"],
+               A_flow_mean=np.full(base.nV, A), mask_sheet=g["mask_sheet"], Hi_Ac=g["Hi_Ac"], Hb_Ac=g["Hb_Ac"],
+               SL_Ac=g["SL_Ac"], dHs_dx_shelf_Ac=g["dHs_dx_shelf_Ac"], dHs_dy_shelf_Ac=g["dHs_dy_shelf_Ac"],
+               A_flow_mean_Ac=np.full(om.nAc, A))
+    return orc, base, om, ssa
+
+
+def oracle_solve_timed(orc, om, ssa, threads, pieces=1, total_sweeps=None):
+    """One full cold-start FP64 solve by the oracle on ``threads`` host threads (OpenMP over
+    the rows of one colour, the reference's own per-colour decomposition), timed on the host.
+    With ``pieces`` > 1 and the solve's sweep count known, the solve is also timed in that
+    many consecutive pieces of equal sweep count: the oracle publishes its running sweep
+    total after every sweep, and a watcher thread stamps each boundary as it is crossed.
+    Returns (rc, outputs, stats, seconds, per-piece seconds)."""
+    prog = np.zeros(1, dtype=np.int64)
+    p = orc.default_params(n_threads=threads, progress=prog)
+    res = {}
+    th = threading.Thread(target=lambda: res.setdefault("r", orc.solve_ssa(om, ssa, p)))
+    marks = []
+    t0 = time.perf_counter()
+    th.start()
+    if pieces > 1 and total_sweeps:
+        for i in range(1, pieces):
+            target = (i * total_sweeps) // pieces
+            while th.is_alive() and int(prog[0]) < target:
+                time.sleep(2e-4)
+            marks.append(time.perf_counter())
+    th.join()
+    t1 = time.perf_counter()
+    marks.append(t1)
+    rc, out, st = res["r"]
+    return rc, out, st, t1 - t0, np.diff(np.array([t0] + marks))
+
+
+def workload_config(size, base, nVAaAc, nnz):
+    """The config keys both arms report: what the workload is, not how an arm runs it."""
+    return {"workload": WORKLOAD % size, "nV": int(base.nV), "nVAaAc": int(nVAaAc), "nnz": int(nnz),
+            "geometry": "Vialov dome H0 3600 m, R 750 km, flat bed, grounded",
+            "sliding": "linear beta^2=1e3", "A_flow": 1e-16,
+            "solver": "cold start; Picard tol 1e-3 (<= 50); SOR omega 1.3, tol 1e-4 m/yr (<= 10000 sweeps)",
+            "l2": "GPU arm: L2 flushed (256 MB write) before every timed step"}
+
+
+def cpu_baseline(size, threads=None):
+    """The oracle (C restatement of the reference's FP64 solve) on the host cores: one full
+    cold-start solve of the same workload, on a mesh and inputs it builds itself, timed
+    directly (no extrapolation). Also returns its solution, the checker of the GPU results."""
     threads = threads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    om = orc.build_aaac(mesh.base)
-    t_mesh = time.perf_counter() - t0
-    p1 = orc.default_params(n_threads=threads, replay_picard=1)
-    t0 = time.perf_counter()
-    orc.solve_ssa(om, ssa, p1)
-    t_visc = time.perf_counter() - t0
-    p2 = orc.default_params(n_threads=threads, replay_picard=2,
-                            replay_sweeps=np.array([sample_sweeps, 0], dtype=np.int32))
-    t0 = time.perf_counter()
-    orc.solve_ssa(om, ssa, p2)
-    t_two = time.perf_counter() - t0
-    t_sweep = max(t_two - 2 * t_visc, 1e-9) / sample_sweeps
-    full = gpu_stats["total_sweeps"] * t_sweep + gpu_stats["picard_iterations"] * t_visc
-    return dict(value=1.0 / full, unit=UNIT, cores=threads, kind="port",
-                sample="oracle FP64 solve on %d host threads: %d SOR sweeps + 2 viscosity updates of the "
-                       "200k-vertex dome (%.3f s/sweep, %.3f s/viscosity), extrapolated to the full solve's "
-                       "%d sweeps and %d Picard iterations" % (threads, sample_sweeps, t_sweep, t_visc,
-                                                              gpu_stats["total_sweeps"],
-                                                              gpu_stats["picard_iterations"]),
-                seconds_per_solve=full, mesh_build_s=t_mesh)
+    orc, base, om, ssa = oracle_workload(size)
+    rc, out, st, secs, _ = oracle_solve_timed(orc, om, ssa, threads)
+    info = dict(value=1.0 / secs, unit=UNIT, cores=threads, kind="port",
+                sample="one full cold-start FP64 solve of the %s-vertex dome by the oracle (C restatement of the "
+                       "reference's Fortran routines, OpenMP over the rows of each colour) on %d host threads: "
+                       "%.1f s, %d Picard iterations, %d SOR sweeps; measured, not extrapolated"
+                       % (size, threads, secs, st["picard_iterations"], st["total_sweeps"]))
+    return info, rc, out, st
 
 
 def run_reference(args):
+    """The reference arm: the oracle's full cold-start solves on all host cores. Warm-up: one
+    full solve (which also gives the sweep count that splits the next one). Timed: one full
+    solve in ``--steps`` consecutive pieces of equal sweep count; value = 1 / the solve's time."""
     rank, world, local = dist_info()
     if rank != 0:
         return 0
-    base, mesh, ssa, sia = make_workload(args.size)
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as orc
     threads = os.cpu_count() or 1
-    om = orc.build_aaac(mesh.base)
-    # Full-solve iteration counts of this workload (from the oracle's own 8-thread run of the
-    # same seeded problem): 13558 SOR sweeps over 8 linear solves, 9 Picard iterations.
-    counts = dict(total_sweeps=13558, picard_iterations=9)
-    sample = args.ref_sample_sweeps
-    times = []
-    for i in range(args.warmup + args.steps):
-        p1 = orc.default_params(n_threads=threads, replay_picard=1)
-        t0 = time.perf_counter()
-        orc.solve_ssa(om, ssa, p1)
-        t_visc = time.perf_counter() - t0
-        p2 = orc.default_params(n_threads=threads, replay_picard=2,
-                                replay_sweeps=np.array([sample, 0], dtype=np.int32))
-        t0 = time.perf_counter()
-        orc.solve_ssa(om, ssa, p2)
-        t_two = time.perf_counter() - t0
-        t_sweep = max(t_two - 2 * t_visc, 1e-9) / sample
-        if i >= args.warmup:
-            times.append(counts["total_sweeps"] * t_sweep + counts["picard_iterations"] * t_visc)
-    sec = statistics.median(times)
-    value = 1.0 / sec
+    orc, base, om, ssa = oracle_workload(args.size)
+    nnz = int(np.asarray(om.nCAaAc).sum())
+    rc_w, _, st_w, secs_w, _ = oracle_solve_timed(orc, om, ssa, threads)
+    rc, out, st, secs, pieces = oracle_solve_timed(orc, om, ssa, threads, pieces=args.steps,
+                                                   total_sweeps=st_w["total_sweeps"])
+    value = 1.0 / secs
+    sample = ("per step: one of %d consecutive pieces (equal SOR sweep counts) of one full cold-start FP64 solve "
+              "of the %s-vertex dome by the oracle (C restatement of the reference's Fortran routines, OpenMP "
+              "over the rows of each colour) on %d host threads; the %d steps together are exactly one solve "
+              "(%.1f s, %d Picard iterations, %d sweeps); warm-up: one full solve (%.1f s)"
+              % (args.steps, args.size, threads, args.steps, secs, st["picard_iterations"], st["total_sweeps"],
+                 secs_w))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dome geometry and mesh)",
-        "config": {"workload": WORKLOAD % args.size, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc), "precision": "fp64",
-                   "l2": "n/a (CPU)"},
+        "warmup": args.warmup, "ms_per_step": float(np.mean(pieces)) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dome geometry and mesh)",
+        "config": workload_config(args.size, base, om.nVAaAc, nnz),
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "per step: 1 viscosity update + %d SOR sweeps of the 200k-vertex dome solve by the "
-                                   "oracle (C restatement of the Fortran routines) on %d host threads, extrapolated to "
-                                   "13558 sweeps / 9 Picard iterations" % (sample, threads)},
+        "precision": "fp64", "status": rc, "picard_iterations": st["picard_iterations"],
+        "sor_sweeps": st["total_sweeps"], "sweeps_per_linear_solve": st["sweeps"],
+        "full_solve_s": secs, "warmup_solve_s": secs_w, "step_ms": [1e3 * float(x) for x in pieces],
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -269,10 +311,31 @@ def profile_case(args):
     p = api.default_params(precision=prec, SSA_max_outer_loops=1, SSA_max_inner_loops=args.profile_sweeps,
                            fp64_exact=1 if args.profile_case == "exact" else 0)
     dm.ssa_upload(ssa, p)
+    L = nat.load()
+    timers = hasattr(L, "ufe_debug_phase_cycles")
+    if timers:
+        import ctypes as ct
+        buf = (ct.c_ulonglong * 16)()
+        L.ufe_debug_phase_cycles.restype = ct.c_int
+        L.ufe_debug_phase_cycles(buf, 16, 1)
     times, st = timed_runs(dm, p, args.steps, args.warmup, dm.stream)
     ms = float(np.mean(times))
-    print(json.dumps({"profile_case": args.profile_case, "size": args.size, "sweeps": st["total_sweeps"],
-                      "ms_per_solve": ms, "us_per_sweep": 1e3 * ms / max(1, st["total_sweeps"])}))
+    line = {"profile_case": args.profile_case, "size": args.size, "sweeps": st["total_sweeps"],
+            "ms_per_solve": ms, "us_per_sweep": 1e3 * ms / max(1, st["total_sweeps"])}
+    if timers:
+        # totals over CTAs and over the warm-up and timed runs; shares of the per-CTA time, and
+        # the same shares of the measured time per sweep
+        n = L.ufe_debug_phase_cycles(buf, 16, 1)
+        names = ["wait_colour", "colour", "arrive", "wait_boundary", "boundary", "decide", "grid_barrier", "other"]
+        cyc = np.array([buf[i] for i in range(len(names))], dtype=np.float64)
+        sweeps_cta = float(buf[len(names)])
+        share = cyc / cyc.sum()
+        line["phase_timers"] = {
+            "runs": args.steps + args.warmup, "cta_sweeps": sweeps_cta,
+            "share": {k: float(v) for k, v in zip(names, share)},
+            "us_per_sweep": {k: float(v) * line["us_per_sweep"] for k, v in zip(names, share)},
+            "cycles_per_cta_sweep": {k: float(v) / max(sweeps_cta, 1.0) for k, v in zip(names, cyc)}}
+    print(json.dumps(line))
     dm.close()
     return 0
 
@@ -692,12 +755,13 @@ def main():
     p64 = api.default_params(precision=nat.UFE_FP64)
     p32 = api.default_params(precision=nat.UFE_MIXED)
 
-    # accuracy of the mixed path against the FP64 path (which matches the oracle to 1e-10)
+    # results of both paths through the C-ABI, checked against the oracle's full solve below
     rc64, o64, s64 = dm.solve_ssa(ssa, p64)
     rc32, o32, s32 = dm.solve_ssa(ssa, p32)
     def rel(a, b):
         return float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    l2 = max(rel(o32[k], o64[k]) for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac"))
+    FIELDS = ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac")
+    l2 = max(rel(o32[k], o64[k]) for k in FIELDS)
 
     dm.ssa_upload(ssa, p64)
     stream_ptr = dm.stream
@@ -756,17 +820,17 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 sweeps / f64 defect", "data": "synthetic (seeded dome geometry and mesh)",
-        "config": {"workload": WORKLOAD % args.size, "nV": int(base.nV), "nVAaAc": int(mesh.nVAaAc),
-                   "nnz": counts["nnz_all"], "precision": "mixed", "sliding": "linear beta^2=1e3",
-                   "picard_iterations": st32["picard_iterations"], "sor_sweeps": st32["total_sweeps"],
-                   "l2": "inputs and coefficient arrays (> 300 MB) larger than L2; no flush",
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": workload_config(args.size, base, mesh.nVAaAc, counts["nnz_all"]),
+        "precision": "mixed", "parallelism": "replicas" if world > 1 else "1 GPU",
+        "picard_iterations": st32["picard_iterations"], "sor_sweeps": st32["total_sweeps"],
+        "working_set": {"mixed_sweep_mb": round(sweep32 / 1e6, 1), "fp64_sweep_mb": round(sweep64 / 1e6, 1),
+                        "note": "the mixed sweep's arrays fit the 129 MB L2, the FP64 sweep's do not"},
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms64, "sor_sweeps": st64["total_sweeps"],
                  "picard_iterations": st64["picard_iterations"],
                  "vertex_sweeps_per_s": counts["nA"] * st64["total_sweeps"] / (ms64 * 1e-3),
                  "achieved_gbs": ach64, "frac": ach64 / peak},
         "mixed_vs_fp64_speedup": fp64_value and value / fp64_value,
-        "rel_l2_mixed_vs_fp64": l2,
+        "rel_l2_mixed_vs_fp64_gpu": l2,
         "vertex_sweeps_per_s": counts["nA"] * st32["total_sweeps"] / (ms32 * 1e-3),
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "kernel": "ssa_persistent<mixed>",
@@ -777,9 +841,16 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(mesh, ssa, st64)
-        line["cpu_baseline"].pop("mesh_build_s", None)
-        line["cpu_baseline"].pop("seconds_per_solve", None)
+        cb, rc_o, oout, ost = cpu_baseline(args.size)
+        line["cpu_baseline"] = cb
+        # accuracy against the oracle's FP64 solve of the same workload (the metric's rel-L2)
+        line["accuracy_vs_oracle"] = {
+            "rel_l2_mixed": max(rel(o32[k], oout[k]) for k in FIELDS),
+            "rel_l2_fp64": max(rel(o64[k], oout[k]) for k in FIELDS),
+            "fp64_same_sweep_counts": s64["sweeps"] == ost["sweeps"],
+            "same_picard_iterations": s64["picard_iterations"] == s32["picard_iterations"] == ost["picard_iterations"],
+            "oracle_status": rc_o, "oracle_sweeps": ost["total_sweeps"],
+            "fields": "U_SSA, V_SSA, Ux_SSA_Ac, Uy_SSA_Ac (max over the four)"}
     dm.close()
     if rank == 0:
         print(json.dumps(line))

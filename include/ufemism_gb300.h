@@ -198,7 +198,10 @@ int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *i
  * Up to 64 devices. The first call on a device looks up the scratch address: make it before
  * any stream capture. The scratch is shared by every call on a device: calls that overlap in
  * time (several threads, or several meshes of the same device) race on it and must be
- * serialised by the caller. Synchronous like ufe_sia_solve. */
+ * serialised by the caller. Synchronous like ufe_sia_solve. The results stay in the caller's
+ * arrays only, not on the handle: the call drops the SIA velocities an earlier ufe_sia_solve
+ * left there, so a later ufe_thickness_update must be given Up_SIA_Ac (with NULL it returns
+ * UFE_BAD_ARG). */
 #define UFE_SIA_NOALLOC_MAX_AC 262144
 int ufe_sia_solve_noalloc(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *in,
                           ufe_sia_out *out);

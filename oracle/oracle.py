@@ -66,7 +66,7 @@ class _Params(ct.Structure):
                 ("SSA_max_inner_loops", I32), ("m_enh_ssa", ct.c_double), ("m_enh_sia", ct.c_double),
                 ("sliding_law", I32), ("use_analytical_GL_flux", I32), ("zero_velocities", I32),
                 ("nZ", I32), ("zeta", P), ("n_threads", I32), ("replay_picard", I32),
-                ("replay_sweeps", P)]
+                ("replay_sweeps", P), ("progress", P)]
 
 
 class _SSA(ct.Structure):
@@ -202,7 +202,7 @@ def default_params(**kw):
     p = dict(SSA_RN_tol=1e-3, SSA_max_outer_loops=50, SSA_max_residual_UV=1e-4, SSA_SOR_omega=1.3,
              SSA_max_inner_loops=10000, m_enh_ssa=1.0, m_enh_sia=1.0, sliding_law=1,
              use_analytical_GL_flux=0, zero_velocities=0, zeta=ZETA_DEFAULT, n_threads=1,
-             replay_picard=0, replay_sweeps=None)
+             replay_picard=0, replay_sweeps=None, progress=None)
     p.update(kw)
     return p
 
@@ -213,7 +213,7 @@ def _params_struct(p):
     s = _Params(p["SSA_RN_tol"], p["SSA_max_outer_loops"], p["SSA_max_residual_UV"], p["SSA_SOR_omega"],
                 p["SSA_max_inner_loops"], p["m_enh_ssa"], p["m_enh_sia"], p["sliding_law"],
                 p["use_analytical_GL_flux"], p["zero_velocities"], zeta.size, _ptr(zeta),
-                p["n_threads"], p["replay_picard"], _ptr(rs))
+                p["n_threads"], p["replay_picard"], _ptr(rs), _ptr(p.get("progress")))
     return s, (zeta, rs)
 
 

@@ -104,6 +104,9 @@ typedef struct or_params {
    * SOR sweep counts in replay_sweeps (ignores the tolerances). */
   int32_t replay_picard;
   const int32_t *replay_sweeps;
+  /* If non-null, the solve stores its running total of SOR sweeps here after every sweep
+   * (read by a benchmark thread to time consecutive pieces of one solve). */
+  volatile int64_t *progress;
 } or_params;
 
 /* Ice fields read / written by solve_SSA (type_ice_model, data_types_module.f90:15-214). */

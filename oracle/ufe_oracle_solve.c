@@ -284,7 +284,7 @@ void or_neumann_AaAc(const or_base *b, const or_aaac *m, double *d) {
 static int sor_loop(const or_base *b, const or_aaac *m, const or_params *p,
                     const int32_t *mask_gl_Ac, const double *RHSx, const double *RHSy,
                     const double *eu, const double *ev, double *U, double *V, int *did_reset,
-                    int *not_converged, double *max_res_out, int n_fixed) {
+                    int *not_converged, double *max_res_out, int n_fixed, int64_t sweeps_before) {
   const int nA = m->nVAaAc, nV = b->nV;
   const double omega = p->SSA_SOR_omega;
   int has_converged = 0, inner_loop_i = 0;
@@ -332,6 +332,7 @@ static int sor_loop(const or_base *b, const or_aaac *m, const or_params *p,
     }
     or_neumann_AaAc(b, m, U);
     or_neumann_AaAc(b, m, V);
+    if (p->progress) *p->progress = sweeps_before + inner_loop_i;
     if (n_fixed > 0) continue;
     if (max_residual_UV < p->SSA_max_residual_UV) {
       *did_reset = 0;
@@ -381,7 +382,7 @@ int or_solve_SSA_linearised(const or_base *b, const or_aaac *m, const or_params 
   if (!w) return OR_ERR_BAD_ARG;
   double *RHSx = w, *RHSy = w + nA, *eu = w + 2 * (size_t)nA, *ev = w + 3 * (size_t)nA;
   rhs_and_centre(m, Hi, Hb, SL, hx, hy, eta, S, RHSx, RHSy, eu, ev);
-  const int ns = sor_loop(b, m, p, mask_gl_Ac, RHSx, RHSy, eu, ev, U, V, &did_reset, &not_conv, max_res, 0);
+  const int ns = sor_loop(b, m, p, mask_gl_Ac, RHSx, RHSy, eu, ev, U, V, &did_reset, &not_conv, max_res, 0, 0);
   if (sweeps) *sweeps = ns;
   free(w);
   if (did_reset) return OR_RESET_ONCE;
@@ -539,7 +540,7 @@ int or_solve_SSA(const or_base *b, const or_aaac *m, const or_params *p, or_ssa_
     int did_reset_now = 0, not_conv = 0;
     const int n_fixed = (p->replay_picard > 0 && p->replay_sweeps) ? p->replay_sweeps[it - 1] : 0;
     const int ns = sor_loop(b, m, p, f->mask_gl_Ac, RHSx, RHSy, eu, ev, U, V, &did_reset_now,
-                            &not_conv, &st->last_max_residual, n_fixed);
+                            &not_conv, &st->last_max_residual, n_fixed, st->total_sweeps);
     if (st->linear_solves < 64) st->sweeps[st->linear_solves] = ns;
     st->linear_solves++;
     st->total_sweeps += ns;

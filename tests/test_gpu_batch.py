@@ -206,3 +206,47 @@ def test_batch_into_reused_host_buffers(ensemble):
         assert all(o is bb for o, bb in zip(outs, bufs))
         check_members(single, stats, outs)
     b.close()
+
+
+ORACLE_SIZES = (2200, 5200, 12000)   # config-4 style members: GRF friction, H0 drawn per member
+
+
+@pytest.fixture(scope="module")
+def oracle_members():
+    """Three ensemble members (log-uniform sizes, dome H0 from U[2000, 4000] m, log beta^2 a
+    Gaussian random field with std 1 and 100 km correlation), each with the oracle's FP64
+    solve on a mesh the oracle built itself."""
+    import os
+    import oracle as orc
+    api.init(0)
+    out = []
+    for i, n in enumerate(ORACLE_SIZES):
+        base, mesh, ssa = wl.ensemble_member(n, 9100 + i)
+        om = orc.build_aaac(base)
+        for k in ("CAaAc", "colour_vi", "Nxx_AaAc"):
+            assert np.array_equal(np.asarray(getattr(om, k)), np.asarray(getattr(mesh, k))), k
+        rc, oo, st = orc.solve_ssa(om, ssa, orc.default_params(n_threads=os.cpu_count() or 1))
+        assert rc in (orc.OR_OK, orc.OR_NOT_CONVERGED)
+        st["status"] = rc
+        out.append((base, mesh, ssa, oo, st))
+    return out
+
+
+@pytest.mark.parametrize("precision", [nat.UFE_FP64, nat.UFE_MIXED])
+def test_batch_members_match_oracle(oracle_members, precision):
+    """Batched members against the oracle directly (not only against the library's single
+    solves): FP64 <= 1e-10 with the oracle's Picard and sweep counts, mixed <= 1e-6."""
+    ens = [(b, m, s) for b, m, s, _, _ in oracle_members]
+    bt, p, rc, stats, timing, outs = run_batch(ens, precision, rows_per_cta=2048)
+    try:
+        assert rc >= 0
+        for i, (_, _, _, oo, ost) in enumerate(oracle_members):
+            assert stats[i]["status"] == ost["status"], i
+            assert stats[i]["picard_iterations"] == ost["picard_iterations"], i
+            if precision == nat.UFE_FP64:
+                assert stats[i]["sweeps"] == ost["sweeps"], i
+            tol = 1e-10 if precision == nat.UFE_FP64 else 1e-6
+            for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac"):
+                assert rel_l2(outs[i][k], oo[k]) <= tol, (i, k, rel_l2(outs[i][k], oo[k]))
+    finally:
+        bt.close()

@@ -153,3 +153,31 @@ def test_noalloc_rejects_mesh_beyond_scratch(setup):
         assert "scratch holds at most %d" % nat.UFE_SIA_NOALLOC_MAX_AC in nat.last_error()
     finally:
         dm.close()
+
+
+def test_noalloc_drops_the_handles_sia_velocities(setup):
+    """After ufe_sia_solve the handle offers its Up_SIA_Ac to a thickness update given none;
+    after a no-allocation call (whose results stay in the caller's arrays) it must not, so a
+    thickness update without Up_SIA_Ac is refused rather than advecting with the older field."""
+    torch, base, mesh, dm = setup
+    p = api.default_params()
+    nZ = len(p["zeta"])
+    sia = sia_inputs(base, mesh, 3600.0, 1e-16)
+    dm.geometry_attach(mesh)
+    ref = dm.solve_sia(sia, p)
+    Hi, _, _ = wl.dome_geometry(base)
+    Aw, Cw = wl.areas_and_widths(base)
+    smb, bmb = np.full(base.nV, 0.3), np.zeros(base.nV)
+    up_ssa = np.zeros(mesh.nAc)
+    h1 = dm.thickness_update(Hi, Aw, Cw, smb, bmb, 10.0, Up_SSA_Ac=up_ssa)[0]
+    h2 = dm.thickness_update(Hi, Aw, Cw, smb, bmb, 10.0, Up_SIA_Ac=ref["Up_SIA_Ac"], Up_SSA_Ac=up_ssa)[0]
+    assert np.array_equal(h1, h2)
+    din = to_device(torch, sia_inputs(base, mesh, 2400.0, 3e-16))
+    dout = device_outputs(torch, mesh.nAc, base.nV, nZ)
+    torch.cuda.synchronize()
+    assert call_noalloc(dm, p, din, dout) == nat.UFE_OK, nat.last_error()
+    with pytest.raises(nat.UfeError) as e:
+        dm.thickness_update(Hi, Aw, Cw, smb, bmb, 10.0, Up_SSA_Ac=up_ssa)
+    assert e.value.status == nat.UFE_BAD_ARG
+    got = dm.thickness_update(Hi, Aw, Cw, smb, bmb, 10.0, Up_SIA_Ac=host(dout["Up_SIA_Ac"]), Up_SSA_Ac=up_ssa)[0]
+    assert np.all(np.isfinite(got))

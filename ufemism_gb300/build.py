@@ -15,9 +15,16 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
-OUT = os.path.join(HERE, "_build")
-LIB = os.path.join(OUT, "libufemism_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Build variants: the product library, and a profiling build whose persistent solver records
+# per-phase SM-cycle totals (ufe_debug_phase_cycles). UFE_BUILD_VARIANT selects the one that
+# ufemism_gb300._native loads.
+VARIANTS = {"": [], "phase_timers": ["-DUFE_PHASE_TIMERS=1"]}
+VARIANT = os.environ.get("UFE_BUILD_VARIANT", "")
+if VARIANT not in VARIANTS:
+    raise RuntimeError("UFE_BUILD_VARIANT must be one of %s" % sorted(VARIANTS))
+OUT = os.path.join(HERE, "_build" + ("_" + VARIANT if VARIANT else ""))
+LIB = os.path.join(OUT, "libufemism_gb300.so")
 
 CU_SOURCES = ["ufe_mesh.cu", "ufe_ssa.cu", "ufe_sia.cu", "ufe_geom.cu"]
 CPP_SOURCES = ["ufe_capi.cpp", "aaac_build.cpp"]
@@ -51,8 +58,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     jobs = []
     for f in CU_SOURCES:
         obj = os.path.join(OUT, f + ".o")
-        jobs.append([nvcc, *ARCH, "-lineinfo", "--fmad=false", *common, *(extra_flags or []), "-c",
-                     os.path.join(SRC, f), "-o", obj])
+        jobs.append([nvcc, *ARCH, "-lineinfo", "--fmad=false", *common, *VARIANTS[VARIANT], *(extra_flags or []),
+                     "-c", os.path.join(SRC, f), "-o", obj])
     for f in CPP_SOURCES:
         obj = os.path.join(OUT, f + ".o")
         jobs.append([nvcc, *common, "-c", os.path.join(SRC, f), "-o", obj])

@@ -296,6 +296,10 @@ extern "C" int ufe_sia_solve_noalloc(ufe_mesh_h h, const ufe_params *p, const uf
   double *scratch = nullptr;
   rc = scratch_address(dev, &scratch);
   if (rc) return rc;
+  // This call's results live only in the caller's arrays. An earlier ufe_sia_solve's
+  // velocities on the handle are now out of date, so they are no longer offered to a
+  // thickness update that is given no Up_SIA_Ac (it returns UFE_BAD_ARG instead).
+  if (h->sia) h->sia->solved = false;
   cudaStream_t s = h->stream;
   // zeta and zeta**n_flow (n = 3) as in ufe_sia_solve, staged from the stack.
   double zc[2 * kMaxZ];

@@ -138,6 +138,54 @@ static_assert(kMixedLag >= 0 && kMixedLag <= kMaxLag, "lag out of range");
 constexpr size_t kLocalRowsMaxBytes = 160 * 1024;
 constexpr int kMaxKrylovRestart = 1000;   // largest GMRES restart length of the VJP
 
+// Per-phase timers of the persistent solver (profiling build only, -DUFE_PHASE_TIMERS=1):
+// thread 0 of every CTA stamps clock64() at the end of each phase of the SOR loop (every
+// phase ends with a CTA barrier, so its stamp is when the whole CTA is through) and adds the
+// SM cycles since the previous stamp to a per-category total; the totals of all CTAs are
+// summed into g_phase_cycles at the end of the launch. The normal build compiles none of it.
+#ifndef UFE_PHASE_TIMERS
+#define UFE_PHASE_TIMERS 0
+#endif
+enum PhaseTimer : int {
+  kTmWaitColour = 0,   // neighbour waits before colour phases
+  kTmColour,           // colour phases (sweep + publish)
+  kTmArrive,           // the sweep's residual into the decision slot / block max
+  kTmWaitBoundary,     // neighbour wait before the boundary phase
+  kTmBoundary,         // boundary phase (+ publish)
+  kTmDecide,           // reading lagged decisions
+  kTmGrid,             // team barriers inside the SOR loop
+  kTmOther,            // viscosity, RN, coefficients, defect, fold, refolds
+  kTmSweeps,           // (count) sweeps of this CTA
+  kTmCount
+};
+#if UFE_PHASE_TIMERS
+__device__ unsigned long long g_phase_cycles[kTmCount];
+#define UFE_TM_DECL                                   \
+  __shared__ unsigned long long s_tm[kTmCount];       \
+  __shared__ long long s_tm0;                         \
+  if (threadIdx.x < kTmCount) s_tm[threadIdx.x] = 0;  \
+  if (threadIdx.x == 0) s_tm0 = clock64();
+#define UFE_TM(cat)                                               \
+  do {                                                            \
+    if (threadIdx.x == 0) {                                       \
+      const long long now_ = clock64();                           \
+      s_tm[cat] += (unsigned long long)(now_ - s_tm0);            \
+      s_tm0 = now_;                                               \
+    }                                                             \
+  } while (0)
+#define UFE_TM_COUNT(cat) do { if (threadIdx.x == 0) s_tm[cat] += 1; } while (0)
+#define UFE_TM_FLUSH()                                                                  \
+  do {                                                                                  \
+    __syncthreads();                                                                    \
+    if (threadIdx.x < kTmCount) atomicAdd(&g_phase_cycles[threadIdx.x], s_tm[threadIdx.x]); \
+  } while (0)
+#else
+#define UFE_TM_DECL
+#define UFE_TM(cat) do { } while (0)
+#define UFE_TM_COUNT(cat) do { } while (0)
+#define UFE_TM_FLUSH() do { } while (0)
+#endif
+
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -838,6 +886,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
   int it = 0;
   unsigned int gsweep = 0;   // sweeps of this launch (the lagged decisions' ring index)
   bool picard_done = false;
+  UFE_TM_DECL
 #define UFE_GRID_SYNC()                                   \
   if (!team_barrier(t, &ctl->err, a.timeout_ns)) {        \
     if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu; \
@@ -876,28 +925,36 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
       bool synced = true;        // a team barrier follows the previous phases of this CTA
       int decided = 0;           // sweeps of this linear solve already decided
       const unsigned int base = gsweep;
+      UFE_TM(kTmOther);
       while (!lin_done && sweeps < a.max_inner) {
         ++sweeps;
+        UFE_TM_COUNT(kTmSweeps);
         const unsigned int G = gsweep++;
         unsigned long long mx = 0ull;
         for (int g = 0; g < 5; ++g) {
           if (g > 0 || !synced) wait_neighbours(a, ps, phases, t.bar());
+          UFE_TM(kTmWaitColour);
           const unsigned long long m = phase_sweep32(a, ps, g, lc);
           mx = m > mx ? m : mx;
           ++phases;
           publish_progress(a, t, phases);
+          UFE_TM(kTmColour);
         }
         lag_arrive(ctl, G, mx);
+        UFE_TM(kTmArrive);
         wait_neighbours(a, ps, phases, t.bar());
+        UFE_TM(kTmWaitBoundary);
         phase_boundary<kM>(a, ps, lc);
         ++phases;
         publish_progress(a, t, phases);
+        UFE_TM(kTmBoundary);
         synced = false;
         const bool refold_now = a.refold > 0 && sweeps % a.refold == 0;
         const bool sync_point = sweeps == a.max_inner || refold_now;
         if (sync_point) {
           UFE_GRID_SYNC();
           synced = true;
+          UFE_TM(kTmGrid);
         }
         const int upto = sync_point ? sweeps : sweeps - kMixedLag;
         int act = 0;             // 1: converged, 2: diverged
@@ -912,6 +969,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
           if (r < a.tol) act = 1;
           else if (r > 1e6) act = 2;
         }
+        UFE_TM(kTmDecide);
         if (act == 1) {
           lin_done = true;
         } else if (act == 2) {
@@ -930,16 +988,21 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
           phase_defect(a, t);
           UFE_GRID_SYNC();
         }
+        UFE_TM(kTmOther);
       }
       if (!synced) UFE_GRID_SYNC();
+      UFE_TM(kTmGrid);
     } else
     while (!lin_done && sweeps < a.max_inner) {
       ++sweeps;
+      UFE_TM(kTmOther);
+      UFE_TM_COUNT(kTmSweeps);
       const int slot = sweeps % 3;
       if (leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
       unsigned long long mx = 0ull;
       for (int g = 0; g < 5; ++g) {
         if (g > 0) wait_neighbours(a, ps, phases, t.bar());
+        UFE_TM(kTmWaitColour);
         unsigned long long m;
         if (kMode == kExact64) m = phase_sweep_exact(a, ps, g);
         else if (kMode == kFast64) m = phase_sweep_fast(a, ps, g, lc);
@@ -947,11 +1010,16 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         mx = m > mx ? m : mx;
         ++phases;
         publish_progress(a, t, phases);
+        UFE_TM(kTmColour);
       }
       block_max_to(&ctl->maxres[slot], mx);
+      UFE_TM(kTmArrive);
       wait_neighbours(a, ps, phases, t.bar());
+      UFE_TM(kTmWaitBoundary);
       phase_boundary<kM>(a, ps, lc);
+      UFE_TM(kTmBoundary);
       UFE_GRID_SYNC();
+      UFE_TM(kTmGrid);
       maxres = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxres[slot]);
       if (maxres < a.tol) {
         lin_done = true;
@@ -999,6 +1067,8 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
     for (int p = tid; p < a.nP; p += nt) a.Na[p] = N[p];
   }
   UFE_GRID_SYNC();
+  UFE_TM(kTmOther);
+  UFE_TM_FLUSH();
   return true;
 #undef UFE_GRID_SYNC
 }
@@ -3099,3 +3169,20 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   }
   return status;
 }
+
+#if UFE_PHASE_TIMERS
+// Profiling build only (not part of the C-ABI header): the per-phase SM-cycle totals of the
+// persistent solver summed over CTAs since the last reset, in PhaseTimer order; `reset`
+// zeroes them after the read.
+extern "C" int ufe_debug_phase_cycles(unsigned long long *out, int n, int reset) {
+  if (!out || n < (int)kTmCount) { set_error("ufe_debug_phase_cycles: need kTmCount slots"); return UFE_BAD_ARG; }
+  int rc = cuda_status(cudaDeviceSynchronize(), "ufe_debug_phase_cycles");
+  if (!rc) rc = cuda_status(cudaMemcpyFromSymbol(out, g_phase_cycles, sizeof(unsigned long long) * kTmCount),
+                            "read phase timers");
+  if (!rc && reset) {
+    static const unsigned long long zeros[kTmCount] = {};
+    rc = cuda_status(cudaMemcpyToSymbol(g_phase_cycles, zeros, sizeof(zeros)), "reset phase timers");
+  }
+  return rc ? rc : (int)kTmCount;
+}
+#endif
