@@ -232,6 +232,21 @@ typedef struct ufe_geometry_out {       /* host arrays, each may be NULL */
 int ufe_geometry_attach(ufe_mesh_h mesh, const ufe_geometry_mesh *geometry);
 int ufe_geometry_update(ufe_mesh_h mesh, const double *Hi, const double *Hb, const double *SL,
                         ufe_geometry_out *out);
+
+/* Every mask of determine_masks (general_ice_model_data_module.f90:97-297) from the device
+ * geometry of the last ufe_geometry_update / ufe_ssa_upload_geometry, where they are computed
+ * beside the others and stay: land, ocean, lake (never set by the routine: all 0), ice, sheet,
+ * shelf, coast, margin, grounding line, calving front, and the type mask `mask` (type_land 0,
+ * ocean 1, lake 2, sheet 3, shelf 4, coast 5, margin 6, groundingline 7, calvingfront 8: the
+ * last type the routine assigns), on the Aa vertices (nV) and the Ac edges (nAc). Host arrays,
+ * each may be NULL. */
+typedef struct ufe_mask_out {
+  int32_t *mask_land, *mask_ocean, *mask_lake, *mask_ice, *mask_sheet, *mask_shelf, *mask_coast, *mask_margin,
+      *mask_gl, *mask_cf, *mask;                                                    /* (nV) */
+  int32_t *mask_land_Ac, *mask_ocean_Ac, *mask_lake_Ac, *mask_ice_Ac, *mask_sheet_Ac, *mask_shelf_Ac,
+      *mask_coast_Ac, *mask_margin_Ac, *mask_gl_Ac, *mask_cf_Ac, *mask_Ac;           /* (nAc) */
+} ufe_mask_out;
+int ufe_geometry_masks(ufe_mesh_h mesh, ufe_mask_out *out);
 int ufe_ssa_upload_geometry(ufe_mesh_h mesh, const ufe_params *params, const double *Hi, const double *Hb,
                             const double *SL, const double *A_flow_mean, const double *A_flow_mean_Ac,
                             const double *beta_sq_AaAc, const ufe_ssa_inout *inout);
@@ -324,8 +339,15 @@ int ufe_thickness_update(ufe_mesh_h mesh, const ufe_thickness_in *in, double *Hi
  * converged to (viscosity and friction linearised at the converged state, Neumann rows as
  * averaging constraints, masks frozen) by a transposed coloured SOR on the device, and
  * returns dJ/d(log beta^2) on AaAc, the sensitivities to the gathered driving-stress slopes
- * and Hi_AaAc and, given the Aa and Ac derivative stencils, dJ/dHi on Aa. Linear sliding law
- * only; the grounding-line flux option is not differentiated. Output arrays may be NULL.
+ * and Hi_AaAc and, given the Aa and Ac derivative stencils, dJ/dHi on Aa. Both sliding laws:
+ * the linear law (this library's extension, S = beta^2), and the reference's
+ * Coulomb_regularised law (SSA_sliding_term, ice_dynamics_module.f90:745-751), whose S(u)
+ * adds a 2x2 block per grounded row to the transposed sweep; under it dJ_dlogbeta_sq_AaAc
+ * holds dJ/d(log tau_c) (tau_c the basal yield stress of basal_yield_stress, 780-844: S is
+ * proportional to it), dJ_dphi_fric_AaAc dJ/d(phi_fric) in degrees, and the friction term
+ * does not depend on Hi (tau_c and the friction denominator both carry max(0.1, Hi)). The
+ * params' sliding law must be the last solve's. The grounding-line flux option is not
+ * differentiated. Output arrays may be NULL.
  * The forward solve should be converged well below the tolerances the gradient is wanted
  * to (the VJP differentiates the fixed point, not the truncated iteration). */
 enum { UFE_VJP_GMRES = 0, UFE_VJP_SOR = 1 };
@@ -355,6 +377,7 @@ typedef struct ufe_vjp_out {
   double *dJ_dHi;                       /* (nV), needs geom */
   double *dJ_dhx_AaAc, *dJ_dhy_AaAc, *dJ_dHi_AaAc;  /* (nVAaAc) sensitivities to the gathered fields */
   double *lambda_U_AaAc, *lambda_V_AaAc;            /* (nVAaAc) adjoint state */
+  double *dJ_dphi_fric_AaAc;                        /* (nVAaAc) Coulomb law only */
 } ufe_vjp_out;
 typedef struct ufe_vjp_stats {
   int32_t status, sweeps;

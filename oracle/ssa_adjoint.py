@@ -220,9 +220,8 @@ class Linearisation:
 
     # ------------------------------------------------------------ parameter derivatives
     def dF_dlogbeta(self):
-        """dF/d(log beta^2) (diagonal per row): -fr U on interior grounded rows."""
-        if self.tau_c is not None:
-            raise ValueError("log(beta^2) is a parameter of the linear law only")
+        """dF/d(log S0) (diagonal per row): -fr U on interior grounded rows, where S0 is the
+        law's coefficient field, S proportional to it: beta^2 (linear) or tau_c (Coulomb)."""
         interior = ~self.edge
         return np.where(interior, -self.fr * self.U, 0.0), np.where(interior, -self.fr * self.V, 0.0)
 
@@ -284,17 +283,81 @@ def geometry_matrix(m, Hi, Hb, SL):
     return Gx, Gy, GH
 
 
+def dlogtau_dHb(Hb, SL, Hi=None):
+    """d log(tau_c) / d Hb per row of basal_yield_stress (ice_dynamics_module.f90:780-844):
+    tau_c = tan(phi pi / 180) rho g max(0.1, Hi) (1 - 0.96 lambda_p), with
+    phi = clamp(5 + 15 (1 + Hb / 1000), 5, 20) and lambda_p = clamp(1 - (Hb - SL) / 1000, 0, 1);
+    a clamped branch contributes nothing."""
+    Hb = np.asarray(Hb, dtype=np.float64)
+    SL = np.asarray(SL, dtype=np.float64)
+    phi_raw = 5.0 + 15.0 * (1.0 + Hb / 1000.0)
+    phi = np.clip(phi_raw, 5.0, 20.0)
+    dphi = np.where((phi_raw > 5.0) & (phi_raw < 20.0), 15.0 / 1000.0, 0.0)
+    lam_raw = 1.0 - (Hb - SL) / 1000.0
+    lam = np.clip(lam_raw, 0.0, 1.0)
+    dlam = np.where((lam_raw > 0.0) & (lam_raw < 1.0), -1.0 / 1000.0, 0.0)
+    r = np.pi / 180.0
+    return r * dphi / (np.sin(r * phi) * np.cos(r * phi)) + (-0.96 * dlam) / (1.0 - 0.96 * lam)
+
+
+def bed_matrix(m, Hi, Hb, SL):
+    """Linear map dHb (Aa, nV) -> (d hx, d hy, d Hb_AaAc) on AaAc rows, masks frozen: the
+    surface Hs = Hi + max(SL - rho_i/rho_sw Hi, Hb) moves with the bed on grounded vertices
+    only, and floating rows take their slope from Hi (the shelf rule), not from Hs."""
+    base = m.base
+    nV, nAc = base.nV, m.nAc
+    Hi, Hb, SL = (np.asarray(a, dtype=np.float64) for a in (Hi, Hb, SL))
+    ocean = Hi < ((SL - Hb) * RHO_SW) / RHO_I
+    slope = np.where(ocean, 0.0, 1.0)                # dHs/dHb per Aa vertex
+    Aci = np.asarray(m.Aci, dtype=np.int64) - 1
+    vi, vj = Aci[:, 0], Aci[:, 1]
+    Hi_Ac, Hb_Ac, SL_Ac = (Hi[vi] + Hi[vj]) / 2.0, (Hb[vi] + Hb[vj]) / 2.0, (SL[vi] + SL[vj]) / 2.0
+    ocean_Ac = Hi_Ac < ((SL_Ac - Hb_Ac) * RHO_SW) / RHO_I
+    nC = np.asarray(base.nC, dtype=np.int64)
+    C = np.asarray(base.C, dtype=np.int64) - 1
+    Nx, Ny = np.asarray(m.Nx), np.asarray(m.Ny)
+    ncm = C.shape[1]
+    slot = np.arange(ncm)[None, :]
+    valid = slot < nC[:, None]
+    rA = np.repeat(np.arange(nV), ncm).reshape(nV, ncm)[valid]
+    kA = np.broadcast_to(slot, (nV, ncm))[valid]
+    cA = C[valid]
+    rows = np.concatenate([rA, np.arange(nV)])
+    cols = np.concatenate([cA, np.arange(nV)])
+    wx = np.concatenate([Nx[rA, kA], Nx[np.arange(nV), nC]])
+    wy = np.concatenate([Ny[rA, kA], Ny[np.arange(nV), nC]])
+    fac = np.where(ocean[rows], 0.0, slope[cols])
+    Gx_aa = sp.csr_matrix((wx * fac, (rows, cols)), shape=(nV, nV))
+    Gy_aa = sp.csr_matrix((wy * fac, (rows, cols)), shape=(nV, nV))
+    Nx_Ac, Ny_Ac = np.asarray(m.Nx_Ac), np.asarray(m.Ny_Ac)
+    ra = np.repeat(np.arange(nAc), 4)
+    ca = Aci.reshape(-1)
+    facA = np.where(ocean_Ac[ra], 0.0, slope[ca])
+    Gx_ac = sp.csr_matrix((Nx_Ac.reshape(-1) * facA, (ra, ca)), shape=(nAc, nV))
+    Gy_ac = sp.csr_matrix((Ny_Ac.reshape(-1) * facA, (ra, ca)), shape=(nAc, nV))
+    GB_ac = sp.csr_matrix((np.full(2 * nAc, 0.5), (np.repeat(np.arange(nAc), 2), np.stack([vi, vj], 1).reshape(-1))),
+                          shape=(nAc, nV))
+    return (sp.vstack([Gx_aa, Gx_ac]).tocsr(), sp.vstack([Gy_aa, Gy_ac]).tocsr(),
+            sp.vstack([sp.identity(nV, format="csr"), GB_ac]).tocsr())
+
+
+def coulomb_bed_gradient(m, f, d_logtau, s_hx, s_hy):
+    """dJ/dHb on Aa under the Coulomb law from the adjoint's dJ/dlog(tau_c) and driving-stress
+    sensitivities (AaAc rows): through tau_c's bed dependence and through the surface slope."""
+    g = gather_fields(m, f)
+    Gx, Gy, GB = bed_matrix(m, f["Hi"], f["Hb"], f["SL"])
+    return GB.T @ (np.asarray(d_logtau) * dlogtau_dHb(g["Hb"], g["SL"])) + Gx.T @ s_hx + Gy.T @ s_hy
+
+
 def adjoint_gradient(lin: Linearisation, gU, gV, G=None):
-    """Solve (dF/du)^T mu = dJ/du and return (mu_U, mu_V, dJ/dlogbeta2 (None under the
-    Coulomb law), dJ/dHi or None, field sensitivities dict)."""
+    """Solve (dF/du)^T mu = dJ/du and return (mu_U, mu_V, dJ/dlog(beta^2) (dJ/dlog(tau_c)
+    under the Coulomb law), dJ/dHi or None, field sensitivities dict)."""
     nA = lin.nA
     K = lin.jacobian()
     mu = spla.spsolve(K.T.tocsc(), np.concatenate([gU, gV]))
     mx, my = mu[:nA], mu[nA:]
-    d_logbeta = None                  # the Coulomb law has no log(beta^2)
-    if lin.tau_c is None:
-        bx, by = lin.dF_dlogbeta()
-        d_logbeta = -(mx * bx + my * by)
+    bx, by = lin.dF_dlogbeta()        # log(beta^2) (linear law) or log(tau_c) (Coulomb law)
+    d_logbeta = -(mx * bx + my * by)
     dhx, dHx, dHy = lin.dF_dfields()
     s_hx = -mx * dhx
     s_hy = -my * dhx

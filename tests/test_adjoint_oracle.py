@@ -160,7 +160,6 @@ def test_coulomb_thickness_gradient_matches_finite_differences(coulomb):
     G = adj.geometry_matrix(m, H, Hb, SL)
     gU, gV = U - Uo, V - Vo
     mx, my, dlb, dHi, sens = adj.adjoint_gradient(lin, gU, gV, G)
-    assert dlb is None
     flot = (SL - Hb) * adj.RHO_SW / adj.RHO_I
     safe = (H > 50.0) & (np.abs(H - flot) > 50.0)
     h = 1e-2
@@ -170,4 +169,44 @@ def test_coulomb_thickness_gradient_matches_finite_differences(coulomb):
         (Um, Vm), _ = solve(fields_for(m, ssa, H - h * d)[0])
         fd = (adj.misfit(Up, Vp, Uo, Vo) - adj.misfit(Um, Vm, Uo, Vo)) / (2 * h)
         an = float(dHi @ d)
+        assert abs(fd - an) <= 1e-5 * abs(an), (fd, an)
+
+
+def bed_fields_for(m, ssa, Hb):
+    """Solve inputs for another bed (the geometry recomputed by the oracle)."""
+    g = orc.update_geometry(m, ssa["Hi"], Hb, ssa["SL"])
+    f = dict(ssa)
+    for k in ("Hb_Ac", "dHs_dx_shelf", "dHs_dy_shelf", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac"):
+        f[k] = g[k]
+    f["Hb"] = Hb
+    return f, g
+
+
+def test_coulomb_friction_gradient_matches_finite_differences_of_the_bed(coulomb):
+    """dJ/dlog(tau_c) under the Coulomb law, checked through the reference's own friction input:
+    the bed Hb sets tau_c (basal_yield_stress: the till friction angle and the pore-water
+    fraction) and the surface slope of grounded ice. The chain dJ/dHb = dJ/dlog(tau_c) dlog(tau_c)/dHb
+    + slope terms against central finite differences of the oracle's forward solve, on
+    perturbations of vertices away from the floatation threshold (masks frozen)."""
+    m, ssa, solve, U, V, out = coulomb
+    H = np.asarray(ssa["Hi"], dtype=np.float64)
+    Hb, SL = np.asarray(ssa["Hb"], dtype=np.float64), np.asarray(ssa["SL"], dtype=np.float64)
+    x, y = m.base.V[:, 0], m.base.V[:, 1]
+    bump = 20.0 * np.exp(-((x - 2e5) ** 2 + (y + 1e5) ** 2) / (2 * (1.5e5) ** 2))
+    # observations from a thicker dome (a misfit well above the solver's tolerance)
+    (Uo, Vo), _ = solve(fields_for(m, ssa, np.where(H > 0, H + bump, H))[0])
+    lin = adj.Linearisation(m, ssa, U, V, tau_c=out["tau_c_AaAc"])
+    gU, gV = U - Uo, V - Vo
+    mx, my, dlt, dHi, sens = adj.adjoint_gradient(lin, gU, gV)
+    dHb = adj.coulomb_bed_gradient(m, ssa, dlt, sens["hx"], sens["hy"])
+    flot = (SL - Hb) * adj.RHO_SW / adj.RHO_I
+    safe = (H > 50.0) & (np.abs(H - flot) > 50.0) & (np.abs(Hb) > 1.0)
+    rng = np.random.default_rng(21)
+    h = 1e-3   # the friction law's curvature in the bed (tan, the pore-water fraction, S(u)) wants a short step
+    for _ in range(2):
+        d = np.where(safe, rng.normal(size=H.size), 0.0)
+        (Up, Vp), _ = solve(bed_fields_for(m, ssa, Hb + h * d)[0])
+        (Um, Vm), _ = solve(bed_fields_for(m, ssa, Hb - h * d)[0])
+        fd = (adj.misfit(Up, Vp, Uo, Vo) - adj.misfit(Um, Vm, Uo, Vo)) / (2 * h)
+        an = float(dHb @ d)
         assert abs(fd - an) <= 1e-5 * abs(an), (fd, an)

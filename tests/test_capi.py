@@ -36,7 +36,8 @@ def test_struct_layouts_match_header():
     for cname, py in (("ufe_params", nat.Params), ("ufe_ssa_stats", nat.SsaStats),
                       ("ufe_batch_config", nat.BatchConfig), ("ufe_batch_timing", nat.BatchTiming),
                       ("ufe_physprop_out", nat.PhyspropOut), ("ufe_triangle_mesh", nat.TriangleMesh),
-                      ("ufe_sia3d_out", nat.Sia3dOut), ("ufe_geometry_out", nat.GeometryOut)):
+                      ("ufe_sia3d_out", nat.Sia3dOut), ("ufe_geometry_out", nat.GeometryOut),
+                      ("ufe_mask_out", nat.MaskOut), ("ufe_vjp_out", nat.VjpOut)):
         body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), text, re.S).group(1)
         body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
         names = re.findall(r"(\w+)(?:\[\d+\])?\s*[,;]", body)

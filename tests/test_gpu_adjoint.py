@@ -97,7 +97,84 @@ def test_vjp_matches_cpu_reference_and_finite_differences(name, kind, method):
     dm.close()
 
 
-def test_vjp_rejects_coulomb_law_and_missing_solve():
+def geometry_fields(m, ssa, Hi=None, Hb=None):
+    """Solve inputs for another thickness or bed, the geometry recomputed by the oracle."""
+    Hi = ssa["Hi"] if Hi is None else Hi
+    Hb = ssa["Hb"] if Hb is None else Hb
+    g = orc.update_geometry(m, Hi, Hb, ssa["SL"])
+    f = dict(ssa, Hi=Hi, Hb=Hb)
+    for k in ("Hi_Ac", "Hb_Ac", "dHs_dx_shelf", "dHs_dy_shelf", "dHs_dx_shelf_Ac", "dHs_dy_shelf_Ac"):
+        f[k] = g[k]
+    return f, g
+
+
+@pytest.mark.parametrize("name,kind", [("1k", "dome"), ("1k", "marine")])
+def test_coulomb_vjp_matches_cpu_reference_and_finite_differences(name, kind):
+    """The reference's Coulomb_regularised law: the transposed sweep carries each grounded
+    row's S'(u) block. Against the CPU reference at the GPU's converged state: the adjoint
+    state, dJ/dlog(tau_c), dJ/dphi_fric, the driving-stress sensitivity and dJ/dHi (<= 1e-8).
+    Against central finite differences of the GPU forward solve (<= 1e-5): dJ/dHi, and on the
+    marine bed (away from the friction law's clamps at Hb = 0) dJ/dHb through tau_c and the
+    surface slope, which checks the friction gradient through the reference's own input."""
+    api.init(0)
+    m = oracle_aaac(name)
+    ssa, sia, g = oracle_inputs(m, kind)
+    dm = api.DeviceMesh(m)
+    p = api.default_params(precision=nat.UFE_FP64, sliding_law=nat.UFE_SLIDING_COULOMB_REGULARISED, **TIGHT)
+
+    def solve(f):
+        rc, out, st = dm.solve_ssa(f, p)
+        assert rc == 0 and st["last_RN"] < 1e-12, st
+        return adj.aaac_velocity(out), out
+
+    H, Hb, SL = (np.asarray(ssa[k], dtype=np.float64) for k in ("Hi", "Hb", "SL"))
+    x, y = m.base.V[:, 0], m.base.V[:, 1]
+    bump = 20.0 * np.exp(-((x - 2e5) ** 2 + (y + 1e5) ** 2) / (2 * (1.5e5) ** 2))
+    (Uo, Vo), _ = solve(geometry_fields(m, ssa, Hi=np.where(H > 0, H + bump, H))[0])
+    (U, V), out0 = solve(ssa)           # the handle now holds the solve the VJP differentiates
+    gU, gV = U - Uo, V - Vo
+    dJ = dict(zip(("U_SSA", "Ux_SSA_Ac"), split(m, gU)))
+    dJ.update(zip(("V_SSA", "Uy_SSA_Ac"), split(m, gV)))
+    rc, vo, st = dm.ssa_vjp(dJ, p, geom_mesh=m)
+    assert rc == nat.UFE_OK, st
+    lin = adj.Linearisation(m, ssa, U, V, tau_c=out0["tau_c_AaAc"])
+    assert np.any(lin.fr > 0)
+    G = adj.geometry_matrix(m, H, Hb, SL)
+    mx, my, dlt, dHi, sens = adj.adjoint_gradient(lin, gU, gV, G)
+    assert rel_l2(vo["lambda_U_AaAc"], mx) <= REF_TOL
+    assert rel_l2(vo["lambda_V_AaAc"], my) <= REF_TOL
+    assert rel_l2(vo["dJ_dlogbeta_sq_AaAc"], dlt) <= REF_TOL
+    assert rel_l2(vo["dJ_dhx_AaAc"], sens["hx"]) <= REF_TOL
+    assert rel_l2(vo["dJ_dHi"], dHi) <= REF_TOL
+    assert np.all(vo["dJ_dHi_AaAc"] == 0.0)     # the friction term does not depend on Hi
+    r = np.pi / 180.0
+    phi = out0["phi_fric_AaAc"]
+    assert rel_l2(vo["dJ_dphi_fric_AaAc"], dlt * r / (np.sin(r * phi) * np.cos(r * phi))) <= REF_TOL
+    rng = np.random.default_rng(17)
+    h = 1e-3
+    flot = (SL - Hb) * adj.RHO_SW / adj.RHO_I
+    safe = (H > 50.0) & (np.abs(H - flot) > 50.0)
+    J = lambda UV: adj.misfit(UV[0], UV[1], Uo, Vo)
+    for _ in range(2):
+        d = np.where(safe, rng.normal(size=H.size), 0.0)
+        fp = solve(geometry_fields(m, ssa, Hi=H + h * d)[0])[0]
+        fm = solve(geometry_fields(m, ssa, Hi=H - h * d)[0])[0]
+        fd = (J(fp) - J(fm)) / (2 * h)
+        an = float(vo["dJ_dHi"] @ d)
+        assert abs(fd - an) <= FD_TOL * abs(an), (fd, an)
+    if kind == "marine":
+        dHb = adj.coulomb_bed_gradient(m, ssa, vo["dJ_dlogbeta_sq_AaAc"], vo["dJ_dhx_AaAc"], vo["dJ_dhy_AaAc"])
+        for _ in range(2):
+            d = np.where(safe & (np.abs(Hb) > 1.0), rng.normal(size=H.size), 0.0)
+            fp = solve(geometry_fields(m, ssa, Hb=Hb + h * d)[0])[0]
+            fm = solve(geometry_fields(m, ssa, Hb=Hb - h * d)[0])[0]
+            fd = (J(fp) - J(fm)) / (2 * h)
+            an = float(dHb @ d)
+            assert abs(fd - an) <= FD_TOL * abs(an), (fd, an)
+    dm.close()
+
+
+def test_vjp_rejects_missing_solve_and_a_changed_law():
     api.init(0)
     m = oracle_aaac("tiny")
     dm = api.DeviceMesh(m)
@@ -108,8 +185,8 @@ def test_vjp_rejects_coulomb_law_and_missing_solve():
     ssa, sia, g = oracle_inputs(m, "dome")
     p = api.default_params(sliding_law=nat.UFE_SLIDING_COULOMB_REGULARISED)
     dm.solve_ssa(ssa, p)
-    rc, out, st = dm.ssa_vjp(dJ, p, check=False)
-    assert rc == nat.UFE_BAD_ARG and "linear sliding" in nat.last_error()
+    rc, out, st = dm.ssa_vjp(dJ, api.default_params(sliding_law=nat.UFE_SLIDING_LINEAR), check=False)
+    assert rc == nat.UFE_BAD_ARG and "sliding law differs" in nat.last_error()
     dm.close()
 
 

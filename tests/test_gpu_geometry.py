@@ -35,6 +35,39 @@ def test_device_geometry_bit_identical_to_oracle(kind):
     dm.close()
 
 
+@pytest.mark.parametrize("kind,size", [("dome", "4k"), ("marine", "4k"), ("marine", "100k")])
+def test_device_masks_bit_identical_to_oracle(kind, size):
+    """determine_masks in full on the device (land, ocean, lake, ice, sheet, shelf, coast,
+    margin, grounding line, calving front and the type mask, on Aa and Ac) against the
+    oracle's literal restatement, after a geometry update and again after the solve's own
+    geometry upload (the masks are born and stay on the device)."""
+    m = oracle_aaac(size)
+    base = m.base
+    Hi, Hb, SL = wl.dome_geometry(base) if kind == "dome" else wl.marine_geometry(base, seed=20261206)
+    ref = orc.determine_masks(m, Hi, Hb, SL)
+    dm = api.DeviceMesh(m)
+    dm.geometry_attach(m)
+    dm.geometry_update(Hi, Hb, SL)
+    got = dm.geometry_masks()
+    for name in orc.MASK_NAMES:
+        k = "mask" if name == "type" else "mask_" + name
+        assert np.array_equal(got[k], ref["mask_" + name]), k
+        assert np.array_equal(got[k + "_Ac"], ref["mask_" + name + "_Ac"]), k + "_Ac"
+    if kind == "marine":
+        for k in ("mask_coast", "mask_gl", "mask_cf", "mask_margin", "mask_gl_Ac", "mask_cf_Ac"):
+            assert got[k].sum() > 0, k
+        assert set(np.unique(got["mask"])) >= {3, 4, 6, 7, 8}
+    # the SSA's own geometry upload recomputes them from other thickness fields
+    Hi2 = np.where(Hi > 0, Hi * 0.8, 0.0)
+    p = api.default_params(precision=nat.UFE_MIXED)
+    dm.ssa_upload_geometry(Hi2, Hb, SL, np.full(base.nV, wl.A_FLOW), np.full(m.nAc, wl.A_FLOW), p)
+    ref2 = orc.determine_masks(m, Hi2, Hb, SL)
+    got2 = dm.geometry_masks()
+    assert np.array_equal(got2["mask"], ref2["mask_type"]) and np.array_equal(got2["mask_Ac"], ref2["mask_type_Ac"])
+    assert np.array_equal(got2["mask_cf"], ref2["mask_cf"])
+    dm.close()
+
+
 def test_solve_from_device_geometry_matches_host_fields():
     m = oracle_aaac("4k")
     ssa, sia, g = oracle_inputs(m, "marine")

@@ -75,6 +75,15 @@ class SiaOut(ct.Structure):
                                  "U_SIA", "V_SIA", "D_SIA")]
 
 
+MASK_NAMES = ("land", "ocean", "lake", "ice", "sheet", "shelf", "coast", "margin", "gl", "cf")
+MASK_OUT_FIELDS = tuple("mask_" + n for n in MASK_NAMES) + ("mask",) + \
+    tuple("mask_" + n + "_Ac" for n in MASK_NAMES) + ("mask_Ac",)
+
+
+class MaskOut(ct.Structure):
+    _fields_ = [(n, P) for n in MASK_OUT_FIELDS]
+
+
 GEOM_MESH_FIELDS = ("nC", "C", "Nx", "Ny", "Aci", "Nx_Ac", "Ny_Ac", "No_Ac", "Np_Ac")
 
 
@@ -136,7 +145,7 @@ class VjpGeom(ct.Structure):
 
 
 VJP_OUT_FIELDS = ("dJ_dlogbeta_sq_AaAc", "dJ_dHi", "dJ_dhx_AaAc", "dJ_dhy_AaAc", "dJ_dHi_AaAc", "lambda_U_AaAc",
-                  "lambda_V_AaAc")
+                  "lambda_V_AaAc", "dJ_dphi_fric_AaAc")
 
 
 class VjpOut(ct.Structure):
@@ -197,6 +206,7 @@ PROTOTYPES = {
     "ufe_sia_solve_noalloc": (I32, [P, ct.POINTER(Params), ct.POINTER(SiaIn), ct.POINTER(SiaOut)]),
     "ufe_geometry_attach": (I32, [P, ct.POINTER(GeometryMesh)]),
     "ufe_geometry_update": (I32, [P, P, P, P, ct.POINTER(GeometryOut)]),
+    "ufe_geometry_masks": (I32, [P, ct.POINTER(MaskOut)]),
     "ufe_ssa_upload_geometry": (I32, [P, ct.POINTER(Params), P, P, P, P, P, P, ct.POINTER(SsaInout)]),
     "ufe_sia_solve_geometry": (I32, [P, ct.POINTER(Params), P, ct.POINTER(SiaOut)]),
     "ufe_sia3d_solve": (I32, [P, ct.POINTER(Params), P, P, ct.POINTER(Sia3dOut)]),

@@ -352,6 +352,18 @@ class DeviceMesh:
             raise nat.UfeError(rc, "ufe_geometry_update")
         return out
 
+    def geometry_masks(self) -> dict:
+        """Every mask of determine_masks from the last device geometry (ufe_geometry_masks):
+        mask_<name> (nV) and mask_<name>_Ac (nAc) for each of nat.MASK_NAMES, plus the type
+        masks mask (nV) and mask_Ac (nAc)."""
+        L = nat.load()
+        out = {k: np.zeros(self.nAc if k.endswith("_Ac") else self.nV, dtype=np.int32) for k in nat.MASK_OUT_FIELDS}
+        mo = nat.MaskOut(*(out[k].ctypes.data for k in nat.MASK_OUT_FIELDS))
+        rc = L.ufe_geometry_masks(self._h, ct.byref(mo))
+        if rc != nat.UFE_OK:
+            raise nat.UfeError(rc, "ufe_geometry_masks")
+        return out
+
     def ssa_upload_geometry(self, Hi, Hb, SL, A_flow_mean, A_flow_mean_Ac, params: dict, beta=None,
                             warm: dict | None = None):
         """ufe_ssa_upload_geometry: the solve's inputs derived on the device from Hi, Hb, SL.

@@ -10,6 +10,7 @@
 //
 // With it a time step uploads Hi, Hb, SL (and the flow factor) instead of about twenty
 // derived fields, and the solve's inputs are born on the device.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -44,13 +45,18 @@ struct GeomWork {
   double *upw = nullptr;       // U, V, d in; ddx, ddy out (nV x nZ each)
   int upw_nZ = 0;
   unsigned long long *upw_missing = nullptr;
+  // determine_masks in full: one 16-bit word per Aa vertex then per Ac edge (mask bits and
+  // the type mask), and a staging array for handing single masks back
+  unsigned short *pk = nullptr;
+  int *mask_stage = nullptr;
   bool computed = false;
 };
 
 void geom_free(GeomWork *w) {
   if (!w) return;
   void *ptrs[] = {w->nC, w->C, w->Aci, w->Nx, w->Ny, w->Nx_Ac, w->Ny_Ac, w->No_Ac, w->Np_Ac, w->dbl, w->msk, w->beta, w->thk, w->thk_int, w->sia3d, w->props,
-                   w->tV, w->tR, w->NxTri, w->NyTri, w->niTri, w->iTri, w->Tri, w->upw, w->upw_missing};
+                   w->tV, w->tR, w->NxTri, w->NyTri, w->niTri, w->iTri, w->Tri, w->upw, w->upw_missing, w->pk,
+                   w->mask_stage};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete w;
@@ -185,6 +191,92 @@ __global__ void k_geom_ac2(const GeomArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// determine_masks in full (general_ice_model_data_module.f90:97-297). Every mask of a vertex
+// or edge is one bit of a 16-bit word, the type mask (the last type the routine assigns, in
+// its order) in the top four bits. The Aa pass reads the neighbours' ocean / ice / sheet /
+// shelf masks that k_geom_aa1 wrote (the reference's first loop, 146-167, completes before
+// the neighbour loop, 171-225, reads it); the Ac pass reads its own maps and the two end
+// vertices' masks (230-294). mask_lake is never set by the routine and stays 0.
+// ---------------------------------------------------------------------------------------
+enum MaskBit : int {
+  kMkLand = 0, kMkOcean, kMkLake, kMkIce, kMkSheet, kMkShelf, kMkCoast, kMkMargin, kMkGl, kMkCf, kMkBits
+};
+enum MaskType : int {
+  kTypeLand = 0, kTypeOcean = 1, kTypeLake = 2, kTypeSheet = 3, kTypeShelf = 4, kTypeCoast = 5, kTypeMargin = 6,
+  kTypeGl = 7, kTypeCf = 8
+};
+constexpr int kTypeShift = 12;
+
+__device__ __forceinline__ unsigned short mask_word(unsigned bits, int type) {
+  return (unsigned short)(bits | ((unsigned)type << kTypeShift));
+}
+
+__global__ void k_masks_aa(const GeomArgs a, unsigned short *pk) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.nV) return;
+  const int *ocean = AAM(a, M_OCEAN), *ice = AAM(a, M_ICE), *sheet = AAM(a, M_SHEET), *shelf = AAM(a, M_SHELF);
+  const int o = ocean[v], i = ice[v], sh = sheet[v], sf = shelf[v];
+  const int land = !o;
+  int type = kTypeLand;
+  unsigned bits = (land << kMkLand) | (o << kMkOcean) | (i << kMkIce) | (sh << kMkSheet) | (sf << kMkShelf);
+  if (o) type = kTypeOcean;
+  if (sh) type = kTypeSheet;
+  if (sf) type = kTypeShelf;
+  // neighbour conditions, each over all neighbours, in the routine's order
+  int coast = 0, margin = 0, gl = 0, cf = 0;
+  const int n = a.nC[v];
+  const size_t ld = a.nV;
+  for (int c = 0; c < n; ++c) {
+    const int j = a.C[v + c * ld] - 1;
+    const int oj = ocean[j];
+    coast |= land & oj;
+    margin |= i & (ice[j] == 0);
+    gl |= sh & shelf[j];
+    cf |= i & oj;
+  }
+  if (coast) type = kTypeCoast;
+  if (margin) type = kTypeMargin;
+  if (gl) type = kTypeGl;
+  if (cf) type = kTypeCf;
+  bits |= (coast << kMkCoast) | (margin << kMkMargin) | (gl << kMkGl) | (cf << kMkCf);
+  pk[v] = mask_word(bits, type);
+}
+
+__global__ void k_masks_ac(const GeomArgs a, unsigned short *pk) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nAc) return;
+  const int o = ACM(a, MC_OCEAN)[c], i = ACM(a, MC_ICE)[c], sh = ACM(a, MC_SHEET)[c], sf = ACM(a, MC_SHELF)[c];
+  const int land = !o;
+  int type = kTypeLand;
+  unsigned bits = (land << kMkLand) | (o << kMkOcean) | (i << kMkIce) | (sh << kMkSheet) | (sf << kMkShelf);
+  if (o) type = kTypeOcean;
+  if (sh) type = kTypeSheet;
+  if (sf) type = kTypeShelf;
+  const int vi = a.Aci[c] - 1, vj = a.Aci[c + a.nAc] - 1;
+  const unsigned wi = pk[vi], wj = pk[vj];
+  auto bit = [](unsigned w, int k) { return (int)((w >> k) & 1u); };
+  const int coast = (bit(wi, kMkLand) && bit(wj, kMkOcean)) || (bit(wj, kMkLand) && bit(wi, kMkOcean));
+  const int margin = (bit(wi, kMkIce) && !bit(wj, kMkIce)) || (bit(wj, kMkIce) && !bit(wi, kMkIce));
+  const int gl = (bit(wi, kMkSheet) && bit(wj, kMkShelf)) || (bit(wj, kMkSheet) && bit(wi, kMkShelf));
+  const int cf = (bit(wi, kMkIce) && !bit(wj, kMkShelf) && bit(wj, kMkOcean)) ||
+                 (bit(wj, kMkIce) && !bit(wi, kMkShelf) && bit(wi, kMkOcean));
+  if (coast) type = kTypeCoast;
+  if (margin) type = kTypeMargin;
+  if (gl) type = kTypeGl;
+  if (cf) type = kTypeCf;
+  bits |= (coast << kMkCoast) | (margin << kMkMargin) | (gl << kMkGl) | (cf << kMkCf);
+  pk[a.nV + c] = mask_word(bits, type);
+}
+
+// One mask (bit k, or the type for k = kMkBits) of n words as the reference's INTEGER array.
+__global__ void k_mask_unpack(int n, const unsigned short *pk, int k, int *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned w = pk[i];
+  out[i] = k == kMkBits ? (int)(w >> kTypeShift) : (int)((w >> k) & 1u);
+}
+
 GeomArgs args_of(GeomWork *w) {
   GeomArgs a;
   a.nV = w->nV; a.nAc = w->nAc; a.ncm = w->ncm;
@@ -214,6 +306,8 @@ int compute(ufe_mesh_h h, const double *Hi, const double *Hb, const double *SL) 
   if (!rc) { k_geom_ac1<<<gc, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_ac1"); }
   if (!rc) { k_geom_aa2<<<gv, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_aa2"); }
   if (!rc) { k_geom_ac2<<<gc, 256, 0, s>>>(a); rc = cuda_status(cudaGetLastError(), "k_geom_ac2"); }
+  if (!rc) { k_masks_aa<<<gv, 256, 0, s>>>(a, w->pk); rc = cuda_status(cudaGetLastError(), "k_masks_aa"); }
+  if (!rc) { k_masks_ac<<<gc, 256, 0, s>>>(a, w->pk); rc = cuda_status(cudaGetLastError(), "k_masks_ac"); }
   w->computed = rc == UFE_OK;
   return rc;
 }
@@ -417,6 +511,8 @@ extern "C" int ufe_geometry_attach(ufe_mesh_h h, const ufe_geometry_mesh *g) {
   if (!rc) rc = cuda_status(cudaMalloc(&w->Np_Ac, nac * sizeof(double)), "geometry");
   if (!rc) rc = cuda_status(cudaMalloc(&w->dbl, ((size_t)A_COUNT * nv + (size_t)C_COUNT * nac) * sizeof(double)), "geometry");
   if (!rc) rc = cuda_status(cudaMalloc(&w->msk, ((size_t)M_COUNT * nv + (size_t)MC_COUNT * nac) * sizeof(int)), "geometry");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->pk, (nv + nac) * sizeof(unsigned short)), "geometry masks");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->mask_stage, std::max(nv, nac) * sizeof(int)), "geometry masks");
   if (!rc) rc = up(w->nC, g->nC, nv, s);
   if (!rc) rc = up(w->C, g->C, nv * nc, s);
   if (!rc) rc = up(w->Aci, g->Aci, 4 * nac, s);
@@ -470,6 +566,37 @@ extern "C" int ufe_geometry_update(ufe_mesh_h h, const double *Hi, const double 
     di(out->mask_gl_Ac, ACM(a, MC_GL), nAc);
   }
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "geometry update");
+  return rc;
+}
+
+extern "C" int ufe_geometry_masks(ufe_mesh_h h, ufe_mask_out *out) {
+  if (!h || !out) { set_error("ufe_geometry_masks: null argument"); return UFE_BAD_ARG; }
+  if (!h->geom || !h->geom->computed) {
+    set_error("ufe_geometry_masks: no device geometry (ufe_geometry_update or ufe_ssa_upload_geometry first)");
+    return UFE_BAD_ARG;
+  }
+  GeomWork *w = h->geom;
+  cudaStream_t s = h->stream;
+  int32_t *aa[kMkBits + 1] = {out->mask_land, out->mask_ocean, out->mask_lake, out->mask_ice, out->mask_sheet,
+                              out->mask_shelf, out->mask_coast, out->mask_margin, out->mask_gl, out->mask_cf,
+                              out->mask};
+  int32_t *ac[kMkBits + 1] = {out->mask_land_Ac, out->mask_ocean_Ac, out->mask_lake_Ac, out->mask_ice_Ac,
+                              out->mask_sheet_Ac, out->mask_shelf_Ac, out->mask_coast_Ac, out->mask_margin_Ac,
+                              out->mask_gl_Ac, out->mask_cf_Ac, out->mask_Ac};
+  int rc = UFE_OK;
+  // one staging array, reused in stream order: each unpack waits for the previous copy
+  auto one = [&](int32_t *dst, const unsigned short *src, int n, int k) {
+    if (!dst || rc) return;
+    k_mask_unpack<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, src, k, w->mask_stage);
+    rc = cuda_status(cudaGetLastError(), "k_mask_unpack");
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(dst, w->mask_stage, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s),
+                              "masks D2H");
+  };
+  for (int k = 0; k <= kMkBits; ++k) {
+    one(aa[k], w->pk, w->nV, k);
+    one(ac[k], w->pk + w->nV, w->nAc, k);
+  }
+  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "geometry masks");
   return rc;
 }
 

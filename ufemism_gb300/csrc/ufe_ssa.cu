@@ -1353,7 +1353,10 @@ struct AdjSetup {
   const double2 *nxy, *h_nxy, *h_cuv;
   const double *sNxy;
   const double *Hi, *Hb, *SL, *hx, *hy, *Af, *beta;
+  const double *tau;                           // Coulomb_regularised: the solve's basal yield stress
   double beta_const, m_enh;
+  int coulomb;                                 // 1: Coulomb_regularised law, 0: linear (S = beta^2)
+  double uq, expo;                             // Coulomb: u_threshold^q and (q - 1) / 2
   const double2 *UV;
   const double *dJ_U, *dJ_V, *dJ_Ux, *dJ_Uy;   // caller order, staged on the device
   double2 *ee, *kh, *alpha, *dinv, *g, *mu;
@@ -1410,17 +1413,24 @@ __global__ void k_adj_rows(const AdjSetup a) {
   const double pexp = (1.0 - 3.0) / (2.0 * 3.0);
   const double eta = pow((a.m_enh * 0.5) * a.Af[p], -1.0 / 3.0) * pow(eps2, pexp);
   const double mH = fmax(0.1, a.Hi[p]);
-  const double S = a.beta ? a.beta[p] : a.beta_const;
-  const double fr = is_floating(a.Hi[p], a.Hb[p], a.SL[p]) ? 0.0 : S / (mH * eta);
+  const bool floating = is_floating(a.Hi[p], a.Hb[p], a.SL[p]);
+  // sliding coefficient at the converged velocities (SSA_sliding_term, ice_dynamics_module.f90:727-779)
+  const double wv = (1e-3 * 1e-3 + ui.x * ui.x) + ui.y * ui.y;
+  const double S = a.coulomb ? (a.tau[p] * pow(wv, a.expo)) / a.uq : (a.beta ? a.beta[p] : a.beta_const);
+  const double fr = floating ? 0.0 : S / (mH * eta);
   const double rg = kIceDensity * kGrav;
   const double2 hc = a.h_cuv[p];
-  const double eu = hc.x - fr, ev = hc.y - fr;
+  // The Coulomb law's S depends on the row's own velocity: d(fr u)/du adds the symmetric 2x2
+  // block 2 expo fr / w [U U, U V; V U, V V] (w = dv^2 + U^2 + V^2) to the row's diagonal and
+  // cross coefficients.
+  const double cS = (a.coulomb && !floating) ? (2.0 * a.expo) * fr / wv : 0.0;
+  const double eu = hc.x - fr - cS * ui.x * ui.x, ev = hc.y - fr - cS * ui.y * ui.y;
   // dF/deta * deta/d(eps2): alpha = p (fr u + rho g h / eta) / eps2
   const double ax = pexp * (fr * ui.x + rg * a.hx[p] / eta) / eps2;
   const double ay = pexp * (fr * ui.y + rg * a.hy[p] / eta) / eps2;
   const double kU = K1 * hn.x + K2 * hn.y, kV = K2 * hn.x + K3 * hn.y;
   a.ee[p] = make_double2(eu, ev);
-  a.c3[p] = 3.0 * a.sNxy[p];
+  a.c3[p] = 3.0 * a.sNxy[p] - cS * ui.x * ui.y;
   a.kh[p] = make_double2(kU, kV);
   a.alpha[p] = make_double2(ax, ay);
   a.dinv[p] = make_double2(1.0 / (eu + kU * ax), 1.0 / (ev + kV * ay));
@@ -1471,7 +1481,10 @@ struct AdjGrad {
   const uint8_t *slice_g;
   const double2 *UV, *mu;
   const double *eta, *fr, *Hi;
+  int coulomb;
+  const double *phi;                                       // Coulomb: till friction angle (degrees)
   double *d_logbeta, *s_hx, *s_hy, *s_H, *lam_U, *lam_V;   // [nA] caller order
+  double *d_phi;                                           // [nA] caller order, Coulomb only
 };
 
 __global__ void k_adj_grad(const AdjGrad a) {
@@ -1484,15 +1497,25 @@ __global__ void k_adj_grad(const AdjGrad a) {
   a.lam_V[r] = m.y;
   if (a.slice_g[p / kSlice] == 5) {
     a.d_logbeta[r] = 0.0; a.s_hx[r] = 0.0; a.s_hy[r] = 0.0; a.s_H[r] = 0.0;
+    if (a.coulomb) a.d_phi[r] = 0.0;
     return;
   }
   const double2 u = a.UV[p];
+  // S is proportional to beta^2 (linear law) or to tau_c (Coulomb law): dF/dlog(coefficient)
+  // = -fr u on the row, so both laws share the gradient with respect to the log coefficient.
   const double w = a.fr[p] * fma(m.x, u.x, m.y * u.y);
   const double rg = kIceDensity * kGrav;
   a.d_logbeta[r] = w;
   a.s_hx[r] = rg * m.x / a.eta[p];
   a.s_hy[r] = rg * m.y / a.eta[p];
-  a.s_H[r] = a.Hi[p] > 0.1 ? -w / a.Hi[p] : 0.0;
+  // Coulomb: tau_c and the friction denominator both carry max(0.1, Hi), so the friction
+  // term does not depend on the thickness.
+  a.s_H[r] = (!a.coulomb && a.Hi[p] > 0.1) ? -w / a.Hi[p] : 0.0;
+  if (a.coulomb) {
+    // tau_c = tan(phi pi / 180) X (basal_yield_stress, 780-844): dlog(tau_c)/dphi = (pi / 180) / (sin cos)
+    const double ph = a.phi[p] * (kPi / 180.0);
+    a.d_phi[r] = w * (kPi / 180.0) / (sin(ph) * cos(ph));
+  }
 }
 
 // dJ/dHi on Aa from the field sensitivities: Hi_AaAc (identity on Aa rows, the mean of the
@@ -1734,6 +1757,7 @@ struct SsaWork {
   bool uploaded = false;
   bool has_beta = false, has_N = false, gl = false;
   bool zero = false;             // the reference's early-out applies
+  int sliding_law = -1;          // law of the last prepared solve
   int grid[3] = {0, 0, 0};        // per SweepMode, one CTA per SM
   int block = kSsaBlock;
 };
@@ -1983,6 +2007,7 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->beta_const = p->beta_sq;
   a->max_inner = p->SSA_max_inner_loops; a->max_outer = p->SSA_max_outer_loops;
   a->sliding_law = p->sliding_law; a->has_beta = w->has_beta;
+  w->sliding_law = p->sliding_law;
   a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 32;
   a->fp32_visc = p->mixed_fp32_viscosity != 0;
   a->timeout_ns = wait_timeout_ns();
@@ -2751,7 +2776,7 @@ struct AdjWork {
   double2 *cT = nullptr, *kT = nullptr;
   double2 *ee = nullptr, *kh = nullptr, *alpha = nullptr, *dinv = nullptr, *g = nullptr, *mu = nullptr;
   double *c3 = nullptr, *s = nullptr, *eta = nullptr, *fr = nullptr, *inv_nb = nullptr, *K = nullptr;
-  double *stage = nullptr;        // dJ/du in (4 blocks), sensitivities out (6 nA), dHi (nV)
+  double *stage = nullptr;        // dJ/du in (4 blocks), sensitivities out (6 nA), dHi (nV), dJ/dphi (nA)
   int *geom_int = nullptr;        // nC, C, Aci
   double *geom_dbl = nullptr;     // Nx, Ny, Nx_Ac, Ny_Ac
   unsigned int *prog = nullptr;
@@ -2795,7 +2820,7 @@ int ensure_adj(ufe_mesh_h h) {
   for (double **q : d1)
     if (!rc) rc = cuda_status(cudaMalloc(q, nP * sizeof(double)), "adj rows");
   if (!rc) rc = cuda_status(cudaMalloc(&w->K, 3 * nP * sizeof(double)), "adj strain");
-  if (!rc) rc = cuda_status(cudaMalloc(&w->stage, (2 * nV + 2 * nAc + 6 * nA + nV) * sizeof(double)), "adj stage");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->stage, (2 * nV + 2 * nAc + 7 * nA + nV) * sizeof(double)), "adj stage");
   if (!rc) rc = cuda_status(cudaMalloc(&w->geom_int, (nV + nV * ncm + 4 * nAc) * sizeof(int)), "adj geom");
   if (!rc) rc = cuda_status(cudaMalloc(&w->geom_dbl, (2 * nV * (ncm + 1) + 8 * nAc) * sizeof(double)), "adj geom");
   if (!rc) rc = cuda_status(cudaMalloc(&w->prog, 32 * (size_t)m.n_patch * sizeof(unsigned int)), "adj progress");
@@ -3012,8 +3037,13 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   if (!w || !w->uploaded) { set_error("ufe_ssa_vjp: no solve on this mesh handle"); return UFE_BAD_ARG; }
   if (w->zero) { set_error("ufe_ssa_vjp: the last solve took the zero-velocity early-out"); return UFE_BAD_ARG; }
   if (w->gl) { set_error("ufe_ssa_vjp: the grounding-line flux option is not differentiated"); return UFE_BAD_ARG; }
-  if (p->sliding_law != UFE_SLIDING_LINEAR) {
-    set_error("ufe_ssa_vjp: the adjoint is implemented for the linear sliding law (S = beta^2)");
+  if (p->sliding_law != UFE_SLIDING_LINEAR && p->sliding_law != UFE_SLIDING_COULOMB_REGULARISED) {
+    set_error("ufe_ssa_vjp: unknown sliding law");
+    return UFE_BAD_ARG;
+  }
+  const bool coulomb = p->sliding_law == UFE_SLIDING_COULOMB_REGULARISED;
+  if (coulomb != (w->sliding_law == UFE_SLIDING_COULOMB_REGULARISED)) {
+    set_error("ufe_ssa_vjp: the sliding law differs from the one of the last solve");
     return UFE_BAD_ARG;
   }
   if (!in->dJ_dU || !in->dJ_dV || !in->dJ_dUx_Ac || !in->dJ_dUy_Ac) { set_error("ufe_ssa_vjp: missing dJ/du"); return UFE_BAD_ARG; }
@@ -3037,7 +3067,7 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   double *st = a->stage;
   double *gU = st, *gV = st + nV, *gUx = st + 2 * nV, *gUy = gUx + nAc;
   double *o_lb = gUy + nAc, *o_hx = o_lb + nA, *o_hy = o_hx + nA, *o_H = o_hy + nA, *o_lU = o_H + nA, *o_lV = o_lU + nA;
-  double *o_dHi = o_lV + nA;
+  double *o_dHi = o_lV + nA, *o_phi = o_dHi + nV;
   std::memset(a->ctl_host, 0, sizeof(AdjCtl));
   rc = cuda_status(cudaEventRecord(a->ev0, s), "event");
   if (!rc) rc = h2d(gU, in->dJ_dU, nV, s);
@@ -3052,6 +3082,8 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   su.orig_of_dev = m.orig_of_dev; su.nxy = m.nxy; su.h_nxy = m.h_nxy; su.h_cuv = m.h_cuv; su.sNxy = m.sNxy;
   su.Hi = F + F_HI * nP; su.Hb = F + F_HB * nP; su.SL = F + F_SL * nP; su.hx = F + F_HX * nP; su.hy = F + F_HY * nP;
   su.Af = F + F_AF * nP; su.beta = w->has_beta ? F + F_BETA * nP : nullptr;
+  su.tau = F + F_TAU * nP; su.coulomb = coulomb ? 1 : 0;
+  su.uq = std::pow(100.0, 0.30); su.expo = 0.5 * (0.30 - 1.0);   // u_threshold, q_plastic (727-779)
   su.beta_const = p->beta_sq; su.m_enh = p->m_enh_ssa; su.UV = w->UV;
   su.dJ_U = gU; su.dJ_V = gV; su.dJ_Ux = gUx; su.dJ_Uy = gUy;
   su.ee = a->ee; su.kh = a->kh; su.alpha = a->alpha; su.dinv = a->dinv; su.g = a->g; su.mu = a->mu;
@@ -3107,7 +3139,9 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   AdjGrad ag;
   ag.nP = (int)nP; ag.nV = (int)nV; ag.orig_of_dev = m.orig_of_dev; ag.deg = m.deg; ag.slice_g = m.slice_g;
   ag.UV = w->UV; ag.mu = a->mu; ag.eta = a->eta; ag.fr = a->fr; ag.Hi = F + F_HI * nP;
+  ag.coulomb = coulomb ? 1 : 0; ag.phi = F + F_PHI * nP;
   ag.d_logbeta = o_lb; ag.s_hx = o_hx; ag.s_hy = o_hy; ag.s_H = o_H; ag.lam_U = o_lU; ag.lam_V = o_lV;
+  ag.d_phi = o_phi;
   if (!rc) {
     k_adj_grad<<<gb, 256, 0, s>>>(ag);
     rc = cuda_status(cudaGetLastError(), "k_adj_grad");
@@ -3143,6 +3177,7 @@ extern "C" int ufe_ssa_vjp(ufe_mesh_h h, const ufe_params *p, const ufe_vjp_para
   if (!rc) rc = d2h(out->lambda_U_AaAc, o_lU, nA, s);
   if (!rc) rc = d2h(out->lambda_V_AaAc, o_lV, nA, s);
   if (!rc && out->dJ_dHi) rc = d2h(out->dJ_dHi, o_dHi, nV, s);
+  if (!rc && coulomb) rc = d2h(out->dJ_dphi_fric_AaAc, o_phi, nA, s);
   if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "ssa vjp");
   if (rc) return rc;
   float ms = 0.f;
