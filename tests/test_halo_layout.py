@@ -1,0 +1,225 @@
+"""The halo sweep program of the device layout, checked on the host (no GPU).
+
+ufe_debug_dump_layout writes the layout ufe_mesh_create would upload for a 152-SM GPU. The
+test checks every index of the halo program against the buffers it addresses, then emulates
+the halo sweeps in numpy exactly as the kernel runs them (each patch's working copy: own rows
+carried over, halo slots reloaded from the buffer the other patches wrote in the previous
+sweep; seven phases; own rows written to the other buffer) and compares them, after several
+sweeps, with a plain sequential coloured sweep over the whole mesh (colours 1..5, then the
+edge rows as the mean of their non-edge neighbours, then the corners as the mean of all
+theirs, the order of solve_SSA_linearised and apply_Neumann_boundary_AaAc). The update rule is
+the same in both, so equality must be exact: the program reads every value at the point of
+the sweep the sequential order reads it.
+"""
+import ctypes as ct
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import base_mesh
+
+from ufemism_gb300 import _native as nat
+from ufemism_gb300 import api
+
+NO_COL = 0xFFFF
+DT = {1: np.uint8, 2: np.uint16, 4: np.int32, 8: np.float64}
+
+
+def dump_layout(mesh, num_sms=152):
+    d, keep = api._mesh_desc(mesh)
+    L = nat.load()
+    fn = L.ufe_debug_dump_layout
+    fn.restype = ct.c_int
+    fn.argtypes = [ct.POINTER(nat.MeshDesc), ct.c_int, ct.c_int, ct.c_char_p]
+    fd, path = tempfile.mkstemp(suffix=".bin")
+    os.close(fd)
+    try:
+        rc = fn(ct.byref(d), num_sms, 0, path.encode())
+        assert rc == nat.UFE_OK, nat.last_error()
+        out = {}
+        with open(path, "rb") as f:
+            while True:
+                head = f.read(32)
+                if not head:
+                    break
+                name = head.split(b"\0")[0].decode()
+                es = f.read(1)[0]
+                n = int(np.frombuffer(f.read(8), dtype=np.int64)[0])
+                raw = f.read(es * n)
+                out[name] = (es, n, raw)
+    finally:
+        os.unlink(path)
+    arr = {}
+    for name, (es, n, raw) in out.items():
+        if name in ("cuv", "hcuv"):
+            arr[name] = np.frombuffer(raw, dtype=np.float64).reshape(-1, 2)
+        elif name in ("cuv32", "hcuv32"):
+            arr[name] = np.frombuffer(raw, dtype=np.float32).reshape(-1, 2)
+        elif name == "slice_ptr":
+            arr[name] = np.frombuffer(raw, dtype=np.int64)
+        else:
+            arr[name] = np.frombuffer(raw, dtype=DT[es])
+    return arr
+
+
+@pytest.fixture(scope="module", params=["tiny", "1k", "4k"])
+def layout(request):
+    base = base_mesh(request.param)
+    mesh = api.build_aaac(base)
+    return mesh, dump_layout(mesh)
+
+
+def phases_of(mesh, lay):
+    """Phase of each device row: its colour (0..4), 5 for edge rows, 6 for the corners."""
+    nV = mesh.base.nV
+    edge = np.concatenate([np.asarray(mesh.base.edge_index) > 0, np.asarray(mesh.edge_index_Ac) > 0])
+    colour = np.asarray(mesh.colour) - 1
+    orig = lay["orig_of_dev"]
+    ph = np.full(orig.size, -1, dtype=np.int64)
+    ok = orig >= 0
+    r = orig[ok]
+    ph[ok] = np.where(r < 4, 6, np.where(edge[r], 5, colour[r]))
+    return ph, edge
+
+
+def test_halo_program_indices_in_bounds(layout):
+    mesh, lay = layout
+    n_patch, nP, nSlices, max_local, has_halo, n_hs, nA, nV = (int(x) for x in lay["sizes"])
+    assert has_halo == 1
+    hp = lay["hp_slice"]
+    assert hp.size == 7 * n_patch + 1 and hp[0] == 0 and hp[-1] == n_hs and np.all(np.diff(hp) >= 0)
+    e0, w = lay["hslice_e0"], lay["hslice_w"]
+    nE = lay["hcol"].size
+    assert e0.size == n_hs and np.all(e0.astype(np.int64) + 32 * w.astype(np.int64) <= nE)
+    assert lay["hrow_l"].size == 32 * n_hs and lay["hrow_g"].size == 32 * n_hs
+    assert lay["hcuv"].shape[0] == nE and lay["hcuv32"].shape[0] == nE
+    assert np.all((lay["hrow_g"] >= 0) & (lay["hrow_g"] < nP))
+    assert np.all((lay["hload_dev"] >= 0) & (lay["hload_dev"] < nP))
+    ps = lay["patch_slice"].reshape(n_patch, 7)
+    hl = lay["hload_ptr"]
+    for b in range(n_patch):
+        n_own = int(ps[b, 6] - ps[b, 0]) * 32
+        n_loc = n_own + int(hl[b + 1] - hl[b])
+        assert n_loc <= max_local
+        s0, s1 = int(hp[7 * b]), int(hp[7 * b + 7])
+        assert s1 - s0 <= 1024
+        rl = lay["hrow_l"][32 * s0:32 * s1]
+        assert np.all((rl >= -1) & (rl < n_loc))
+        for s in range(s0, s1):
+            cols = lay["hcol"][e0[s]:e0[s] + 32 * int(w[s])]
+            assert np.all((cols == NO_COL) | (cols < n_loc))
+        # every row is updated by exactly its owner among the own slots
+        g = lay["hrow_g"][32 * s0:32 * s1][rl >= 0]
+        own = rl[rl >= 0] < n_own
+        assert np.all((g[own] >= ps[b, 0] * 32) & (g[own] < ps[b, 6] * 32))
+        assert np.all((g[~own] < ps[b, 0] * 32) | (g[~own] >= ps[b, 6] * 32))
+    sp, sl = lay["hsync_ptr"], lay["hsync_list"]
+    assert sp.size == n_patch + 1 and np.all(sl < n_patch)
+    for b in range(n_patch):     # symmetric: a patch waits for every patch it reads and reads it back
+        for q in sl[sp[b]:sp[b + 1]]:
+            assert b in sl[sp[q]:sp[q + 1]]
+
+
+def _update(nb, c, ui, rhs, e, s3, omega=1.3):
+    """One colour-row update (any fixed rule of the neighbours in order, the row and its data)."""
+    su = 0.0
+    sv = 0.0
+    for (x, y), (cx, cy) in zip(nb, c):
+        su = su + x * cx
+        sv = sv + y * cy
+    ru = ((su + s3 * ui[1]) + e[0] * ui[0] - rhs[0]) / e[0]
+    rv = ((sv + s3 * ui[0]) + e[1] * ui[1] - rhs[1]) / e[1]
+    return (ui[0] - omega * ru, ui[1] - omega * rv)
+
+
+def _mean(vals, ncm=16):
+    sx = 0.0
+    sy = 0.0
+    for x, y in vals:
+        sx = sx + x
+        sy = sy + y
+    n = len(vals)
+    if n < ncm:
+        sx = sx + 0.0
+        sy = sy + 0.0
+    return (sx / n, sy / n)
+
+
+def test_halo_sweeps_equal_the_sequential_sweep(layout):
+    mesh, lay = layout
+    n_patch, nP, nSlices, max_local, has_halo, n_hs, nA, nV = (int(x) for x in lay["sizes"])
+    ph, edge = phases_of(mesh, lay)
+    orig = lay["orig_of_dev"]
+    dev = lay["dev_of_orig"]
+    rng = np.random.default_rng(7)
+    U0 = rng.normal(size=(nP, 2))
+    rhs = rng.normal(size=(nP, 2))
+    e = 4.0 + rng.random(size=(nP, 2))
+    s3 = rng.normal(size=nP) * 0.1
+    skip = np.zeros(nP, dtype=bool)
+    ac_rows = np.flatnonzero((orig >= nV) & (ph >= 0) & (ph < 5))
+    skip[rng.choice(ac_rows, size=max(1, ac_rows.size // 50), replace=False)] = True   # Dirichlet rows
+    CA = np.asarray(mesh.CAaAc) - 1
+    nCA = np.asarray(mesh.nCAaAc)
+    col, cuv, sptr = lay["col"], lay["cuv"], lay["slice_ptr"]
+
+    def entries(p):
+        s, l = divmod(p, 32)
+        n = nCA[orig[p]]
+        idx = sptr[s] + np.arange(n) * 32 + l
+        return col[idx], cuv[idx]
+
+    # sequential reference: colours, edges, corners on one array
+    sweeps = 3
+    U = U0.copy()
+    for _ in range(sweeps):
+        for f in range(5):
+            for p in np.flatnonzero(ph == f):
+                if skip[p]:
+                    continue
+                cj, cc = entries(p)
+                U[p] = _update([U[j] for j in cj], cc, U[p], rhs[p], e[p], s3[p])
+        for p in np.flatnonzero(ph == 5):
+            r = orig[p]
+            U[p] = _mean([U[dev[CA[r, c]]] for c in range(nCA[r]) if not edge[CA[r, c]]])
+        for p in np.flatnonzero(ph == 6):
+            r = orig[p]
+            U[p] = _mean([U[dev[CA[r, c]]] for c in range(nCA[r])])
+
+    # the halo program, patches as if concurrent: halo slots from buf[par], own rows to buf[par ^ 1]
+    ps = lay["patch_slice"].reshape(n_patch, 7)
+    hp, e0, w = lay["hp_slice"], lay["hslice_e0"], lay["hslice_w"]
+    hl, hd = lay["hload_ptr"], lay["hload_dev"]
+    rowl, rowg, hcol, hcuv = lay["hrow_l"], lay["hrow_g"], lay["hcol"], lay["hcuv"]
+    buf = [U0.copy(), U0.copy()]
+    local = []
+    for b in range(n_patch):
+        p0, n_own = ps[b, 0] * 32, (ps[b, 6] - ps[b, 0]) * 32
+        local.append(np.concatenate([U0[p0:p0 + n_own], np.zeros((hl[b + 1] - hl[b], 2))]))
+    par = 0
+    for _ in range(sweeps):
+        for b in range(n_patch):
+            ld = local[b]
+            p0, n_own = ps[b, 0] * 32, (ps[b, 6] - ps[b, 0]) * 32
+            ld[n_own:] = buf[par][hd[hl[b]:hl[b + 1]]]
+            for f in range(7):
+                for s in range(hp[7 * b + f], hp[7 * b + f + 1]):
+                    for lane in range(32):
+                        l, g = rowl[32 * s + lane], rowg[32 * s + lane]
+                        if l < 0 or (f < 5 and skip[g]):
+                            continue
+                        ks = [k for k in range(w[s]) if hcol[e0[s] + 32 * k + lane] != NO_COL]
+                        cj = [hcol[e0[s] + 32 * k + lane] for k in ks]
+                        if f < 5:
+                            cc = [hcuv[e0[s] + 32 * k + lane] for k in ks]
+                            ld[l] = _update([ld[j] for j in cj], cc, ld[l], rhs[g], e[g], s3[g])
+                        else:
+                            ld[l] = _mean([ld[j] for j in cj])
+                        if l < n_own:
+                            buf[par ^ 1][g] = ld[l]
+        par ^= 1
+    got = buf[par]
+    live = ph >= 0
+    assert np.array_equal(got[live], U[live])

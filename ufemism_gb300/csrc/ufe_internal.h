@@ -100,6 +100,33 @@ struct DevMesh {
   int2 *Aci12 = nullptr;        // [nAc] (vi, vj) 0-based
   int *iAci = nullptr;          // [nV * ncm] column-major Ac ids (0-based), for map_Ac_to_Aa
   int *nC = nullptr;            // [nV]
+
+  // Halo sweep program (single solves). One SOR sweep runs in seven phases: colours 1..5,
+  // then the edge rows, then the corners. A patch updates, besides its own rows, the halo
+  // rows whose updates its own rows read within the same sweep (the closure of "reads a row
+  // of an earlier phase"), with the same arithmetic, so that a whole sweep needs the
+  // neighbouring patches only once, at its start. Its working copy of the velocities
+  // (shared memory) holds its own device rows [p0, p1) at local index p - p0, then its halo
+  // rows. The program lists, per phase, slices of 32 (local row, device row) slots with
+  // their entries as local columns and coefficients, in the reference's neighbour order.
+  bool has_halo = false;
+  int max_local = 0;            // largest own slots + halo rows of a patch
+  int max_hslices = 0;          // largest number of program slices of a patch
+  int max_hsync = 0;
+  int n_hslices = 0;
+  int64_t n_hE = 0;
+  int *hp_slice = nullptr;      // [n_patch * 7 + 1] first program slice of phases 0..6 of each patch, then the end
+  int *hslice_e0 = nullptr;     // [n_hslices] first entry of a program slice
+  uint8_t *hslice_w = nullptr;  // [n_hslices] entries per slot
+  int *hrow_l = nullptr;        // [n_hslices * 32] local row, -1 = padding
+  int *hrow_g = nullptr;        // [n_hslices * 32] device row
+  uint16_t *hcol = nullptr;     // [n_hE] local column, 0xffff = padding
+  float2 *hcuv32 = nullptr;     // [n_hE]
+  double2 *hcuv = nullptr;      // [n_hE]
+  int *hload_ptr = nullptr;     // [n_patch + 1] a patch's halo rows in hload_dev
+  int *hload_dev = nullptr;     // device row of each halo slot
+  int *hsync_ptr = nullptr;     // [n_patch + 1] patches a patch waits for / is waited for by
+  int *hsync_list = nullptr;
 };
 
 struct SsaWork;   // per-handle device buffers of the SSA solve (ufe_ssa.cu)

@@ -4,6 +4,7 @@
 // colour_vi, CAaAc and the N*_AaAc coefficient columns; mesh_ArakawaC_module.f90:583-724 walks
 // CAaAc for derivatives and the Neumann boundary) with one upload per mesh.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -28,11 +29,37 @@ int upload(T **p, const std::vector<T> &h, cudaStream_t s, const char *what) {
   return cuda_status(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s), what);
 }
 
+// Host-only layout dump (tests): set by ufe_debug_dump_layout around a mesh_create that
+// stops before touching the device and writes its host arrays to a file instead. Each record:
+// a 32-byte name, an element-size byte, an element count (int64), the raw elements.
+thread_local const char *t_dump_path = nullptr;
+thread_local int t_dump_sms = 0;
+
+struct LayoutDump {
+  FILE *fp;
+  bool good;
+  explicit LayoutDump(const char *path) : fp(std::fopen(path, "wb")), good(fp != nullptr) {}
+  ~LayoutDump() { if (fp) std::fclose(fp); }
+  bool ok() const { return good; }
+  template <class T>
+  void put(const char *name, const std::vector<T> &v) {
+    if (!good) return;
+    char head[32] = {0};
+    std::snprintf(head, sizeof head, "%s", name);
+    const uint8_t es = (uint8_t)sizeof(T);
+    const int64_t n = (int64_t)v.size();
+    good = std::fwrite(head, 1, 32, fp) == 32 && std::fwrite(&es, 1, 1, fp) == 1 && std::fwrite(&n, 8, 1, fp) == 1 &&
+           (n == 0 || std::fwrite(v.data(), sizeof(T), (size_t)n, fp) == (size_t)n);
+  }
+};
+
 void free_mesh(DevMesh &m) {
   void *ptrs[] = {m.orig_of_dev, m.dev_of_orig, m.deg, m.slice_ptr, m.col, m.cuv, m.nxy,
                   m.cuv32, m.nxy32, m.h_nxy, m.h_cuv, m.sNxy, m.s3Nxy, m.h_nxy32, m.s3Nxy32, m.bnd_ptr,
                   m.bnd_nbr, m.V, m.Aci12, m.iAci, m.nC, m.patch_slice, m.patch_edge0, m.edge_row,
-                  m.sync_ptr, m.sync_list, m.slice_e0, m.slice_w, m.slice_g};
+                  m.sync_ptr, m.sync_list, m.slice_e0, m.slice_w, m.slice_g, m.hp_slice, m.hslice_e0,
+                  m.hslice_w, m.hrow_l, m.hrow_g, m.hcol, m.hcuv32, m.hcuv, m.hload_ptr, m.hload_dev,
+                  m.hsync_ptr, m.hsync_list};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   m = DevMesh();
@@ -99,9 +126,14 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
       if (CA(r, c) < 4) { set_error("ufe_mesh_create: corner connected to corner"); return UFE_BAD_MESH; }
 
   int dev = 0, num_sms = 0;
-  int rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
-  if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
-  if (rc || num_sms < 1) return UFE_NO_DEVICE;
+  int rc = UFE_OK;
+  if (t_dump_path) {
+    num_sms = t_dump_sms;   // host-only layout dump: no device is touched
+  } else {
+    rc = cuda_status(cudaGetDevice(&dev), "cudaGetDevice");
+    if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+    if (rc || num_sms < 1) return UFE_NO_DEVICE;
+  }
 
   // ---- spatial patches: one per CTA of the persistent solver ------------------------------
   // Rows in Morton order of their coordinates (Aa vertex, or the midpoint of the Ac edge),
@@ -303,6 +335,144 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
   m.max_sync = max_sync;
   if (max_sync > kMaxSync) { set_error("ufe_mesh_create: a patch touches too many other patches"); return UFE_BAD_MESH; }
 
+  // ---- halo sweep program (single solves only) --------------------------------------------
+  // Phases of a sweep: colours 0..4 (non-edge rows), 5 edge rows, 6 corners; an update reads
+  // CAaAc neighbours (edge rows: the non-edge ones). A patch must also update every row of an
+  // earlier phase that one of its updates reads (transitively): such a row is current only
+  // after its own update in this sweep. Everything else it reads is a start-of-sweep value.
+  std::vector<int> hp_slice, hslice_e0, hrow_l, hrow_g, hload_ptr(1, 0), hload_dev, hsync_ptr(1, 0), hsync_list;
+  std::vector<uint8_t> hslice_w;
+  std::vector<uint16_t> hcol;
+  std::vector<float2> hcuv32;
+  std::vector<double2> hcuv;
+  bool halo_ok = n_patch_request == 0;
+  if (halo_ok) {
+    std::vector<int8_t> ph(m.nP, -1);
+    for (int p = 0; p < m.nP; ++p) {
+      const int r = orig_of_dev[p];
+      if (r >= 0) ph[p] = (int8_t)(r < 4 ? 6 : is_edge(r) ? 5 : colour_of[r]);
+    }
+    auto reads_of = [&](int p, std::vector<int> &out) {
+      out.clear();
+      const int r = orig_of_dev[p];
+      for (int c = 0; c < d->nCAaAc[r]; ++c) {
+        const int j = CA(r, c);
+        if (ph[p] == 5 && is_edge(j)) continue;
+        out.push_back(dev_of_orig[j]);
+      }
+    };
+    std::vector<int> in_r(m.nP, -1), lidx(m.nP, -1), stamp(m.nP, -1), rd;
+    std::vector<std::vector<int>> hreads(n_patch);
+    int64_t nE_h = 0;
+    for (int b = 0; b < n_patch && halo_ok; ++b) {
+      const int p0 = patch_slice[(size_t)b * (kGroups + 1)] * kSlice;
+      const int p1 = patch_slice[(size_t)b * (kGroups + 1) + kGroups] * kSlice;
+      std::vector<int> R;
+      for (int p = p0; p < p1; ++p)
+        if (ph[p] >= 0) { in_r[p] = b; R.push_back(p); }
+      for (size_t k = 0; k < R.size(); ++k) {
+        reads_of(R[k], rd);
+        for (int j : rd)
+          if (ph[j] < ph[R[k]] && in_r[j] != b) { in_r[j] = b; R.push_back(j); }
+      }
+      // local slots: own device rows first, then the halo rows (every row read or updated)
+      const int n_own = p1 - p0;
+      std::vector<int> halo;
+      auto local_of = [&](int p) {
+        if (p >= p0 && p < p1) return p - p0;
+        if (stamp[p] != b) { stamp[p] = b; lidx[p] = n_own + (int)halo.size(); halo.push_back(p); }
+        return lidx[p];
+      };
+      for (int p : R) {
+        local_of(p);
+        reads_of(p, rd);
+        for (int j : rd) local_of(j);
+      }
+      if (n_own + (int)halo.size() > 65535) { halo_ok = false; break; }
+      m.max_local = std::max(m.max_local, n_own + (int)halo.size());
+      for (int p : halo) hreads[b].push_back(patch_of[orig_of_dev[p]]);
+      hload_dev.insert(hload_dev.end(), halo.begin(), halo.end());
+      hload_ptr.push_back((int)hload_dev.size());
+      // program: per phase, the own rows in device order (keeping the device slices of the
+      // colour groups, so per-row loads stay coalesced), then the halo rows by degree
+      const int first_slice = (int)hslice_e0.size();
+      for (int f = 0; f < 7; ++f) {
+        hp_slice.push_back((int)hslice_e0.size());
+        std::vector<int> rows;   // device rows, -1 = padding slot
+        if (f < 5) {
+          const int g0 = patch_slice[(size_t)b * (kGroups + 1) + f] * kSlice;
+          const int g1 = patch_slice[(size_t)b * (kGroups + 1) + f + 1] * kSlice;
+          for (int p = g0; p < g1; ++p) rows.push_back(ph[p] == f ? p : -1);
+        } else {
+          for (int p = p0; p < p1; ++p)
+            if (ph[p] == f) rows.push_back(p);
+          while (rows.size() % kSlice) rows.push_back(-1);
+        }
+        std::vector<int> hrows;
+        for (int p : R)
+          if ((p < p0 || p >= p1) && ph[p] == f) hrows.push_back(p);
+        std::stable_sort(hrows.begin(), hrows.end(), [&](int x, int y) { return d->nCAaAc[orig_of_dev[x]] > d->nCAaAc[orig_of_dev[y]]; });
+        rows.insert(rows.end(), hrows.begin(), hrows.end());
+        while (rows.size() % kSlice) rows.push_back(-1);
+        for (size_t s0 = 0; s0 < rows.size(); s0 += kSlice) {
+          int w = 0;
+          for (int l = 0; l < kSlice; ++l) {
+            const int p = rows[s0 + l];
+            if (p < 0) continue;
+            reads_of(p, rd);
+            w = std::max(w, (int)rd.size());
+          }
+          hslice_e0.push_back((int)nE_h);
+          hslice_w.push_back((uint8_t)w);
+          hcol.resize((size_t)nE_h + (size_t)w * kSlice, 0xffff);
+          hcuv32.resize((size_t)nE_h + (size_t)w * kSlice, make_float2(0, 0));
+          hcuv.resize((size_t)nE_h + (size_t)w * kSlice, make_double2(0, 0));
+          for (int l = 0; l < kSlice; ++l) {
+            const int p = rows[s0 + l];
+            hrow_l.push_back(p < 0 ? -1 : local_of(p));
+            hrow_g.push_back(p < 0 ? 0 : p);
+            if (p < 0) continue;
+            reads_of(p, rd);
+            // the device SELL entries of p hold the same neighbours in the same order (the
+            // edge rows' list skips their edge neighbours: their coefficients are unused)
+            const int s = p / kSlice, ln = p % kSlice;
+            for (size_t k = 0; k < rd.size(); ++k) {
+              const size_t e = (size_t)nE_h + k * kSlice + l;
+              hcol[e] = (uint16_t)local_of(rd[k]);
+              if (f < 5) {
+                const int64_t ed = slice_ptr[s] + (int64_t)k * kSlice + ln;
+                hcuv32[e] = cuv32[ed];
+                hcuv[e] = cuv[ed];
+              }
+            }
+          }
+          nE_h += (int64_t)w * kSlice;
+        }
+      }
+      m.max_hslices = std::max(m.max_hslices, (int)hslice_e0.size() - first_slice);
+      if (m.max_hslices > kMaxPatchSlices || nE_h >= ((int64_t)1 << 31)) halo_ok = false;
+    }
+    if (halo_ok) {
+      hp_slice.push_back((int)hslice_e0.size());   // end of the last patch
+      // the start-of-sweep wait: the owners of a patch's halo rows, and the patches that read it
+      std::vector<std::vector<int>> hs(n_patch);
+      for (int b = 0; b < n_patch; ++b)
+        for (int q : hreads[b])
+          if (q != b) { hs[b].push_back(q); hs[q].push_back(b); }
+      for (int b = 0; b < n_patch; ++b) {
+        std::sort(hs[b].begin(), hs[b].end());
+        hs[b].erase(std::unique(hs[b].begin(), hs[b].end()), hs[b].end());
+        m.max_hsync = std::max(m.max_hsync, (int)hs[b].size());
+        hsync_list.insert(hsync_list.end(), hs[b].begin(), hs[b].end());
+        hsync_ptr.push_back((int)hsync_list.size());
+      }
+      if (m.max_hsync > kMaxSync) halo_ok = false;
+      m.n_hslices = (int)hslice_e0.size();
+      m.n_hE = nE_h;
+    }
+  }
+  m.has_halo = halo_ok;
+
   // ---- geometry ---------------------------------------------------------------------------
   std::vector<double2> V(nV);
   for (int v = 0; v < nV; ++v) V[v] = make_double2(d->V[v], d->V[v + (int64_t)nV]);
@@ -323,6 +493,21 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
       if (c < nC[v] && (a < 0 || a >= nAc)) { set_error("ufe_mesh_create: iAci out of range"); return UFE_BAD_MESH; }
       iAci[v + (size_t)c * nV] = c < nC[v] ? a : 0;
     }
+  }
+
+  if (t_dump_path) {
+    LayoutDump f(t_dump_path);
+    if (!f.ok()) { set_error("ufe_debug_dump_layout: cannot write the file"); return UFE_BAD_ARG; }
+    const std::vector<int> sizes = {n_patch, m.nP, m.nSlices, m.max_local, m.has_halo ? 1 : 0, m.n_hslices, nA, nV};
+    f.put("sizes", sizes);
+    f.put("orig_of_dev", orig_of_dev); f.put("dev_of_orig", dev_of_orig); f.put("deg", deg);
+    f.put("patch_slice", patch_slice); f.put("slice_ptr", slice_ptr); f.put("slice_w", slice_w); f.put("col", col);
+    f.put("cuv", cuv); f.put("cuv32", cuv32); f.put("sync_ptr", sync_ptr); f.put("sync_list", sync_list);
+    f.put("hp_slice", hp_slice); f.put("hslice_e0", hslice_e0); f.put("hslice_w", hslice_w);
+    f.put("hrow_l", hrow_l); f.put("hrow_g", hrow_g); f.put("hcol", hcol); f.put("hcuv", hcuv);
+    f.put("hcuv32", hcuv32); f.put("hload_ptr", hload_ptr); f.put("hload_dev", hload_dev);
+    f.put("hsync_ptr", hsync_ptr); f.put("hsync_list", hsync_list);
+    return f.ok() ? UFE_OK : UFE_BAD_ARG;
   }
 
   // ---- upload -------------------------------------------------------------------------------
@@ -360,6 +545,20 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
   if (!rc) rc = upload(&m.slice_e0, slice_e0, S, "slice_e0");
   if (!rc) rc = upload(&m.slice_w, slice_w, S, "slice_w");
   if (!rc) rc = upload(&m.slice_g, slice_g, S, "slice_g");
+  if (!rc && m.has_halo) {
+    rc = upload(&m.hp_slice, hp_slice, S, "hp_slice");
+    if (!rc) rc = upload(&m.hslice_e0, hslice_e0, S, "hslice_e0");
+    if (!rc) rc = upload(&m.hslice_w, hslice_w, S, "hslice_w");
+    if (!rc) rc = upload(&m.hrow_l, hrow_l, S, "hrow_l");
+    if (!rc) rc = upload(&m.hrow_g, hrow_g, S, "hrow_g");
+    if (!rc) rc = upload(&m.hcol, hcol, S, "hcol");
+    if (!rc) rc = upload(&m.hcuv32, hcuv32, S, "hcuv32");
+    if (!rc) rc = upload(&m.hcuv, hcuv, S, "hcuv");
+    if (!rc) rc = upload(&m.hload_ptr, hload_ptr, S, "hload_ptr");
+    if (!rc) rc = upload(&m.hload_dev, hload_dev, S, "hload_dev");
+    if (!rc) rc = upload(&m.hsync_ptr, hsync_ptr, S, "hsync_ptr");
+    if (!rc) rc = upload(&m.hsync_list, hsync_list, S, "hsync_list");
+  }
   if (!rc) rc = cuda_status(cudaStreamSynchronize(S), "mesh upload");
   h->m = m;
   if (rc) {
@@ -375,6 +574,19 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
 }  // namespace ufe
 
 extern "C" int ufe_mesh_create(const ufe_mesh_desc *d, ufe_mesh_h *out) { return mesh_create(d, 0, out); }
+
+// Test hook (not part of the public header): the device layout ufe_mesh_create would upload
+// for a GPU of `num_sms` SMs, built on the host alone and written to `path` (record format
+// in LayoutDump), so that its index arrays and the halo program can be checked without a GPU.
+extern "C" int ufe_debug_dump_layout(const ufe_mesh_desc *d, int num_sms, int n_patch, const char *path) {
+  if (!path || num_sms < 1) { set_error("ufe_debug_dump_layout: bad argument"); return UFE_BAD_ARG; }
+  t_dump_path = path;
+  t_dump_sms = num_sms;
+  ufe_mesh_h h = nullptr;
+  const int rc = mesh_create(d, n_patch, &h);
+  t_dump_path = nullptr;
+  return rc;
+}
 
 extern "C" int ufe_mesh_destroy(ufe_mesh_h h) {
   if (!h) return UFE_OK;

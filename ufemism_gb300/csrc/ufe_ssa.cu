@@ -38,6 +38,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "ufe_internal.h"
@@ -98,6 +99,14 @@ struct SsaArgs {
   const int *edge_row;
   const int *sync_ptr;
   const int *sync_list;
+  // halo sweep program (DevMesh, ufe_internal.h)
+  const int *hp_slice, *hslice_e0;
+  const uint8_t *hslice_w;
+  const int *hrow_l, *hrow_g;
+  const uint16_t *hcol;
+  const float2 *hcuv32;
+  const double2 *hcuv;
+  const int *hload_ptr, *hload_dev, *hsync_ptr, *hsync_list;
   unsigned int *prog;      // per-CTA progress counters (stride 32 words)
   int nP;
   int nSlices;
@@ -107,6 +116,8 @@ struct SsaArgs {
   const uint8_t *skip;    // Dirichlet rows (grounding-line Ac rows under the GL-flux option), may be null
   double2 *UV;            // FP64 velocities (u0 in the mixed path)
   float2 *dUV;            // mixed: correction d
+  double2 *UVb;           // halo sweeps, FP64 modes: the second velocity buffer
+  float2 *dUVb;           // halo sweeps, mixed: the second correction buffer
   float2 *r0;             // mixed: defect
   float2 *rcp32;          // mixed: FP32 reciprocals of (eu, ev)
   double *eta, *Na, *Nb, *S;
@@ -444,6 +455,10 @@ struct PatchSmem {
   int edge0, edge1;
   int nsync;
   int sync[kMaxSync];
+  // halo sweeps: program slices of the 7 phases (e0, w hold the program's slices), the own
+  // device rows [p0, p0 + n_own) and the halo slots [n_own, n_own + nh) of the working copy
+  int hps[8];
+  int p0, n_own, nh, hl0;
 };
 
 // One colour of the FP64 sweep in the reference's expression order (parity mode).
@@ -668,6 +683,205 @@ __device__ void phase_boundary(const SsaArgs &a, const PatchSmem &ps, const Loca
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Halo sweeps: one phase of the sweep program over this patch's working copy `ld` (shared
+// memory; own rows, then halo rows). Every update uses the arithmetic, and the neighbour
+// order, of the phased sweeps above, so an own row gets the same value either way; own rows
+// are also written to `out` (the buffer the neighbours read at the next sweep's start) and
+// alone enter the maximum residual.
+// ---------------------------------------------------------------------------------------
+constexpr uint16_t kNoCol = 0xffff;
+
+__device__ __forceinline__ int halo_global(const SsaArgs &a, const PatchSmem &ps, int l) {
+  return l < ps.n_own ? ps.p0 + l : a.hload_dev[ps.hl0 + l - ps.n_own];
+}
+
+// Colour phase f of the FP32 correction sweep (as phase_sweep32).
+__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, float2 *ld, float2 *out) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+  const float omega = (float)a.omega;
+  float mx = 0.0f;
+  const int base = ps.hps[0];
+  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
+    const int w = ps.w[s - base];
+    const int64_t e0 = ps.e0[s - base] + lane;
+    const int slot = s * kSlice + lane;
+    const int l = a.hrow_l[slot];
+    const int g = a.hrow_g[slot];
+    int j[kBatch];
+    float2 c[kBatch];
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q) {
+      j[q] = q < w ? (int)a.hcol[e0 + (int64_t)q * kSlice] : (int)kNoCol;
+      c[q] = q < w ? a.hcuv32[e0 + (int64_t)q * kSlice] : make_float2(0.f, 0.f);
+    }
+    const float s3 = a.s3Nxy32[g];
+    const float2 r = a.rcp32[g];
+    const float2 d = a.r0[g];
+    if (l < 0 || (a.skip && a.skip[g])) continue;   // padding slot, or a Dirichlet row
+    const float2 di = ld[l];
+    float su = 0.0f, sv = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q) {
+      if (j[q] != (int)kNoCol) {
+        const float2 u = ld[j[q]];
+        su = fmaf(u.x, c[q].x, su);
+        sv = fmaf(u.y, c[q].y, sv);
+      }
+    }
+    for (int k = kBatch; k < w; ++k) {
+      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+      if (jj == (int)kNoCol) break;
+      const float2 cc = a.hcuv32[e0 + (int64_t)k * kSlice];
+      const float2 v = ld[jj];
+      su = fmaf(v.x, cc.x, su);
+      sv = fmaf(v.y, cc.y, sv);
+    }
+    const float ru = fmaf(fmaf(s3, di.y, su) - d.x, r.x, di.x);
+    const float rv = fmaf(fmaf(s3, di.x, sv) - d.y, r.y, di.y);
+    const float2 dn = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
+    ld[l] = dn;
+    if (l < ps.n_own) {
+      out[g] = dn;
+      mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
+    }
+  }
+  return abs_bits((double)mx);
+}
+
+// Colour phase f of the FP64 sweeps (as phase_sweep_exact and phase_sweep_fast).
+template <bool kExact>
+__device__ unsigned long long halo_colour64(const SsaArgs &a, const PatchSmem &ps, int f, double2 *ld, double2 *out) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+  const double omega = a.omega;
+  unsigned long long mx = 0ull;
+  const int base = ps.hps[0];
+  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
+    const int w = ps.w[s - base];
+    const int64_t e0 = ps.e0[s - base] + lane;
+    const int slot = s * kSlice + lane;
+    const int l = a.hrow_l[slot];
+    const int g = a.hrow_g[slot];
+    if (l < 0 || (a.skip && a.skip[g])) continue;
+    double su = 0.0, sv = 0.0;
+    double ru, rv;
+    const double2 ui = ld[l];
+    if (kExact) {
+      for (int k = 0; k < w; ++k) {
+        const int64_t e = e0 + (int64_t)k * kSlice;
+        const int jj = a.hcol[e];
+        if (jj == (int)kNoCol) break;
+        const double2 c = a.hcuv[e];
+        const double2 u = ld[jj];
+        su = su + u.x * c.x;
+        sv = sv + u.y * c.y;
+      }
+      const double sxy = a.sNxy[g];
+      const double Uxy = ui.x * sxy, Vxy = ui.y * sxy;
+      const double2 ec = a.euv[g];
+      const double2 b = a.rhs[g];
+      const double lhsx = (su + 3.0 * Vxy) + ec.x * ui.x;
+      const double lhsy = (sv + 3.0 * Uxy) + ec.y * ui.y;
+      ru = (lhsx - b.x) / ec.x;
+      rv = (lhsy - b.y) / ec.y;
+    } else {
+      int j[kBatch];
+#pragma unroll
+      for (int q = 0; q < kBatch; ++q) j[q] = q < w ? (int)a.hcol[e0 + (int64_t)q * kSlice] : (int)kNoCol;
+      const double s3 = a.s3Nxy[g];
+      const double2 r = a.rcp[g];
+      const double2 b = a.rhs[g];
+#pragma unroll
+      for (int q = 0; q < kBatch; ++q) {
+        if (j[q] != (int)kNoCol) {
+          const double2 c = a.hcuv[e0 + (int64_t)q * kSlice];
+          const double2 u = ld[j[q]];
+          su = fma(u.x, c.x, su);
+          sv = fma(u.y, c.y, sv);
+        }
+      }
+      for (int k = kBatch; k < w; ++k) {
+        const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+        if (jj == (int)kNoCol) break;
+        const double2 c = a.hcuv[e0 + (int64_t)k * kSlice];
+        const double2 u = ld[jj];
+        su = fma(u.x, c.x, su);
+        sv = fma(u.y, c.y, sv);
+      }
+      ru = fma(fma(s3, ui.y, su) - b.x, r.x, ui.x);
+      rv = fma(fma(s3, ui.x, sv) - b.y, r.y, ui.y);
+    }
+    const double2 un = kExact ? make_double2(ui.x - omega * ru, ui.y - omega * rv)
+                              : make_double2(fma(-omega, ru, ui.x), fma(-omega, rv, ui.y));
+    ld[l] = un;
+    if (l < ps.n_own) {
+      out[g] = un;
+      const unsigned long long bu = abs_bits(ru), bv = abs_bits(rv);
+      mx = bu > mx ? bu : mx;
+      mx = bv > mx ? bv : mx;
+    }
+  }
+  return mx;
+}
+
+// Boundary phase f (5: edge rows, 6: corners) of apply_Neumann_boundary_AaAc: the mean of the
+// listed neighbours (edge rows: the non-edge ones; corners: all, the edge rows among them
+// already updated in phase 5), as phase_boundary.
+template <bool kM, class T>
+__device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *ld, T *out) {
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+  const int base = ps.hps[0];
+  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
+    const int w = ps.w[s - base];
+    const int64_t e0 = ps.e0[s - base] + lane;
+    const int slot = s * kSlice + lane;
+    const int l = a.hrow_l[slot];
+    if (l < 0) continue;
+    const int g = a.hrow_g[slot];
+    double sx = 0.0, sy = 0.0;
+    int nvals = 0;
+    for (int k = 0; k < w; ++k) {
+      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+      if (jj == (int)kNoCol) break;
+      double2 u;
+      if constexpr (kM) {
+        u = a.UV[halo_global(a, ps, jj)];
+        const float2 dj = reinterpret_cast<const float2 *>(ld)[jj];
+        u.x = u.x + (double)dj.x;
+        u.y = u.y + (double)dj.y;
+      } else {
+        u = reinterpret_cast<const double2 *>(ld)[jj];
+      }
+      sx = sx + u.x;
+      sy = sy + u.y;
+      ++nvals;
+    }
+    if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
+    const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
+    T nv;
+    if constexpr (kM) {
+      const double2 u0 = a.UV[g];
+      nv = make_float2((float)(v.x - u0.x), (float)(v.y - u0.y));
+    } else {
+      nv = v;
+    }
+    ld[l] = nv;
+    if (l < ps.n_own) out[g] = nv;
+  }
+}
+
+// Halo slots of the working copy from the buffer the neighbours wrote in the last sweep.
+template <class T>
+__device__ __forceinline__ void halo_load(const SsaArgs &a, const PatchSmem &ps, T *ld, const T *in) {
+  for (int i = threadIdx.x; i < ps.nh; i += blockDim.x) ld[ps.n_own + i] = in[a.hload_dev[ps.hl0 + i]];
+}
+
+// Own rows of the working copy into a global buffer.
+template <class T>
+__device__ __forceinline__ void halo_store_own(const PatchSmem &ps, const T *ld, T *dst) {
+  for (int i = threadIdx.x; i < ps.n_own; i += blockDim.x) dst[ps.p0 + i] = ld[i];
+}
+
 // Mixed path: u0 += d, d = 0 on every row.
 template <class Team>
 __device__ void phase_fold(const SsaArgs &a, const Team &t) {
@@ -856,23 +1070,63 @@ __device__ __forceinline__ void load_patch(const Args &a, int b, PatchSmem &ps) 
   __syncthreads();
 }
 
+// Patch b's halo program (phase slice ranges and slice table), own rows, halo slots and the
+// patches of its start-of-sweep wait into shared memory.
+__device__ __forceinline__ void load_patch_halo(const SsaArgs &a, int b, PatchSmem &ps) {
+  if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
+  if (threadIdx.x < 8) ps.hps[threadIdx.x] = a.hp_slice[b * 7 + threadIdx.x];
+  if (threadIdx.x == 0) {
+    ps.nsync = a.hsync_ptr[b + 1] - a.hsync_ptr[b];
+    ps.hl0 = a.hload_ptr[b];
+    ps.nh = a.hload_ptr[b + 1] - a.hload_ptr[b];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ps.p0 = ps.ps[0] * kSlice;
+    ps.n_own = (ps.ps[kGroups] - ps.ps[0]) * kSlice;
+  }
+  for (int i = threadIdx.x; i < ps.nsync; i += blockDim.x) ps.sync[i] = a.hsync_list[a.hsync_ptr[b] + i];
+  for (int s = ps.hps[0] + threadIdx.x; s < ps.hps[7]; s += blockDim.x) {
+    ps.e0[s - ps.hps[0]] = a.hslice_e0[s];
+    ps.w[s - ps.hps[0]] = a.hslice_w[s];
+  }
+  __syncthreads();
+}
+
 // The whole solve_SSA of one problem, run by the CTAs of a team (each CTA owns one patch).
 // Returns false when a bounded wait failed; the error is recorded in the problem's control
-// block and the team's barrier counter.
-template <int kMode, class Team>
+// block and the team's barrier counter. kHalo: the halo sweeps (one neighbour wait per
+// sweep, the patch's working copy in shared memory, velocities double-buffered by sweep).
+template <int kMode, class Team, bool kHalo = false>
 __device__ bool solve_member(const SsaArgs &a, Team &t) {
   constexpr bool kM = kMode == kMixed;
+  using T = typename std::conditional<kM, float2, double2>::type;
   SsaCtl *ctl = a.ctl;
-  unsigned int phases = 0;   // colour phases completed by this patch
+  unsigned int phases = 0;   // colour phases (halo sweeps: sweeps) completed by this patch
   const bool leader = t.rank() == 0 && threadIdx.x == 0;
   __shared__ PatchSmem ps;
-  load_patch(a, t.rank(), ps);
+  if constexpr (kHalo) load_patch_halo(a, t.rank(), ps);
+  else load_patch(a, t.rank(), ps);
   extern __shared__ __align__(16) unsigned char ufe_local_rows[];
   const LocalRows lc{ufe_local_rows, ps.ps[0] * kSlice,
                      (kMode != kExact64 && a.local_rows) ? (ps.ps[kGroups] - ps.ps[0]) * kSlice : 0};
+  T *const hbuf0 = reinterpret_cast<T *>(kM ? (void *)a.dUV : (void *)a.UV);
+  T *const hbuf1 = reinterpret_cast<T *>(kM ? (void *)a.dUVb : (void *)a.UVb);
+  T *const hld = reinterpret_cast<T *>(ufe_local_rows);
   // (Re)load the mirror from global memory: at the start and after the grid-wide phases
-  // that rewrite every row (fold, reset).
+  // that rewrite every row (fold, reset). Halo sweeps: the own rows of the working copy, also
+  // copied into the second buffer, which then holds every row that no sweep writes (Dirichlet
+  // rows) as well.
   auto reload = [&]() {
+    if constexpr (kHalo) {
+      for (int i = threadIdx.x; i < ps.n_own; i += blockDim.x) {
+        const T v = hbuf0[ps.p0 + i];
+        hld[i] = v;
+        hbuf1[ps.p0 + i] = v;
+      }
+      __syncthreads();
+      return;
+    }
     if (!lc.n) return;
     for (int i = threadIdx.x; i < lc.n; i += blockDim.x) {
       if (kM) static_cast<float2 *>(lc.base)[i] = a.dUV[lc.p0 + i];
@@ -915,6 +1169,131 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
     bool lin_done = false;
     int did_reset = 0;
     double maxres = 0.0;
+    if constexpr (kHalo) {
+      // Halo sweeps. A sweep waits once for the patches whose rows it reads (they finished
+      // the previous sweep, so the buffer `par` holds their rows) and for those that read its
+      // rows (they are done reading the buffer it is about to write), loads its halo slots,
+      // runs the seven phases on its working copy with CTA barriers only, and writes its own
+      // rows to buffer par ^ 1. Sync points commit the own rows to the canonical buffer.
+      constexpr bool kLag = kM && kMixedLag > 0;
+      int par = 0;
+      bool synced = true;
+      int decided = 0;
+      const unsigned int base = gsweep;
+      UFE_TM(kTmOther);
+      while (!lin_done && sweeps < a.max_inner) {
+        ++sweeps;
+        UFE_TM_COUNT(kTmSweeps);
+        const unsigned int G = gsweep++;
+        const int slot = sweeps % 3;
+        if (!kLag && leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
+        if (!synced) wait_neighbours(a, ps, phases, t.bar());
+        halo_load(a, ps, hld, par ? hbuf1 : hbuf0);
+        __syncthreads();
+        UFE_TM(kTmWaitColour);
+        T *const out = par ? hbuf0 : hbuf1;
+        unsigned long long mx = 0ull;
+        for (int f = 0; f < 5; ++f) {
+          if (ps.hps[f + 1] == ps.hps[f]) continue;
+          unsigned long long m;
+          if constexpr (kM) m = halo_colour32(a, ps, f, hld, out);
+          else m = halo_colour64<kMode == kExact64>(a, ps, f, hld, out);
+          mx = m > mx ? m : mx;
+          __syncthreads();
+        }
+        UFE_TM(kTmColour);
+        for (int f = 5; f < 7; ++f) {
+          if (ps.hps[f + 1] == ps.hps[f]) continue;
+          halo_boundary<kM>(a, ps, f, hld, out);
+          __syncthreads();
+        }
+        UFE_TM(kTmBoundary);
+        par ^= 1;
+        if constexpr (kLag) {
+          lag_arrive(ctl, G, mx);
+          ++phases;
+          publish_progress(a, t, phases);
+          UFE_TM(kTmArrive);
+          synced = false;
+          const bool refold_now = a.refold > 0 && sweeps % a.refold == 0;
+          const bool sync_point = sweeps == a.max_inner || refold_now;
+          if (sync_point) {
+            if (par) halo_store_own(ps, hld, hbuf0);
+            par = 0;
+            UFE_GRID_SYNC();
+            synced = true;
+            UFE_TM(kTmGrid);
+          }
+          const int upto = sync_point ? sweeps : sweeps - kMixedLag;
+          int act = 0;             // 1: converged, 2: diverged
+          while (decided < upto && act == 0) {
+            ++decided;
+            double r;
+            if (!lag_residual(a, t, base + (unsigned)(decided - 1), r)) {
+              if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu;
+              return false;
+            }
+            maxres = r;
+            if (r < a.tol) act = 1;
+            else if (r > 1e6) act = 2;
+          }
+          UFE_TM(kTmDecide);
+          if (act == 1) {
+            lin_done = true;
+          } else if (act == 2) {
+            if (!synced) { UFE_GRID_SYNC(); synced = true; }
+            phase_zero_velocity(a, t, kM);
+            UFE_GRID_SYNC();
+            reload();
+            par = 0;
+            did_reset = 1;
+            lin_done = true;
+          } else if (sweeps == a.max_inner) {
+            if (leader) ctl->not_converged += 1;
+          } else if (refold_now) {
+            phase_fold(a, t);
+            UFE_GRID_SYNC();
+            reload();
+            phase_defect(a, t);
+            UFE_GRID_SYNC();
+          }
+          UFE_TM(kTmOther);
+        } else {
+          block_max_to(&ctl->maxres[slot], mx);
+          UFE_TM(kTmArrive);
+          UFE_GRID_SYNC();
+          UFE_TM(kTmGrid);
+          maxres = __longlong_as_double((long long)*(volatile unsigned long long *)&ctl->maxres[slot]);
+          if (maxres < a.tol) {
+            lin_done = true;
+          } else if (maxres > 1e6) {
+            phase_zero_velocity(a, t, kM);
+            UFE_GRID_SYNC();
+            reload();
+            par = 0;
+            did_reset = 1;
+            lin_done = true;
+          } else if (sweeps == a.max_inner) {
+            if (leader) ctl->not_converged += 1;
+          } else if (kM && a.refold > 0 && sweeps % a.refold == 0) {
+            if (par) halo_store_own(ps, hld, hbuf0);
+            par = 0;
+            UFE_GRID_SYNC();
+            phase_fold(a, t);
+            UFE_GRID_SYNC();
+            reload();
+            phase_defect(a, t);
+            UFE_GRID_SYNC();
+          }
+          UFE_TM(kTmOther);
+        }
+      }
+      // the final own rows into the canonical buffer before the grid-wide phases read it
+      const bool commit = par || (kLag && !synced);
+      if (par) halo_store_own(ps, hld, hbuf0);
+      if (commit) UFE_GRID_SYNC();
+      UFE_TM(kTmGrid);
+    } else
     if constexpr (kM && kMixedLag > 0) {
       // Mixed sweeps with lagged decisions: the boundary phase is a counted phase and the next
       // sweep's first colour waits for the neighbours' boundary rows, so no team barrier
@@ -1084,10 +1463,10 @@ __device__ __forceinline__ void stage_args(SsaArgs &dst, const SsaArgs *src) {
 
 // Single solve: the whole grid is one team; the argument block stays in the kernel's
 // parameter space (constant bank operands cost no registers).
-template <int kMode>
+template <int kMode, bool kHalo>
 __global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(const SsaArgs a) {
   GridTeam t{&a.ctl->bar_count, 0u};
-  solve_member<kMode>(a, t);
+  solve_member<kMode, GridTeam, kHalo>(a, t);
 }
 
 // Ensemble of independent solves in one launch. The grid is cut into teams; a team of T
@@ -1746,6 +2125,8 @@ struct SsaWork {
   double *f = nullptr;           // Hi, Hb, SL, hx, hy, Af, beta, tau, phi, eta, Na, Nb, S
   double2 *UV = nullptr, *rhs = nullptr, *euv = nullptr, *rcp = nullptr;
   float2 *dUV = nullptr, *r0 = nullptr, *rcp32 = nullptr;
+  double2 *UVb = nullptr;        // halo sweeps: second velocity buffer (FP64 modes)
+  float2 *dUVb = nullptr;        // halo sweeps: second correction buffer (mixed)
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   unsigned int *prog = nullptr;
@@ -1758,6 +2139,7 @@ struct SsaWork {
   bool has_beta = false, has_N = false, gl = false;
   bool zero = false;             // the reference's early-out applies
   int sliding_law = -1;          // law of the last prepared solve
+  bool halo_used = false;        // the last single solve ran the halo sweeps
   int grid[3] = {0, 0, 0};        // per SweepMode, one CTA per SM
   int block = kSsaBlock;
 };
@@ -1765,7 +2147,8 @@ struct SsaWork {
 void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
-                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh};
+                  w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh,
+                  w->UVb, w->dUVb};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -1800,24 +2183,28 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc) rc = cuda_status(cudaMalloc(&w->rcp, (size_t)m.nP * sizeof(double2)), "ssa rcp");
   if (!rc) rc = cuda_status(cudaMalloc(&w->rcp32, (size_t)m.nP * sizeof(float2)), "ssa rcp32");
   if (!rc) rc = cuda_status(cudaMalloc(&w->skip, (size_t)m.nP), "ssa skip");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->UVb, (size_t)m.nP * sizeof(double2)), "ssa UVb");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->dUVb, (size_t)m.nP * sizeof(float2)), "ssa dUVb");
   if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(SsaCtl)), "ssa ctl");
   if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(SsaCtl)), "ssa ctl host");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev1), "event");
   if (!rc) rc = cuda_status(cudaMemsetAsync(w->skip, 0, (size_t)m.nP, h->stream), "memset skip");
   // Persistent grid: every CTA co-resident (cooperative launch), one CTA of 1024 threads per SM.
-  const void *kernels[3] = {(const void *)ssa_persistent<kExact64>, (const void *)ssa_persistent<kFast64>,
-                            (const void *)ssa_persistent<kMixed>};
+  const void *kernels[6] = {(const void *)ssa_persistent<kExact64, false>, (const void *)ssa_persistent<kFast64, false>,
+                            (const void *)ssa_persistent<kMixed, false>, (const void *)ssa_persistent<kExact64, true>,
+                            (const void *)ssa_persistent<kFast64, true>, (const void *)ssa_persistent<kMixed, true>};
   int gmax = 0;
-  for (int k = 0; k < 3 && !rc; ++k) {
+  for (int k = 0; k < 6 && !rc; ++k) {
+    if (k >= 3 && !m.has_halo) break;
     int per_sm = 0;
     rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], w->block, 0), "occupancy");
     if (!rc && per_sm * h->num_sms < m.n_patch) {
       set_error("ssa kernel: not enough co-resident CTAs for one per patch");
       rc = UFE_CUDA_ERROR;
     }
-    w->grid[k] = m.n_patch;   // one CTA per patch (n_patch <= kCtasPerSm * number of SMs)
-    gmax = gmax > w->grid[k] ? gmax : w->grid[k];
+    w->grid[k % 3] = m.n_patch;   // one CTA per patch (n_patch <= kCtasPerSm * number of SMs)
+    gmax = gmax > w->grid[k % 3] ? gmax : w->grid[k % 3];
   }
   if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)gmax * sizeof(double)), "rn_part");
   if (!rc) rc = cuda_status(cudaMalloc(&w->prog, 32 * (size_t)gmax * sizeof(unsigned int)), "progress counters");
@@ -1993,6 +2380,10 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->s3Nxy = m.s3Nxy; a->h_nxy32 = m.h_nxy32; a->s3Nxy32 = m.s3Nxy32; a->bnd_ptr = m.bnd_ptr; a->bnd_nbr = m.bnd_nbr;
   a->slice_e0 = m.slice_e0; a->slice_w = m.slice_w; a->slice_g = m.slice_g; a->patch_slice = m.patch_slice;
   a->patch_edge0 = m.patch_edge0; a->edge_row = m.edge_row; a->sync_ptr = m.sync_ptr; a->sync_list = m.sync_list;
+  a->hp_slice = m.hp_slice; a->hslice_e0 = m.hslice_e0; a->hslice_w = m.hslice_w; a->hrow_l = m.hrow_l;
+  a->hrow_g = m.hrow_g; a->hcol = m.hcol; a->hcuv32 = m.hcuv32; a->hcuv = m.hcuv; a->hload_ptr = m.hload_ptr;
+  a->hload_dev = m.hload_dev; a->hsync_ptr = m.hsync_ptr; a->hsync_list = m.hsync_list;
+  a->UVb = w->UVb; a->dUVb = w->dUVb;
   a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
   a->Hi = fl.Hi; a->Hb = fl.Hb; a->SL = fl.SL; a->hx = fl.hx; a->hy = fl.hy; a->Af = fl.Af;
   a->beta = fl.beta; a->tau = fl.tau;
@@ -2065,10 +2456,14 @@ int stats_of(const SsaCtl &c, ufe_ssa_stats *stats, double ms) {
   return status;
 }
 
-const void *persistent_kernel(int mode) {
-  return mode == kMixed ? (const void *)ssa_persistent<kMixed>
-         : mode == kFast64 ? (const void *)ssa_persistent<kFast64>
-                           : (const void *)ssa_persistent<kExact64>;
+const void *persistent_kernel(int mode, bool halo) {
+  if (halo)
+    return mode == kMixed ? (const void *)ssa_persistent<kMixed, true>
+           : mode == kFast64 ? (const void *)ssa_persistent<kFast64, true>
+                             : (const void *)ssa_persistent<kExact64, true>;
+  return mode == kMixed ? (const void *)ssa_persistent<kMixed, false>
+         : mode == kFast64 ? (const void *)ssa_persistent<kFast64, false>
+                           : (const void *)ssa_persistent<kExact64, false>;
 }
 
 }  // namespace
@@ -2093,10 +2488,16 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     // FP64 sweeps are bound by the FP64 pipe and gain nothing, so they keep plain loads).
     // UFE_SSA_LOCAL_ROWS=0 turns it off.
     const DevMesh &m = h->m;
-    const size_t bytes = (size_t)m.max_patch_slices * kSlice * (mode == kMixed ? sizeof(float2) : sizeof(double2));
+    const size_t elem = mode == kMixed ? sizeof(float2) : sizeof(double2);
+    // Halo sweeps when the mesh has the program and the largest working copy fits
+    // (UFE_SSA_HALO=0 turns them off); else the phased sweeps with the optional mirror.
+    const char *henv = std::getenv("UFE_SSA_HALO");
+    const bool halo = m.has_halo && (size_t)m.max_local * elem <= kLocalRowsMaxBytes && !(henv && henv[0] == '0');
+    const size_t bytes = halo ? (size_t)m.max_local * elem : (size_t)m.max_patch_slices * kSlice * elem;
     const char *env = std::getenv("UFE_SSA_LOCAL_ROWS");
-    bool local = mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0');
-    const void *fn = persistent_kernel(mode);
+    bool local = halo || (mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0'));
+    const void *fn = persistent_kernel(mode, halo);
+    w->halo_used = halo;
     if (local) {
       // Ask for a shared-memory carveout that holds the mirror (the rest stays L1), and keep
       // the plain loads if one CTA per SM would then no longer fit.
@@ -2108,7 +2509,10 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
       const int pct = smem_sm > 0 ? (int)std::min<size_t>(100, (100 * (bytes + fa.sharedSizeBytes + 2048) + smem_sm - 1) / smem_sm) : 100;
       if (!rc) rc = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct), "carveout");
       if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, w->block, bytes), "occupancy");
-      if (!rc && per_sm * h->num_sms < w->grid[mode]) local = false;
+      if (!rc && per_sm * h->num_sms < w->grid[mode]) {
+        if (halo) { set_error("ufe_ssa_run: the halo sweeps' working copy leaves no room for one CTA per SM"); rc = UFE_CUDA_ERROR; }
+        local = false;
+      }
     }
     a.local_rows = local ? 1 : 0;
     const size_t smem = local ? bytes : 0;
