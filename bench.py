@@ -297,6 +297,62 @@ def run_reference(args):
     return 0
 
 
+def adjoint_summary(dm, mesh, ssa, p, forward_ms):
+    """The metric's third quantity on the line's own workload: the VJP (ufe_ssa_vjp, GMRES on
+    transposed coloured sweeps) of the default-tolerance mixed forward solve, for
+    J = 1/2 sum over AaAc of |u - u_obs|^2 with u_obs from a forward solve whose log(beta^2) is
+    perturbed by a Gaussian random field (std 0.3, 100 km), timed with CUDA events on the
+    device and set against that forward solve's time; and its agreement with central finite
+    differences (h = 1e-4, 4 random directions) on a small marine case solved to tight
+    tolerances, where the forward's truncation error does not mask the gradient."""
+    from ufemism_gb300 import _native as nat
+    from ufemism_gb300 import api, workloads
+    from ufemism_gb300.meshgen import dome_mesh
+    lbo = np.log(1e3) + workloads.log_beta_field(mesh, std=0.3, ell=100e3, seed=20261210, mean=0.0)
+    rc, oo, so = dm.solve_ssa(dict(ssa, beta_sq_AaAc=np.exp(lbo)), p, check=False)
+    rc, out, st = dm.solve_ssa(ssa, p, check=False)     # the solve the VJP differentiates
+    dJ = {k: out[k] - oo[k] for k in ("U_SSA", "V_SSA", "Ux_SSA_Ac", "Uy_SSA_Ac")}
+    vms = []
+    for _ in range(3):
+        rcv, g, vs = dm.ssa_vjp(dJ, p, check=False)
+        vms.append(vs["device_ms"])
+    res = {"workload": "the line's workload; VJP of the mixed default-tolerance forward solve",
+           "vjp_ms": float(np.median(vms)), "vjp_status": rcv, "vjp_gmres_sweeps": vs["sweeps"],
+           "vjp_rel_residual": vs["last_rel_update"], "forward_ms": forward_ms,
+           "vjp_over_forward": float(np.median(vms)) / forward_ms}
+    # finite differences on the 1k marine case, forward solved tightly in FP64
+    base = dome_mesh("1k")
+    m1 = api.build_aaac(base)
+    Hi, Hb, SL = workloads.marine_geometry(base, seed=20261206)
+    f1, _ = workloads.prepare_inputs(m1, Hi, Hb, SL)
+    d1 = api.DeviceMesh(m1)
+    tight = api.default_params(precision=nat.UFE_FP64, SSA_RN_tol=1e-13, SSA_max_residual_UV=1e-11,
+                               SSA_max_outer_loops=300, SSA_max_inner_loops=1000000)
+    lb = workloads.log_beta_field(m1, std=1.0, ell=100e3, seed=5)
+
+    def fwd(l):
+        rc1, o1, _ = d1.solve_ssa(dict(f1, beta_sq_AaAc=np.exp(l)), tight, check=False)
+        return np.concatenate([o1["U_SSA"], o1["Ux_SSA_Ac"]]), np.concatenate([o1["V_SSA"], o1["Uy_SSA_Ac"]])
+
+    Uo, Vo = fwd(lb + workloads.log_beta_field(m1, std=0.3, ell=100e3, seed=11, mean=0.0))
+    U, V = fwd(lb)
+    nV = base.nV
+    rcv, g1, _ = d1.ssa_vjp({"U_SSA": (U - Uo)[:nV], "Ux_SSA_Ac": (U - Uo)[nV:], "V_SSA": (V - Vo)[:nV],
+                             "Uy_SSA_Ac": (V - Vo)[nV:]}, tight, check=False)
+    J = lambda a, b: 0.5 * float(np.sum((a - Uo) ** 2 + (b - Vo) ** 2))
+    rng = np.random.default_rng(20261212)
+    errs = []
+    for _ in range(4):
+        dvec = rng.normal(size=m1.nVAaAc)
+        fd = (J(*fwd(lb + 1e-4 * dvec)) - J(*fwd(lb - 1e-4 * dvec))) / 2e-4
+        an = float(g1["dJ_dlogbeta_sq_AaAc"] @ dvec)
+        errs.append(abs(fd - an) / abs(an))
+    d1.close()
+    res["fd_check"] = {"workload": "1k-vertex marine, FP64 forward to Picard 1e-13 / SOR 1e-11, dJ/dlog(beta^2)",
+                       "directions": len(errs), "h": 1e-4, "rel_err_max": max(errs)}
+    return res
+
+
 def profile_case(args):
     """One capped solve for profiler captures: a single linear solve of exactly
     ``--profile-sweeps`` SOR sweeps (SSA_max_outer_loops = 1) on the chosen workload size,
@@ -715,6 +771,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", default="200k")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="leave out the adjoint keys of the default line")
     ap.add_argument("--ref-sample-sweeps", type=int, default=40)
     ap.add_argument("--adj-rn-tol", type=float, default=1e-10, help="adjoint: forward Picard tolerance")
     ap.add_argument("--adj-tol", type=float, default=1e-12, help="adjoint: VJP relative residual tolerance")
@@ -804,6 +861,8 @@ def main():
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e_value = world * 1000.0 / float(np.mean(e2e_ms))
 
+    adjoint = adjoint_summary(dm, mesh, ssa, p32, ms32) if not args.no_adjoint else None
+
     peak, peak_kind = load_peaks()
     bytes32, sweep32 = algorithmic_bytes(counts, st32, True)
     bytes64, sweep64 = algorithmic_bytes(counts, st64, False)
@@ -840,6 +899,8 @@ def main():
         "gpu_launches": 3 * args.steps,
         "clocks": clocks,
     }
+    if adjoint:
+        line["adjoint"] = adjoint
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb, rc_o, oout, ost = cpu_baseline(args.size)
         line["cpu_baseline"] = cb

@@ -76,3 +76,35 @@ def test_200k_mixed_matches_oracle(dome200k):
     sel = (r > 200e3) & (r < 600e3)
     ur = (gout["U_SSA"][sel] * x[sel] + gout["V_SSA"][sel] * y[sel]) / r[sel]
     assert np.all(ur > 0)
+
+
+@pytest.fixture(scope="module")
+def marine16k():
+    """The marine setup (sloping bed with a Gaussian random field, floating shelf) on a 16k
+    mesh: the largest of the seeded marine meshes on which the reference's SOR converges
+    within its 10,000-sweep cap after the cold-start linear solve (from 50k vertices up,
+    every linear solve of the oracle stops at the cap)."""
+    api.init(0)
+    m = oracle_aaac("16k")
+    ssa, sia, g = oracle_inputs(m, "marine")
+    assert g["mask_shelf"].sum() > 0
+    rc, out, st = orc.solve_ssa(m, ssa, orc.default_params(n_threads=os.cpu_count() or 1))
+    assert rc in (orc.OR_OK, orc.OR_NOT_CONVERGED), rc
+    assert all(s < 10000 for s in st["sweeps"][1:]), st["sweeps"]
+    out["status"] = rc
+    dm = api.DeviceMesh(m)
+    yield m, ssa, (out, st), dm
+    dm.close()
+
+
+def test_16k_marine_fp64_and_mixed_match_oracle(marine16k):
+    m, ssa, (oout, ost), dm = marine16k
+    rc, gout, gst = dm.solve_ssa(ssa, api.default_params(precision=nat.UFE_FP64), check=False)
+    assert rc == oout["status"]
+    assert gst["sweeps"] == ost["sweeps"]
+    assert max(_errors(gout, oout).values()) <= FP64_TOL
+    rc, gout, gst = dm.solve_ssa(ssa, api.default_params(precision=nat.UFE_MIXED), check=False)
+    assert rc == oout["status"]
+    assert gst["picard_iterations"] == ost["picard_iterations"]
+    err = _errors(gout, oout)
+    assert max(err.values()) <= MIXED_TOL, err

@@ -16,10 +16,12 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# Build variants: the product library, and a profiling build whose persistent solver records
-# per-phase SM-cycle totals (ufe_debug_phase_cycles). UFE_BUILD_VARIANT selects the one that
+# Build variants: the product library; a profiling build whose persistent solver records
+# per-phase SM-cycle totals (ufe_debug_phase_cycles); builds whose mixed sweeps decide
+# convergence two sweeps late (for measuring the lag). UFE_BUILD_VARIANT selects the one that
 # ufemism_gb300._native loads.
-VARIANTS = {"": [], "phase_timers": ["-DUFE_PHASE_TIMERS=1"]}
+VARIANTS = {"": [], "phase_timers": ["-DUFE_PHASE_TIMERS=1"], "lag2": ["-DUFE_MIXED_LAG=2"],
+            "lag2_phase_timers": ["-DUFE_MIXED_LAG=2", "-DUFE_PHASE_TIMERS=1"]}
 VARIANT = os.environ.get("UFE_BUILD_VARIANT", "")
 if VARIANT not in VARIANTS:
     raise RuntimeError("UFE_BUILD_VARIANT must be one of %s" % sorted(VARIANTS))

@@ -127,6 +127,8 @@ struct DevMesh {
   int *hload_dev = nullptr;     // device row of each halo slot
   int *hsync_ptr = nullptr;     // [n_patch + 1] patches a patch waits for / is waited for by
   int *hsync_list = nullptr;
+  float *hs3_32 = nullptr;      // [n_hslices * 32] 3 sNxy of the slot's row (FP32), 0 on padding
+  double *hs3 = nullptr;        // [n_hslices * 32] the same in FP64
 };
 
 struct SsaWork;   // per-handle device buffers of the SSA solve (ufe_ssa.cu)

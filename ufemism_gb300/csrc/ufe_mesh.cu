@@ -59,7 +59,7 @@ void free_mesh(DevMesh &m) {
                   m.bnd_nbr, m.V, m.Aci12, m.iAci, m.nC, m.patch_slice, m.patch_edge0, m.edge_row,
                   m.sync_ptr, m.sync_list, m.slice_e0, m.slice_w, m.slice_g, m.hp_slice, m.hslice_e0,
                   m.hslice_w, m.hrow_l, m.hrow_g, m.hcol, m.hcuv32, m.hcuv, m.hload_ptr, m.hload_dev,
-                  m.hsync_ptr, m.hsync_list};
+                  m.hsync_ptr, m.hsync_list, m.hs3_32, m.hs3};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   m = DevMesh();
@@ -558,6 +558,14 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
     if (!rc) rc = upload(&m.hload_dev, hload_dev, S, "hload_dev");
     if (!rc) rc = upload(&m.hsync_ptr, hsync_ptr, S, "hsync_ptr");
     if (!rc) rc = upload(&m.hsync_list, hsync_list, S, "hsync_list");
+    // per-slot copies of the static cross-term coefficient (the kernels then need no
+    // dependent load through the slot's device row)
+    std::vector<float> hs3_32(hrow_g.size(), 0.0f);
+    std::vector<double> hs3(hrow_g.size(), 0.0);
+    for (size_t k = 0; k < hrow_g.size(); ++k)
+      if (hrow_l[k] >= 0) { hs3_32[k] = s3Nxy32[hrow_g[k]]; hs3[k] = s3Nxy[hrow_g[k]]; }
+    if (!rc) rc = upload(&m.hs3_32, hs3_32, S, "hs3_32");
+    if (!rc) rc = upload(&m.hs3, hs3, S, "hs3");
   }
   if (!rc) rc = cuda_status(cudaStreamSynchronize(S), "mesh upload");
   h->m = m;

@@ -107,6 +107,10 @@ struct SsaArgs {
   const float2 *hcuv32;
   const double2 *hcuv;
   const int *hload_ptr, *hload_dev, *hsync_ptr, *hsync_list;
+  const float *hs3_32;
+  const double *hs3;
+  float4 *hsd32;           // halo sweeps, mixed: per slot (1/eu, 1/ev, defect x, y) in FP32
+  double2 *hrcp, *hrhs;    // halo sweeps, fast FP64: per slot (1/eu, 1/ev) and (RHSx, RHSy)
   unsigned int *prog;      // per-CTA progress counters (stride 32 words)
   int nP;
   int nSlices;
@@ -715,9 +719,10 @@ __device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &p
       j[q] = q < w ? (int)a.hcol[e0 + (int64_t)q * kSlice] : (int)kNoCol;
       c[q] = q < w ? a.hcuv32[e0 + (int64_t)q * kSlice] : make_float2(0.f, 0.f);
     }
-    const float s3 = a.s3Nxy32[g];
-    const float2 r = a.rcp32[g];
-    const float2 d = a.r0[g];
+    const float s3 = a.hs3_32[slot];
+    const float4 sd = a.hsd32[slot];
+    const float2 r = make_float2(sd.x, sd.y);
+    const float2 d = make_float2(sd.z, sd.w);
     if (l < 0 || (a.skip && a.skip[g])) continue;   // padding slot, or a Dirichlet row
     const float2 di = ld[l];
     float su = 0.0f, sv = 0.0f;
@@ -788,9 +793,9 @@ __device__ unsigned long long halo_colour64(const SsaArgs &a, const PatchSmem &p
       int j[kBatch];
 #pragma unroll
       for (int q = 0; q < kBatch; ++q) j[q] = q < w ? (int)a.hcol[e0 + (int64_t)q * kSlice] : (int)kNoCol;
-      const double s3 = a.s3Nxy[g];
-      const double2 r = a.rcp[g];
-      const double2 b = a.rhs[g];
+      const double s3 = a.hs3[slot];
+      const double2 r = a.hrcp[slot];
+      const double2 b = a.hrhs[slot];
 #pragma unroll
       for (int q = 0; q < kBatch; ++q) {
         if (j[q] != (int)kNoCol) {
@@ -868,6 +873,26 @@ __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *l
     ld[l] = nv;
     if (l < ps.n_own) out[g] = nv;
   }
+}
+
+// Per-slot copies of the row data a sweep reads that change between linear solves (mixed:
+// the FP32 reciprocals of the centre coefficients and the defect; fast FP64: the reciprocals
+// and the right-hand side), refreshed by each CTA for its own program slots once the
+// grid-wide phase that wrote them is complete.
+template <int kMode>
+__device__ __forceinline__ void halo_refresh(const SsaArgs &a, const PatchSmem &ps) {
+  for (int k = 32 * ps.hps[0] + (int)threadIdx.x; k < 32 * ps.hps[7]; k += blockDim.x) {
+    if (a.hrow_l[k] < 0) continue;
+    const int g = a.hrow_g[k];
+    if constexpr (kMode == kMixed) {
+      const float2 r = a.rcp32[g], d = a.r0[g];
+      a.hsd32[k] = make_float4(r.x, r.y, d.x, d.y);
+    } else {
+      a.hrcp[k] = a.rcp[g];
+      a.hrhs[k] = a.rhs[g];
+    }
+  }
+  __syncthreads();
 }
 
 // Halo slots of the working copy from the buffer the neighbours wrote in the last sweep.
@@ -1180,6 +1205,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
       bool synced = true;
       int decided = 0;
       const unsigned int base = gsweep;
+      halo_refresh<kMode>(a, ps);
       UFE_TM(kTmOther);
       while (!lin_done && sweeps < a.max_inner) {
         ++sweeps;
@@ -1256,6 +1282,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
             reload();
             phase_defect(a, t);
             UFE_GRID_SYNC();
+            halo_refresh<kMode>(a, ps);
           }
           UFE_TM(kTmOther);
         } else {
@@ -1284,6 +1311,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
             reload();
             phase_defect(a, t);
             UFE_GRID_SYNC();
+            halo_refresh<kMode>(a, ps);
           }
           UFE_TM(kTmOther);
         }
@@ -2127,6 +2155,8 @@ struct SsaWork {
   float2 *dUV = nullptr, *r0 = nullptr, *rcp32 = nullptr;
   double2 *UVb = nullptr;        // halo sweeps: second velocity buffer (FP64 modes)
   float2 *dUVb = nullptr;        // halo sweeps: second correction buffer (mixed)
+  float4 *hsd32 = nullptr;       // halo sweeps: per-slot row data (mixed)
+  double2 *hrcp = nullptr, *hrhs = nullptr;   // halo sweeps: per-slot row data (fast FP64)
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   unsigned int *prog = nullptr;
@@ -2148,7 +2178,7 @@ void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
                   w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh,
-                  w->UVb, w->dUVb};
+                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -2185,17 +2215,21 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc) rc = cuda_status(cudaMalloc(&w->skip, (size_t)m.nP), "ssa skip");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->UVb, (size_t)m.nP * sizeof(double2)), "ssa UVb");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->dUVb, (size_t)m.nP * sizeof(float2)), "ssa dUVb");
+  const size_t nslots = (size_t)m.n_hslices * kSlice;
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hsd32, nslots * sizeof(float4)), "ssa hsd32");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrcp, nslots * sizeof(double2)), "ssa hrcp");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrhs, nslots * sizeof(double2)), "ssa hrhs");
   if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(SsaCtl)), "ssa ctl");
   if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(SsaCtl)), "ssa ctl host");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev1), "event");
   if (!rc) rc = cuda_status(cudaMemsetAsync(w->skip, 0, (size_t)m.nP, h->stream), "memset skip");
   // Persistent grid: every CTA co-resident (cooperative launch), one CTA of 1024 threads per SM.
-  const void *kernels[6] = {(const void *)ssa_persistent<kExact64, false>, (const void *)ssa_persistent<kFast64, false>,
-                            (const void *)ssa_persistent<kMixed, false>, (const void *)ssa_persistent<kExact64, true>,
-                            (const void *)ssa_persistent<kFast64, true>, (const void *)ssa_persistent<kMixed, true>};
+  const void *kernels[5] = {(const void *)ssa_persistent<kExact64, false>, (const void *)ssa_persistent<kFast64, false>,
+                            (const void *)ssa_persistent<kMixed, false>, (const void *)ssa_persistent<kFast64, true>,
+                            (const void *)ssa_persistent<kMixed, true>};
   int gmax = 0;
-  for (int k = 0; k < 6 && !rc; ++k) {
+  for (int k = 0; k < 5 && !rc; ++k) {
     if (k >= 3 && !m.has_halo) break;
     int per_sm = 0;
     rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], w->block, 0), "occupancy");
@@ -2203,8 +2237,8 @@ int ensure_work(ufe_mesh_h h) {
       set_error("ssa kernel: not enough co-resident CTAs for one per patch");
       rc = UFE_CUDA_ERROR;
     }
-    w->grid[k % 3] = m.n_patch;   // one CTA per patch (n_patch <= kCtasPerSm * number of SMs)
-    gmax = gmax > w->grid[k % 3] ? gmax : w->grid[k % 3];
+    if (k < 3) w->grid[k] = m.n_patch;   // one CTA per patch (n_patch <= kCtasPerSm * number of SMs)
+    gmax = gmax > m.n_patch ? gmax : m.n_patch;
   }
   if (!rc) rc = cuda_status(cudaMalloc(&w->rn_part, 2 * (size_t)gmax * sizeof(double)), "rn_part");
   if (!rc) rc = cuda_status(cudaMalloc(&w->prog, 32 * (size_t)gmax * sizeof(unsigned int)), "progress counters");
@@ -2383,7 +2417,8 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->hp_slice = m.hp_slice; a->hslice_e0 = m.hslice_e0; a->hslice_w = m.hslice_w; a->hrow_l = m.hrow_l;
   a->hrow_g = m.hrow_g; a->hcol = m.hcol; a->hcuv32 = m.hcuv32; a->hcuv = m.hcuv; a->hload_ptr = m.hload_ptr;
   a->hload_dev = m.hload_dev; a->hsync_ptr = m.hsync_ptr; a->hsync_list = m.hsync_list;
-  a->UVb = w->UVb; a->dUVb = w->dUVb;
+  a->UVb = w->UVb; a->dUVb = w->dUVb; a->hs3_32 = m.hs3_32; a->hs3 = m.hs3;
+  a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs;
   a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
   a->Hi = fl.Hi; a->Hb = fl.Hb; a->SL = fl.SL; a->hx = fl.hx; a->hy = fl.hy; a->Af = fl.Af;
   a->beta = fl.beta; a->tau = fl.tau;
@@ -2457,10 +2492,7 @@ int stats_of(const SsaCtl &c, ufe_ssa_stats *stats, double ms) {
 }
 
 const void *persistent_kernel(int mode, bool halo) {
-  if (halo)
-    return mode == kMixed ? (const void *)ssa_persistent<kMixed, true>
-           : mode == kFast64 ? (const void *)ssa_persistent<kFast64, true>
-                             : (const void *)ssa_persistent<kExact64, true>;
+  if (halo) return mode == kMixed ? (const void *)ssa_persistent<kMixed, true> : (const void *)ssa_persistent<kFast64, true>;
   return mode == kMixed ? (const void *)ssa_persistent<kMixed, false>
          : mode == kFast64 ? (const void *)ssa_persistent<kFast64, false>
                            : (const void *)ssa_persistent<kExact64, false>;
@@ -2492,7 +2524,11 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     // Halo sweeps when the mesh has the program and the largest working copy fits
     // (UFE_SSA_HALO=0 turns them off); else the phased sweeps with the optional mirror.
     const char *henv = std::getenv("UFE_SSA_HALO");
-    const bool halo = m.has_halo && (size_t)m.max_local * elem <= kLocalRowsMaxBytes && !(henv && henv[0] == '0');
+    // The parity (exact) mode keeps the phased sweeps: without fused multiply-adds it is bound
+    // by the FP64 pipe, and the halo rows' extra updates measured slower there (133 against
+    // 125 us per sweep on the 200k dome).
+    const bool halo = m.has_halo && mode != kExact64 && (size_t)m.max_local * elem <= kLocalRowsMaxBytes &&
+                      !(henv && henv[0] == '0');
     const size_t bytes = halo ? (size_t)m.max_local * elem : (size_t)m.max_patch_slices * kSlice * elem;
     const char *env = std::getenv("UFE_SSA_LOCAL_ROWS");
     bool local = halo || (mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0'));
