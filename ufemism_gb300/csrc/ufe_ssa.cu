@@ -152,6 +152,12 @@ static_assert(kMixedLag >= 0 && kMixedLag <= kMaxLag, "lag out of range");
 // Largest shared-memory mirror of a patch's rows (the rest of the 228 KB of an SM stays L1).
 constexpr size_t kLocalRowsMaxBytes = 160 * 1024;
 constexpr int kMaxKrylovRestart = 1000;   // largest GMRES restart length of the VJP
+// Threads per CTA of the halo sweeps: fewer warps with more registers each, so that a warp can
+// hold the loads of two slices at once (a colour of a 200k-vertex patch has 43-50 slices).
+#ifndef UFE_HALO_BLOCK
+#define UFE_HALO_BLOCK 768
+#endif
+constexpr int kHaloBlock = UFE_HALO_BLOCK;
 
 // Per-phase timers of the persistent solver (profiling build only, -DUFE_PHASE_TIMERS=1):
 // thread 0 of every CTA stamps clock64() at the end of each phase of the SOR loop (every
@@ -700,56 +706,82 @@ __device__ __forceinline__ int halo_global(const SsaArgs &a, const PatchSmem &ps
   return l < ps.n_own ? ps.p0 + l : a.hload_dev[ps.hl0 + l - ps.n_own];
 }
 
-// Colour phase f of the FP32 correction sweep (as phase_sweep32).
+// One slot's share of a colour phase of the FP32 correction sweep (as phase_sweep32): the
+// loads, issued for two slices before either is used so that a warp with two slices in a
+// phase waits for one round trip, not two; then the update.
+// Entries a slot loads up front (most AaAc rows have 6 neighbours; wider rows load the rest
+// after the first ones).
+constexpr int kBatchH = 6;
+
+struct Slot32 {
+  int w, l, g;
+  int64_t e0;
+  int j[kBatchH];
+  float2 c[kBatchH];
+  float s3;
+  float4 sd;
+};
+
+__device__ __forceinline__ void slot32_load(const SsaArgs &a, const PatchSmem &ps, int s, int lane, Slot32 &q) {
+  const int base = ps.hps[0];
+  q.w = ps.w[s - base];
+  q.e0 = ps.e0[s - base] + lane;
+  const int slot = s * kSlice + lane;
+  q.l = a.hrow_l[slot];
+  q.g = a.hrow_g[slot];
+#pragma unroll
+  for (int k = 0; k < kBatchH; ++k) {
+    q.j[k] = k < q.w ? (int)a.hcol[q.e0 + (int64_t)k * kSlice] : (int)kNoCol;
+    q.c[k] = k < q.w ? a.hcuv32[q.e0 + (int64_t)k * kSlice] : make_float2(0.f, 0.f);
+  }
+  q.s3 = a.hs3_32[slot];
+  q.sd = a.hsd32[slot];
+}
+
+__device__ __forceinline__ void slot32_update(const SsaArgs &a, const PatchSmem &ps, const Slot32 &q, float2 *ld,
+                                              float2 *out, float omega, float &mx) {
+  if (q.l < 0 || (a.skip && a.skip[q.g])) return;   // padding slot, or a Dirichlet row
+  const float2 di = ld[q.l];
+  float su = 0.0f, sv = 0.0f;
+#pragma unroll
+  for (int k = 0; k < kBatchH; ++k) {
+    if (q.j[k] != (int)kNoCol) {
+      const float2 u = ld[q.j[k]];
+      su = fmaf(u.x, q.c[k].x, su);
+      sv = fmaf(u.y, q.c[k].y, sv);
+    }
+  }
+  for (int k = kBatchH; k < q.w; ++k) {
+    const int jj = a.hcol[q.e0 + (int64_t)k * kSlice];
+    if (jj == (int)kNoCol) break;
+    const float2 cc = a.hcuv32[q.e0 + (int64_t)k * kSlice];
+    const float2 v = ld[jj];
+    su = fmaf(v.x, cc.x, su);
+    sv = fmaf(v.y, cc.y, sv);
+  }
+  const float ru = fmaf(fmaf(q.s3, di.y, su) - q.sd.z, q.sd.x, di.x);
+  const float rv = fmaf(fmaf(q.s3, di.x, sv) - q.sd.w, q.sd.y, di.y);
+  const float2 dn = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
+  ld[q.l] = dn;
+  if (q.l < ps.n_own) {
+    out[q.g] = dn;
+    mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
+  }
+}
+
+// Colour phase f of the FP32 correction sweep: warp w takes slices w, w + nwarps, ... in pairs.
 __device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, float2 *ld, float2 *out) {
   const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const float omega = (float)a.omega;
   float mx = 0.0f;
-  const int base = ps.hps[0];
-  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
-    const int w = ps.w[s - base];
-    const int64_t e0 = ps.e0[s - base] + lane;
-    const int slot = s * kSlice + lane;
-    const int l = a.hrow_l[slot];
-    const int g = a.hrow_g[slot];
-    int j[kBatch];
-    float2 c[kBatch];
-#pragma unroll
-    for (int q = 0; q < kBatch; ++q) {
-      j[q] = q < w ? (int)a.hcol[e0 + (int64_t)q * kSlice] : (int)kNoCol;
-      c[q] = q < w ? a.hcuv32[e0 + (int64_t)q * kSlice] : make_float2(0.f, 0.f);
-    }
-    const float s3 = a.hs3_32[slot];
-    const float4 sd = a.hsd32[slot];
-    const float2 r = make_float2(sd.x, sd.y);
-    const float2 d = make_float2(sd.z, sd.w);
-    if (l < 0 || (a.skip && a.skip[g])) continue;   // padding slot, or a Dirichlet row
-    const float2 di = ld[l];
-    float su = 0.0f, sv = 0.0f;
-#pragma unroll
-    for (int q = 0; q < kBatch; ++q) {
-      if (j[q] != (int)kNoCol) {
-        const float2 u = ld[j[q]];
-        su = fmaf(u.x, c[q].x, su);
-        sv = fmaf(u.y, c[q].y, sv);
-      }
-    }
-    for (int k = kBatch; k < w; ++k) {
-      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
-      if (jj == (int)kNoCol) break;
-      const float2 cc = a.hcuv32[e0 + (int64_t)k * kSlice];
-      const float2 v = ld[jj];
-      su = fmaf(v.x, cc.x, su);
-      sv = fmaf(v.y, cc.y, sv);
-    }
-    const float ru = fmaf(fmaf(s3, di.y, su) - d.x, r.x, di.x);
-    const float rv = fmaf(fmaf(s3, di.x, sv) - d.y, r.y, di.y);
-    const float2 dn = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
-    ld[l] = dn;
-    if (l < ps.n_own) {
-      out[g] = dn;
-      mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
-    }
+  const int s_end = ps.hps[f + 1];
+  for (int s = ps.hps[f] + wid; s < s_end; s += 2 * nwarps) {
+    Slot32 qa, qb;
+    const bool two = s + nwarps < s_end;
+    slot32_load(a, ps, s, lane, qa);
+    if (two) slot32_load(a, ps, s + nwarps, lane, qb);
+    slot32_update(a, ps, qa, ld, out, omega, mx);
+    if (two) slot32_update(a, ps, qb, ld, out, omega, mx);
   }
   return abs_bits((double)mx);
 }
@@ -1492,7 +1524,7 @@ __device__ __forceinline__ void stage_args(SsaArgs &dst, const SsaArgs *src) {
 // Single solve: the whole grid is one team; the argument block stays in the kernel's
 // parameter space (constant bank operands cost no registers).
 template <int kMode, bool kHalo>
-__global__ void __launch_bounds__(kSsaBlock, kCtasPerSm) ssa_persistent(const SsaArgs a) {
+__global__ void __launch_bounds__(kHalo ? kHaloBlock : kSsaBlock, kCtasPerSm) ssa_persistent(const SsaArgs a) {
   GridTeam t{&a.ctl->bar_count, 0u};
   solve_member<kMode, GridTeam, kHalo>(a, t);
 }
@@ -2232,7 +2264,8 @@ int ensure_work(ufe_mesh_h h) {
   for (int k = 0; k < 5 && !rc; ++k) {
     if (k >= 3 && !m.has_halo) break;
     int per_sm = 0;
-    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], w->block, 0), "occupancy");
+    rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernels[k], k >= 3 ? kHaloBlock : w->block, 0),
+                     "occupancy");
     if (!rc && per_sm * h->num_sms < m.n_patch) {
       set_error("ssa kernel: not enough co-resident CTAs for one per patch");
       rc = UFE_CUDA_ERROR;
@@ -2544,7 +2577,7 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
       if (!rc) rc = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), "smem attribute");
       const int pct = smem_sm > 0 ? (int)std::min<size_t>(100, (100 * (bytes + fa.sharedSizeBytes + 2048) + smem_sm - 1) / smem_sm) : 100;
       if (!rc) rc = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct), "carveout");
-      if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, w->block, bytes), "occupancy");
+      if (!rc) rc = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, halo ? kHaloBlock : w->block, bytes), "occupancy");
       if (!rc && per_sm * h->num_sms < w->grid[mode]) {
         if (halo) { set_error("ufe_ssa_run: the halo sweeps' working copy leaves no room for one CTA per SM"); rc = UFE_CUDA_ERROR; }
         local = false;
@@ -2554,7 +2587,8 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     const size_t smem = local ? bytes : 0;
     void *args[] = {(void *)&a};
     if (!rc)
-      rc = cuda_status(cudaLaunchCooperativeKernel(fn, dim3(w->grid[mode]), dim3(w->block), args, smem, s), "ssa_persistent");
+      rc = cuda_status(cudaLaunchCooperativeKernel(fn, dim3(w->grid[mode]), dim3(halo ? kHaloBlock : w->block), args, smem, s),
+                       "ssa_persistent");
   }
   if (!rc) rc = launch_finish(h, s);
   if (!rc) rc = cuda_status(cudaEventRecord(w->ev1, s), "event");
