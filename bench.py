@@ -365,7 +365,8 @@ def profile_case(args):
     dm = api.DeviceMesh(mesh)
     prec = {"mixed": nat.UFE_MIXED, "fp64": nat.UFE_FP64, "exact": nat.UFE_FP64}[args.profile_case]
     p = api.default_params(precision=prec, SSA_max_outer_loops=1, SSA_max_inner_loops=args.profile_sweeps,
-                           fp64_exact=1 if args.profile_case == "exact" else 0)
+                           fp64_exact=1 if args.profile_case == "exact" else 0,
+                           mixed_refold_sweeps=args.refold_sweeps)
     dm.ssa_upload(ssa, p)
     L = nat.load()
     timers = hasattr(L, "ufe_debug_phase_cycles")
@@ -765,6 +766,7 @@ def main():
     ap.add_argument("--profile-case", choices=["mixed", "fp64", "exact"], default=None,
                     help="run one capped solve (for profiler captures) instead of the benchmark")
     ap.add_argument("--profile-sweeps", type=int, default=60)
+    ap.add_argument("--refold-sweeps", type=int, default=0, help="profile case: mixed refold interval (0: default)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)

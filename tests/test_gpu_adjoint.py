@@ -207,3 +207,58 @@ def test_vjp_reports_divergence_and_recovers():
     rc2, out2, st2 = dm.ssa_vjp(dJ, p)
     assert rc2 == nat.UFE_OK
     dm.close()
+
+
+def test_vjp_at_100k_matches_cpu_adjoint_and_tangent_linear():
+    """The benchmark's adjoint size (100k-vertex marine setup, log-normal friction field): the
+    GPU VJP against the CPU reference linearised at the GPU's own state, through one sparse LU
+    of the Jacobian (about 0.8M unknowns) used both ways: the adjoint state and the gradients
+    (transposed solve, <= 1e-8), and tangent-linear directional derivatives of J on random
+    directions of log(beta^2) and of Hi against the VJP's gradients (<= 1e-8). Both sides
+    linearise at the same velocities, so the forward solve runs at the default tolerances."""
+    import scipy.sparse.linalg as spla
+    api.init(0)
+    m = oracle_aaac("100k")
+    ssa, sia, g = oracle_inputs(m, "marine")
+    lb = wl.log_beta_field(m, std=1.0, ell=100e3, seed=5)
+    dm = api.DeviceMesh(m)
+    p = api.default_params(precision=nat.UFE_MIXED)
+    f_obs = dict(ssa, beta_sq_AaAc=np.exp(lb + wl.log_beta_field(m, std=0.3, ell=100e3, seed=11, mean=0.0)))
+    rc, oo, _ = dm.solve_ssa(f_obs, p, check=False)
+    f0 = dict(ssa, beta_sq_AaAc=np.exp(lb))
+    rc, out, st = dm.solve_ssa(f0, p, check=False)
+    U, V = adj.aaac_velocity(out)
+    Uo, Vo = adj.aaac_velocity(oo)
+    gU, gV = U - Uo, V - Vo
+    dJ = dict(zip(("U_SSA", "Ux_SSA_Ac"), split(m, gU)))
+    dJ.update(zip(("V_SSA", "Uy_SSA_Ac"), split(m, gV)))
+    rcv, vo, vs = dm.ssa_vjp(dJ, p, geom_mesh=m)
+    assert rcv == nat.UFE_OK, vs
+    lin = adj.Linearisation(m, f0, U, V)
+    K = lin.jacobian().tocsc()
+    lu = spla.splu(K)
+    nA = m.nVAaAc
+    mu = lu.solve(np.concatenate([gU, gV]), trans="T")
+    mx, my = mu[:nA], mu[nA:]
+    assert rel_l2(vo["lambda_U_AaAc"], mx) <= REF_TOL
+    assert rel_l2(vo["lambda_V_AaAc"], my) <= REF_TOL
+    bx, by = lin.dF_dlogbeta()
+    assert rel_l2(vo["dJ_dlogbeta_sq_AaAc"], -(mx * bx + my * by)) <= REF_TOL
+    G = adj.geometry_matrix(m, ssa["Hi"], ssa["Hb"], ssa["SL"])
+    Gx, Gy, GH = G
+    dhx, dHx, dHy = lin.dF_dfields()
+    rng = np.random.default_rng(29)
+    for _ in range(4):
+        d = rng.normal(size=nA)
+        du = lu.solve(np.concatenate([-bx * d, -by * d]))
+        tlm = float(gU @ du[:nA] + gV @ du[nA:])
+        an = float(vo["dJ_dlogbeta_sq_AaAc"] @ d)
+        assert abs(tlm - an) <= REF_TOL * abs(an), (tlm, an)
+    for _ in range(2):
+        d = rng.normal(size=m.base.nV) * (np.asarray(ssa["Hi"]) > 50.0)
+        rhs = np.concatenate([-(dhx * (Gx @ d) + dHx * (GH @ d)), -(dhx * (Gy @ d) + dHy * (GH @ d))])
+        du = lu.solve(rhs)
+        tlm = float(gU @ du[:nA] + gV @ du[nA:])
+        an = float(vo["dJ_dHi"] @ d)
+        assert abs(tlm - an) <= REF_TOL * abs(an), (tlm, an)
+    dm.close()

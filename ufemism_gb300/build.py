@@ -18,12 +18,10 @@ SRC = os.path.join(HERE, "csrc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Build variants: the product library; a profiling build whose persistent solver records
 # per-phase SM-cycle totals (ufe_debug_phase_cycles); builds whose mixed sweeps decide
-# convergence two sweeps late, or whose halo sweeps run 1024-thread CTAs (for measurements).
-# UFE_BUILD_VARIANT selects the one that
+# convergence two sweeps late (for measuring the lag). UFE_BUILD_VARIANT selects the one that
 # ufemism_gb300._native loads.
 VARIANTS = {"": [], "phase_timers": ["-DUFE_PHASE_TIMERS=1"], "lag2": ["-DUFE_MIXED_LAG=2"],
-            "lag2_phase_timers": ["-DUFE_MIXED_LAG=2", "-DUFE_PHASE_TIMERS=1"],
-            "halo1024": ["-DUFE_HALO_BLOCK=1024"]}
+            "lag2_phase_timers": ["-DUFE_MIXED_LAG=2", "-DUFE_PHASE_TIMERS=1"]}
 VARIANT = os.environ.get("UFE_BUILD_VARIANT", "")
 if VARIANT not in VARIANTS:
     raise RuntimeError("UFE_BUILD_VARIANT must be one of %s" % sorted(VARIANTS))

@@ -110,7 +110,9 @@ struct SsaArgs {
   const float *hs3_32;
   const double *hs3;
   float4 *hsd32;           // halo sweeps, mixed: per slot (1/eu, 1/ev, defect x, y) in FP32
-  double2 *hrcp, *hrhs;    // halo sweeps, fast FP64: per slot (1/eu, 1/ev) and (RHSx, RHSy)
+  double2 *hrcp, *hrhs;    // halo sweeps, fast FP64: per slot (1/eu, 1/ev) and (RHSx, RHSy);
+                           // mixed: hrcp holds a boundary slot's own FP64 base
+  double2 *hbu0;           // halo sweeps, mixed: per boundary entry the neighbour's FP64 base
   unsigned int *prog;      // per-CTA progress counters (stride 32 words)
   int nP;
   int nSlices;
@@ -134,6 +136,7 @@ struct SsaArgs {
   int refold;
   int fp32_visc;
   int local_rows;          // keep the patch's own velocities (mixed: corrections) in shared memory
+  int l2_keep;             // halo sweeps: load the program with an L2 evict-last hint
   long long timeout_ns;
 };
 
@@ -152,10 +155,11 @@ static_assert(kMixedLag >= 0 && kMixedLag <= kMaxLag, "lag out of range");
 // Largest shared-memory mirror of a patch's rows (the rest of the 228 KB of an SM stays L1).
 constexpr size_t kLocalRowsMaxBytes = 160 * 1024;
 constexpr int kMaxKrylovRestart = 1000;   // largest GMRES restart length of the VJP
-// Threads per CTA of the halo sweeps: fewer warps with more registers each, so that a warp can
-// hold the loads of two slices at once (a colour of a 200k-vertex patch has 43-50 slices).
+// Threads per CTA of the halo sweeps. Measured on the 200k dome: 1024 threads, one slice per
+// warp at a time, 27.1 us per mixed sweep; 768 threads with two slices' loads issued together
+// per warp (80 registers), 28.6 us.
 #ifndef UFE_HALO_BLOCK
-#define UFE_HALO_BLOCK 768
+#define UFE_HALO_BLOCK 1024
 #endif
 constexpr int kHaloBlock = UFE_HALO_BLOCK;
 
@@ -706,82 +710,82 @@ __device__ __forceinline__ int halo_global(const SsaArgs &a, const PatchSmem &ps
   return l < ps.n_own ? ps.p0 + l : a.hload_dev[ps.hl0 + l - ps.n_own];
 }
 
-// One slot's share of a colour phase of the FP32 correction sweep (as phase_sweep32): the
-// loads, issued for two slices before either is used so that a warp with two slices in a
-// phase waits for one round trip, not two; then the update.
-// Entries a slot loads up front (most AaAc rows have 6 neighbours; wider rows load the rest
-// after the first ones).
-constexpr int kBatchH = 6;
-
-struct Slot32 {
-  int w, l, g;
-  int64_t e0;
-  int j[kBatchH];
-  float2 c[kBatchH];
-  float s3;
-  float4 sd;
-};
-
-__device__ __forceinline__ void slot32_load(const SsaArgs &a, const PatchSmem &ps, int s, int lane, Slot32 &q) {
-  const int base = ps.hps[0];
-  q.w = ps.w[s - base];
-  q.e0 = ps.e0[s - base] + lane;
-  const int slot = s * kSlice + lane;
-  q.l = a.hrow_l[slot];
-  q.g = a.hrow_g[slot];
-#pragma unroll
-  for (int k = 0; k < kBatchH; ++k) {
-    q.j[k] = k < q.w ? (int)a.hcol[q.e0 + (int64_t)k * kSlice] : (int)kNoCol;
-    q.c[k] = k < q.w ? a.hcuv32[q.e0 + (int64_t)k * kSlice] : make_float2(0.f, 0.f);
-  }
-  q.s3 = a.hs3_32[slot];
-  q.sd = a.hsd32[slot];
+// Loads of the halo program with an L2 eviction-priority hint: the program is re-read every
+// sweep, and with the hint it outlives the FP64 arrays the grid-wide phases stream through
+// L2 between sweeps (defect, fold, viscosity). Only for arrays no kernel writes.
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ int ld_keep_u16(const uint16_t *q, uint64_t pol) {
+  unsigned short v;
+  asm volatile("ld.global.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(q), "l"(pol));
+  return (int)v;
+}
+__device__ __forceinline__ float2 ld_keep_f2(const float2 *q, uint64_t pol) {
+  float2 v;
+  asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(q), "l"(pol));
+  return v;
 }
 
-__device__ __forceinline__ void slot32_update(const SsaArgs &a, const PatchSmem &ps, const Slot32 &q, float2 *ld,
-                                              float2 *out, float omega, float &mx) {
-  if (q.l < 0 || (a.skip && a.skip[q.g])) return;   // padding slot, or a Dirichlet row
-  const float2 di = ld[q.l];
-  float su = 0.0f, sv = 0.0f;
-#pragma unroll
-  for (int k = 0; k < kBatchH; ++k) {
-    if (q.j[k] != (int)kNoCol) {
-      const float2 u = ld[q.j[k]];
-      su = fmaf(u.x, q.c[k].x, su);
-      sv = fmaf(u.y, q.c[k].y, sv);
-    }
-  }
-  for (int k = kBatchH; k < q.w; ++k) {
-    const int jj = a.hcol[q.e0 + (int64_t)k * kSlice];
-    if (jj == (int)kNoCol) break;
-    const float2 cc = a.hcuv32[q.e0 + (int64_t)k * kSlice];
-    const float2 v = ld[jj];
-    su = fmaf(v.x, cc.x, su);
-    sv = fmaf(v.y, cc.y, sv);
-  }
-  const float ru = fmaf(fmaf(q.s3, di.y, su) - q.sd.z, q.sd.x, di.x);
-  const float rv = fmaf(fmaf(q.s3, di.x, sv) - q.sd.w, q.sd.y, di.y);
-  const float2 dn = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
-  ld[q.l] = dn;
-  if (q.l < ps.n_own) {
-    out[q.g] = dn;
-    mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
-  }
-}
-
-// Colour phase f of the FP32 correction sweep: warp w takes slices w, w + nwarps, ... in pairs.
+// Colour phase f of the FP32 correction sweep (as phase_sweep32).
+template <bool kKeep>
 __device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, float2 *ld, float2 *out) {
+  const uint64_t pol = kKeep ? l2_keep_policy() : 0ull;
   const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const float omega = (float)a.omega;
   float mx = 0.0f;
-  const int s_end = ps.hps[f + 1];
-  for (int s = ps.hps[f] + wid; s < s_end; s += 2 * nwarps) {
-    Slot32 qa, qb;
-    const bool two = s + nwarps < s_end;
-    slot32_load(a, ps, s, lane, qa);
-    if (two) slot32_load(a, ps, s + nwarps, lane, qb);
-    slot32_update(a, ps, qa, ld, out, omega, mx);
-    if (two) slot32_update(a, ps, qb, ld, out, omega, mx);
+  const int base = ps.hps[0];
+  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
+    const int w = ps.w[s - base];
+    const int64_t e0 = ps.e0[s - base] + lane;
+    const int slot = s * kSlice + lane;
+    const int l = a.hrow_l[slot];
+    const int g = a.hrow_g[slot];
+    int j[kBatch];
+    float2 c[kBatch];
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q) {
+      if (kKeep) {
+        j[q] = q < w ? ld_keep_u16(a.hcol + e0 + (int64_t)q * kSlice, pol) : (int)kNoCol;
+        c[q] = q < w ? ld_keep_f2(a.hcuv32 + e0 + (int64_t)q * kSlice, pol) : make_float2(0.f, 0.f);
+      } else {
+        j[q] = q < w ? (int)a.hcol[e0 + (int64_t)q * kSlice] : (int)kNoCol;
+        c[q] = q < w ? a.hcuv32[e0 + (int64_t)q * kSlice] : make_float2(0.f, 0.f);
+      }
+    }
+    const float s3 = a.hs3_32[slot];
+    const float4 sd = a.hsd32[slot];
+    const float2 r = make_float2(sd.x, sd.y);
+    const float2 d = make_float2(sd.z, sd.w);
+    if (l < 0 || (a.skip && a.skip[g])) continue;   // padding slot, or a Dirichlet row
+    const float2 di = ld[l];
+    float su = 0.0f, sv = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kBatch; ++q) {
+      if (j[q] != (int)kNoCol) {
+        const float2 u = ld[j[q]];
+        su = fmaf(u.x, c[q].x, su);
+        sv = fmaf(u.y, c[q].y, sv);
+      }
+    }
+    for (int k = kBatch; k < w; ++k) {
+      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+      if (jj == (int)kNoCol) break;
+      const float2 cc = a.hcuv32[e0 + (int64_t)k * kSlice];
+      const float2 v = ld[jj];
+      su = fmaf(v.x, cc.x, su);
+      sv = fmaf(v.y, cc.y, sv);
+    }
+    const float ru = fmaf(fmaf(s3, di.y, su) - d.x, r.x, di.x);
+    const float rv = fmaf(fmaf(s3, di.x, sv) - d.y, r.y, di.y);
+    const float2 dn = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
+    ld[l] = dn;
+    if (l < ps.n_own) {
+      out[g] = dn;
+      mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
+    }
   }
   return abs_bits((double)mx);
 }
@@ -882,7 +886,7 @@ __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *l
       if (jj == (int)kNoCol) break;
       double2 u;
       if constexpr (kM) {
-        u = a.UV[halo_global(a, ps, jj)];
+        u = a.hbu0[e0 + (int64_t)k * kSlice];   // the neighbour's FP64 base, copied at the last refresh
         const float2 dj = reinterpret_cast<const float2 *>(ld)[jj];
         u.x = u.x + (double)dj.x;
         u.y = u.y + (double)dj.y;
@@ -897,7 +901,7 @@ __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *l
     const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
     T nv;
     if constexpr (kM) {
-      const double2 u0 = a.UV[g];
+      const double2 u0 = a.hrcp[slot];            // the row's own FP64 base (mixed: hrcp holds it)
       nv = make_float2((float)(v.x - u0.x), (float)(v.y - u0.y));
     } else {
       nv = v;
@@ -919,6 +923,20 @@ __device__ __forceinline__ void halo_refresh(const SsaArgs &a, const PatchSmem &
     if constexpr (kMode == kMixed) {
       const float2 r = a.rcp32[g], d = a.r0[g];
       a.hsd32[k] = make_float4(r.x, r.y, d.x, d.y);
+      if (k >= 32 * ps.hps[5]) {
+        // boundary slots: the FP64 bases (u0) of the row and of the neighbours it averages,
+        // so that the boundary phase reads them with its entries instead of through two
+        // dependent loads
+        a.hrcp[k] = a.UV[g];
+        const int s = k / kSlice, lane = k % kSlice;
+        const int w = ps.w[s - ps.hps[0]];
+        const int64_t e0 = ps.e0[s - ps.hps[0]] + lane;
+        for (int q = 0; q < w; ++q) {
+          const int jj = a.hcol[e0 + (int64_t)q * kSlice];
+          if (jj == (int)kNoCol) break;
+          a.hbu0[e0 + (int64_t)q * kSlice] = a.UV[halo_global(a, ps, jj)];
+        }
+      }
     } else {
       a.hrcp[k] = a.rcp[g];
       a.hrhs[k] = a.rhs[g];
@@ -1254,7 +1272,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         for (int f = 0; f < 5; ++f) {
           if (ps.hps[f + 1] == ps.hps[f]) continue;
           unsigned long long m;
-          if constexpr (kM) m = halo_colour32(a, ps, f, hld, out);
+          if constexpr (kM) m = a.l2_keep ? halo_colour32<true>(a, ps, f, hld, out) : halo_colour32<false>(a, ps, f, hld, out);
           else m = halo_colour64<kMode == kExact64>(a, ps, f, hld, out);
           mx = m > mx ? m : mx;
           __syncthreads();
@@ -2189,6 +2207,7 @@ struct SsaWork {
   float2 *dUVb = nullptr;        // halo sweeps: second correction buffer (mixed)
   float4 *hsd32 = nullptr;       // halo sweeps: per-slot row data (mixed)
   double2 *hrcp = nullptr, *hrhs = nullptr;   // halo sweeps: per-slot row data (fast FP64)
+  double2 *hbu0 = nullptr;       // halo sweeps: per boundary entry FP64 base (mixed)
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   unsigned int *prog = nullptr;
@@ -2210,7 +2229,7 @@ void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
                   w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh,
-                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs};
+                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs, w->hbu0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -2251,6 +2270,7 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hsd32, nslots * sizeof(float4)), "ssa hsd32");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrcp, nslots * sizeof(double2)), "ssa hrcp");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrhs, nslots * sizeof(double2)), "ssa hrhs");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hbu0, (size_t)m.n_hE * sizeof(double2)), "ssa hbu0");
   if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(SsaCtl)), "ssa ctl");
   if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(SsaCtl)), "ssa ctl host");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
@@ -2451,7 +2471,7 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->hrow_g = m.hrow_g; a->hcol = m.hcol; a->hcuv32 = m.hcuv32; a->hcuv = m.hcuv; a->hload_ptr = m.hload_ptr;
   a->hload_dev = m.hload_dev; a->hsync_ptr = m.hsync_ptr; a->hsync_list = m.hsync_list;
   a->UVb = w->UVb; a->dUVb = w->dUVb; a->hs3_32 = m.hs3_32; a->hs3 = m.hs3;
-  a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs;
+  a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs; a->hbu0 = w->hbu0;
   a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
   a->Hi = fl.Hi; a->Hb = fl.Hb; a->SL = fl.SL; a->hx = fl.hx; a->hy = fl.hy; a->Af = fl.Af;
   a->beta = fl.beta; a->tau = fl.tau;
@@ -2567,6 +2587,8 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     bool local = halo || (mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0'));
     const void *fn = persistent_kernel(mode, halo);
     w->halo_used = halo;
+    const char *kenv = std::getenv("UFE_SSA_L2KEEP");
+    a.l2_keep = halo && kenv && kenv[0] == '1';
     if (local) {
       // Ask for a shared-memory carveout that holds the mirror (the rest stays L1), and keep
       // the plain loads if one CTA per SM would then no longer fit.
