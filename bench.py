@@ -74,7 +74,7 @@ def mesh_counts(mesh):
     return dict(nV=nV, nA=nA, nnz_all=nnz_all, nnz_act=nnz_act, n_act=n_act, n_edge=n_edge, nb_bnd=nb_bnd)
 
 
-def algorithmic_bytes(c, st, mixed: bool, refold: int = 32):
+def algorithmic_bytes(c, st, mixed: bool, refold: int = 64):
     """Compulsory DRAM bytes of one persistent-kernel launch (each array touched once per
     phase; neighbour gathers of U,V counted once through the row's own U,V)."""
     if not mixed:
@@ -372,9 +372,10 @@ def profile_case(args):
     timers = hasattr(L, "ufe_debug_phase_cycles")
     if timers:
         import ctypes as ct
-        buf = (ct.c_ulonglong * 16)()
+        NT = 9
+        buf = (ct.c_ulonglong * (NT + 1024 * NT))()
         L.ufe_debug_phase_cycles.restype = ct.c_int
-        L.ufe_debug_phase_cycles(buf, 16, 1)
+        L.ufe_debug_phase_cycles(buf, NT + 1024 * NT, 1)
     times, st = timed_runs(dm, p, args.steps, args.warmup, dm.stream)
     ms = float(np.mean(times))
     line = {"profile_case": args.profile_case, "size": args.size, "sweeps": st["total_sweeps"],
@@ -382,7 +383,7 @@ def profile_case(args):
     if timers:
         # totals over CTAs and over the warm-up and timed runs; shares of the per-CTA time, and
         # the same shares of the measured time per sweep
-        n = L.ufe_debug_phase_cycles(buf, 16, 1)
+        n = L.ufe_debug_phase_cycles(buf, NT + 1024 * NT, 1)
         names = ["wait_colour", "colour", "arrive", "wait_boundary", "boundary", "decide", "grid_barrier", "other"]
         cyc = np.array([buf[i] for i in range(len(names))], dtype=np.float64)
         sweeps_cta = float(buf[len(names)])
@@ -392,6 +393,18 @@ def profile_case(args):
             "share": {k: float(v) for k, v in zip(names, share)},
             "us_per_sweep": {k: float(v) * line["us_per_sweep"] for k, v in zip(names, share)},
             "cycles_per_cta_sweep": {k: float(v) / max(sweeps_cta, 1.0) for k, v in zip(names, cyc)}}
+        # per CTA: the time it spends working (not waiting for other CTAs) per sweep
+        per = np.array([buf[NT + i] for i in range(1024 * NT)], dtype=np.float64).reshape(1024, NT)
+        per = per[per[:, NT - 1] > 0]
+        waits = per[:, 0] + per[:, 3] + per[:, 5] + per[:, 6]
+        busy = (per[:, :NT - 1].sum(axis=1) - waits) / per[:, NT - 1]
+        us = line["us_per_sweep"] / (per[:, :NT - 1].sum(axis=1) / per[:, NT - 1]).mean()
+        line["phase_timers"]["busy_us_per_sweep_per_cta"] = {
+            "min": float(busy.min() * us), "mean": float(busy.mean() * us), "max": float(busy.max() * us),
+            "slowest_ctas": [int(i) for i in np.argsort(-busy)[:8]],
+            "colour_us_by_cta_max": float((per[:, 1] / per[:, NT - 1]).max() * us),
+            "boundary_us_by_cta_max": float((per[:, 4] / per[:, NT - 1]).max() * us),
+            "all_busy_us": [round(float(b * us), 2) for b in busy]}
     print(json.dumps(line))
     dm.close()
     return 0
@@ -870,13 +883,16 @@ def main():
     bytes64, sweep64 = algorithmic_bytes(counts, st64, False)
     ach32 = bytes32 / (ms32 * 1e-3) / 1e9
     ach64 = bytes64 / (ms64 * 1e-3) / 1e9
-    traffic = None
+    # DRAM traffic per launch and L2 throughput of the kernel from an ncu capture of a capped
+    # solve of this workload (profiles/), scaled to this launch's sweeps
+    traffic = tprof = None
     prof = os.path.join(ROOT, "profiles", "ssa_persistent_traffic.json")
     if os.path.exists(prof):
         try:
-            traffic = json.load(open(prof)).get("dram_bytes_per_launch_scaled")
+            tprof = json.load(open(prof))
+            traffic = tprof["dram_bytes_per_sweep"] * st32["total_sweeps"]
         except Exception:
-            traffic = None
+            traffic = tprof = None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
@@ -895,6 +911,11 @@ def main():
         "vertex_sweeps_per_s": counts["nA"] * st32["total_sweeps"] / (ms32 * 1e-3),
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
                      "traffic": traffic, "peak_kind": peak_kind, "kernel": "ssa_persistent<mixed>",
+                     "dram_frac": None if traffic is None else traffic / (ms32 * 1e-3) / 1e9 / peak,
+                     "l2_throughput_pct_ncu": None if tprof is None else tprof.get("lts_throughput_pct"),
+                     "note": "achieved/frac: algorithmic bytes (each array once per sweep) over the launch time; "
+                             "dram_frac: measured DRAM bytes over the same time; the mixed sweep's working set "
+                             "lives in L2, so it is bound by L2 latency and synchronisation, not by HBM",
                      "algorithmic_bytes_per_launch": bytes32, "bytes_per_sweep": sweep32},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         # k_gather + ssa_persistent + k_scatter per mixed solve in the timed region
