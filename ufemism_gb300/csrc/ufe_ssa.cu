@@ -883,15 +883,21 @@ __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *l
     const int l = a.hrow_l[slot];
     if (l < 0) continue;
     const int g = a.hrow_g[slot];
+    // every load of the slot up front (an edge row averages at most a few neighbours), so the
+    // phase costs one round trip, not one per neighbour
+    constexpr int kB = 4;
+    int jb[kB];
+    double2 ub[kB];
+#pragma unroll
+    for (int k = 0; k < kB; ++k) {
+      jb[k] = k < w ? (int)a.hcol[e0 + (int64_t)k * kSlice] : (int)kNoCol;
+      if constexpr (kM) ub[k] = k < w ? a.hbu0[e0 + (int64_t)k * kSlice] : make_double2(0.0, 0.0);
+    }
     double sx = 0.0, sy = 0.0;
     int nvals = 0;
-    for (int k = 0; k < w; ++k) {
-      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
-      if (jj == (int)kNoCol) break;
-      double2 u;
+    auto add = [&](int jj, double2 u) {
       if constexpr (kM) {
-        u = a.hbu0[e0 + (int64_t)k * kSlice];   // the neighbour's FP64 base, copied at the last refresh
-        const float2 dj = reinterpret_cast<const float2 *>(ld)[jj];
+        const float2 dj = reinterpret_cast<const float2 *>(ld)[jj];   // u: the neighbour's FP64 base
         u.x = u.x + (double)dj.x;
         u.y = u.y + (double)dj.y;
       } else {
@@ -900,6 +906,15 @@ __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *l
       sx = sx + u.x;
       sy = sy + u.y;
       ++nvals;
+    };
+    // the entries are packed from the first (padding only after the last), in the reference's order
+#pragma unroll
+    for (int k = 0; k < kB; ++k)
+      if (jb[k] != (int)kNoCol) add(jb[k], kM ? ub[k] : make_double2(0.0, 0.0));
+    for (int k = kB; k < w; ++k) {
+      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+      if (jj == (int)kNoCol) break;
+      add(jj, kM ? a.hbu0[e0 + (int64_t)k * kSlice] : make_double2(0.0, 0.0));
     }
     if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
     const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
