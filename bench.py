@@ -404,7 +404,9 @@ def profile_case(args):
             "slowest_ctas": [int(i) for i in np.argsort(-busy)[:8]],
             "colour_us_by_cta_max": float((per[:, 1] / per[:, NT - 1]).max() * us),
             "boundary_us_by_cta_max": float((per[:, 4] / per[:, NT - 1]).max() * us),
-            "all_busy_us": [round(float(b * us), 2) for b in busy]}
+            "all_busy_us": [round(float(b * us), 2) for b in busy],
+            "per_cta_us": {k: [round(float(v * us), 2) for v in per[:, i] / per[:, NT - 1]]
+                           for i, k in enumerate(names)}}
     print(json.dumps(line))
     dm.close()
     return 0
