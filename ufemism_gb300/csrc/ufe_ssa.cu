@@ -109,10 +109,9 @@ struct SsaArgs {
   const int *hload_ptr, *hload_dev, *hsync_ptr, *hsync_list;
   const float *hs3_32;
   const double *hs3;
-  float4 *hsd32;           // halo sweeps, mixed: per slot (1/eu, 1/ev, defect x, y) in FP32
-  double2 *hrcp, *hrhs;    // halo sweeps, fast FP64: per slot (1/eu, 1/ev) and (RHSx, RHSy);
-                           // mixed: hrcp holds a boundary slot's own FP64 base
-  double2 *hbu0;           // halo sweeps, mixed: per boundary entry the neighbour's FP64 base
+  float4 *hsd32;           // halo sweeps, mixed: per slot (1/eu, 1/ev, defect x, y) in FP32;
+                           // boundary slots: (c0 x, c0 y, 1 / count, 0), see halo_boundary
+  double2 *hrcp, *hrhs;    // halo sweeps, fast FP64: per slot (1/eu, 1/ev) and (RHSx, RHSy)
   unsigned int *prog;      // per-CTA progress counters (stride 32 words)
   int nP;
   int nSlices;
@@ -871,59 +870,68 @@ __device__ unsigned long long halo_colour64(const SsaArgs &a, const PatchSmem &p
 
 // Boundary phase f (5: edge rows, 6: corners) of apply_Neumann_boundary_AaAc: the mean of the
 // listed neighbours (edge rows: the non-edge ones; corners: all, the edge rows among them
-// already updated in phase 5), as phase_boundary.
+// already updated in phase 5), as phase_boundary. Every load of a slot is issued before any is
+// used (an edge row averages at most a few neighbours), so a phase costs one round trip.
+// Mixed: with u0 fixed between refolds, mean(u0_j + d_j) - u0_i = c0_i + mean(d_j), where
+// c0_i = mean(u0_j) - u0_i is formed in FP64 at the refresh; the sweep then adds the FP32
+// corrections only.
 template <bool kM, class T>
 __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *ld, T *out) {
   const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const int base = ps.hps[0];
+  constexpr int kB = 4;
   for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
     const int w = ps.w[s - base];
     const int64_t e0 = ps.e0[s - base] + lane;
     const int slot = s * kSlice + lane;
     const int l = a.hrow_l[slot];
-    if (l < 0) continue;
     const int g = a.hrow_g[slot];
-    // every load of the slot up front (an edge row averages at most a few neighbours), so the
-    // phase costs one round trip, not one per neighbour
-    constexpr int kB = 4;
     int jb[kB];
-    double2 ub[kB];
 #pragma unroll
-    for (int k = 0; k < kB; ++k) {
-      jb[k] = k < w ? (int)a.hcol[e0 + (int64_t)k * kSlice] : (int)kNoCol;
-      if constexpr (kM) ub[k] = k < w ? a.hbu0[e0 + (int64_t)k * kSlice] : make_double2(0.0, 0.0);
-    }
-    double sx = 0.0, sy = 0.0;
-    int nvals = 0;
-    auto add = [&](int jj, double2 u) {
-      if constexpr (kM) {
-        const float2 dj = reinterpret_cast<const float2 *>(ld)[jj];   // u: the neighbour's FP64 base
-        u.x = u.x + (double)dj.x;
-        u.y = u.y + (double)dj.y;
-      } else {
-        u = reinterpret_cast<const double2 *>(ld)[jj];
-      }
-      sx = sx + u.x;
-      sy = sy + u.y;
-      ++nvals;
-    };
-    // the entries are packed from the first (padding only after the last), in the reference's order
-#pragma unroll
-    for (int k = 0; k < kB; ++k)
-      if (jb[k] != (int)kNoCol) add(jb[k], kM ? ub[k] : make_double2(0.0, 0.0));
-    for (int k = kB; k < w; ++k) {
-      const int jj = a.hcol[e0 + (int64_t)k * kSlice];
-      if (jj == (int)kNoCol) break;
-      add(jj, kM ? a.hbu0[e0 + (int64_t)k * kSlice] : make_double2(0.0, 0.0));
-    }
-    if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
-    const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
+    for (int k = 0; k < kB; ++k) jb[k] = k < w ? (int)a.hcol[e0 + (int64_t)k * kSlice] : (int)kNoCol;
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (kM) c = a.hsd32[slot];
+    if (l < 0) continue;
     T nv;
     if constexpr (kM) {
-      const double2 u0 = a.hrcp[slot];            // the row's own FP64 base (mixed: hrcp holds it)
-      nv = make_float2((float)(v.x - u0.x), (float)(v.y - u0.y));
+      float sx = 0.0f, sy = 0.0f;
+#pragma unroll
+      for (int k = 0; k < kB; ++k)
+        if (jb[k] != (int)kNoCol) {
+          const float2 dj = ld[jb[k]];
+          sx = sx + dj.x;
+          sy = sy + dj.y;
+        }
+      for (int k = kB; k < w; ++k) {
+        const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+        if (jj == (int)kNoCol) break;
+        const float2 dj = ld[jj];
+        sx = sx + dj.x;
+        sy = sy + dj.y;
+      }
+      nv = make_float2(fmaf(sx, c.z, c.x), fmaf(sy, c.z, c.y));
     } else {
-      nv = v;
+      // the packed entries in the reference's order (padding only after the last)
+      double sx = 0.0, sy = 0.0;
+      int nvals = 0;
+#pragma unroll
+      for (int k = 0; k < kB; ++k)
+        if (jb[k] != (int)kNoCol) {
+          const double2 u = ld[jb[k]];
+          sx = sx + u.x;
+          sy = sy + u.y;
+          ++nvals;
+        }
+      for (int k = kB; k < w; ++k) {
+        const int jj = a.hcol[e0 + (int64_t)k * kSlice];
+        if (jj == (int)kNoCol) break;
+        const double2 u = ld[jj];
+        sx = sx + u.x;
+        sy = sy + u.y;
+        ++nvals;
+      }
+      if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
+      nv = make_double2(sx / (double)nvals, sy / (double)nvals);
     }
     ld[l] = nv;
     if (l < ps.n_own) out[g] = nv;
@@ -943,18 +951,24 @@ __device__ __forceinline__ void halo_refresh(const SsaArgs &a, const PatchSmem &
       const float2 r = a.rcp32[g], d = a.r0[g];
       a.hsd32[k] = make_float4(r.x, r.y, d.x, d.y);
       if (k >= 32 * ps.hps[5]) {
-        // boundary slots: the FP64 bases (u0) of the row and of the neighbours it averages,
-        // so that the boundary phase reads them with its entries instead of through two
-        // dependent loads
-        a.hrcp[k] = a.UV[g];
+        // boundary slots: c0 = mean of the averaged neighbours' u0 minus the row's u0 (FP64),
+        // and 1 / (number averaged), for halo_boundary
         const int s = k / kSlice, lane = k % kSlice;
         const int w = ps.w[s - ps.hps[0]];
         const int64_t e0 = ps.e0[s - ps.hps[0]] + lane;
+        double sx = 0.0, sy = 0.0;
+        int n = 0;
         for (int q = 0; q < w; ++q) {
           const int jj = a.hcol[e0 + (int64_t)q * kSlice];
           if (jj == (int)kNoCol) break;
-          a.hbu0[e0 + (int64_t)q * kSlice] = a.UV[halo_global(a, ps, jj)];
+          const double2 u = a.UV[halo_global(a, ps, jj)];
+          sx = sx + u.x;
+          sy = sy + u.y;
+          ++n;
         }
+        const double2 u0 = a.UV[g];
+        const double rn = n > 0 ? 1.0 / (double)n : 0.0;
+        a.hsd32[k] = make_float4((float)(sx * rn - u0.x), (float)(sy * rn - u0.y), (float)rn, 0.0f);
       }
     } else {
       a.hrcp[k] = a.rcp[g];
@@ -2226,7 +2240,6 @@ struct SsaWork {
   float2 *dUVb = nullptr;        // halo sweeps: second correction buffer (mixed)
   float4 *hsd32 = nullptr;       // halo sweeps: per-slot row data (mixed)
   double2 *hrcp = nullptr, *hrhs = nullptr;   // halo sweeps: per-slot row data (fast FP64)
-  double2 *hbu0 = nullptr;       // halo sweeps: per boundary entry FP64 base (mixed)
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   unsigned int *prog = nullptr;
@@ -2248,7 +2261,7 @@ void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
                   w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh,
-                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs, w->hbu0};
+                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -2289,7 +2302,6 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hsd32, nslots * sizeof(float4)), "ssa hsd32");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrcp, nslots * sizeof(double2)), "ssa hrcp");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrhs, nslots * sizeof(double2)), "ssa hrhs");
-  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hbu0, (size_t)m.n_hE * sizeof(double2)), "ssa hbu0");
   if (!rc) rc = cuda_status(cudaMalloc(&w->ctl, sizeof(SsaCtl)), "ssa ctl");
   if (!rc) rc = cuda_status(cudaMallocHost(&w->ctl_host, sizeof(SsaCtl)), "ssa ctl host");
   if (!rc) rc = cuda_status(cudaEventCreate(&w->ev0), "event");
@@ -2490,7 +2502,7 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->hrow_g = m.hrow_g; a->hcol = m.hcol; a->hcuv32 = m.hcuv32; a->hcuv = m.hcuv; a->hload_ptr = m.hload_ptr;
   a->hload_dev = m.hload_dev; a->hsync_ptr = m.hsync_ptr; a->hsync_list = m.hsync_list;
   a->UVb = w->UVb; a->dUVb = w->dUVb; a->hs3_32 = m.hs3_32; a->hs3 = m.hs3;
-  a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs; a->hbu0 = w->hbu0;
+  a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs;
   a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
   a->Hi = fl.Hi; a->Hb = fl.Hb; a->SL = fl.SL; a->hx = fl.hx; a->hy = fl.hy; a->Af = fl.Af;
   a->beta = fl.beta; a->tau = fl.tau;
