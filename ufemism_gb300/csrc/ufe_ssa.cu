@@ -135,8 +135,6 @@ struct SsaArgs {
   int refold;
   int fp32_visc;
   int local_rows;          // keep the patch's own velocities (mixed: corrections) in shared memory
-  int stage_off;           // halo sweeps, mixed: byte offset of the warps' staging areas in dynamic
-                           // shared memory (after the working copy), 0 = no staging
   long long timeout_ns;
 };
 
@@ -714,10 +712,8 @@ __device__ __forceinline__ int halo_global(const SsaArgs &a, const PatchSmem &ps
   return l < ps.n_own ? ps.p0 + l : a.hload_dev[ps.hl0 + l - ps.n_own];
 }
 
-// One slice of a colour phase of the FP32 correction sweep (as phase_sweep32), its slot
-// records and entries read through pointers that are already offset by the lane: either the
-// program in global memory or a copy of it staged in shared memory (same layout: entry k of
-// the lane at [32 k]).
+// One slice of a colour phase of the FP32 correction sweep (as phase_sweep32), its entries
+// read through pointers already offset by the lane (entry k of the lane at [32 k]).
 __device__ __forceinline__ void slice32(const SsaArgs &a, const PatchSmem &ps, int w, const uint16_t *pc,
                                         const float2 *pcu, int l, int g, float s3, float4 sd, float2 *ld, float2 *out,
                                         float omega, float &mx) {
@@ -757,92 +753,23 @@ __device__ __forceinline__ void slice32(const SsaArgs &a, const PatchSmem &ps, i
   }
 }
 
-// Shared-memory copy of one program slice (mixed halo sweeps): columns (w x 32 u16),
-// coefficients (w x 32 float2), local rows, device rows, 3 sNxy (32 each, 4 bytes), row data
-// (32 float4). Every region starts on a 16-byte boundary in both memories.
-constexpr int kStageMaxW = 10;
-constexpr int kStageBytes = kStageMaxW * kSlice * 2 + kStageMaxW * kSlice * 8 + kSlice * (4 + 4 + 4 + 16);
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
-}
-
-// The warp copies slice s (w entries per slot) into its staging area with asynchronous
-// 16-byte copies, committed as one group.
-__device__ __forceinline__ void stage_slice32(const SsaArgs &a, const PatchSmem &ps, int s, int w, unsigned char *st,
-                                              int lane) {
-  const int64_t e0 = ps.e0[s - ps.hps[0]];
-  const int b_col = w * kSlice * 2, b_cuv = w * kSlice * 8;
-  const int total = (b_col + b_cuv + kSlice * 28) / 16;
-  const char *col = reinterpret_cast<const char *>(a.hcol + e0);
-  const char *cuv = reinterpret_cast<const char *>(a.hcuv32 + e0);
-  const int64_t sl = (int64_t)s * kSlice;
-  for (int q = lane; q < total; q += 32) {
-    const int off = q * 16;
-    const char *src;
-    if (off < b_col) {
-      src = col + off;
-    } else if (off < b_col + b_cuv) {
-      src = cuv + (off - b_col);
-    } else {
-      const int o = off - b_col - b_cuv;
-      if (o < 128) src = reinterpret_cast<const char *>(a.hrow_l + sl) + o;
-      else if (o < 256) src = reinterpret_cast<const char *>(a.hrow_g + sl) + (o - 128);
-      else if (o < 384) src = reinterpret_cast<const char *>(a.hs3_32 + sl) + (o - 256);
-      else src = reinterpret_cast<const char *>(a.hsd32 + sl) + (o - 384);
-    }
-    cp_async16(st + off, src);
-  }
-  asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-// Colour phase f of the FP32 correction sweep. Warp w takes slices w, w + nwarps, ...: a
-// colour of a 200k-vertex patch has 43-50 slices for 32 warps, so about half the warps take
-// two. The second slice is staged into shared memory by asynchronous copies issued before
-// the first is processed, so that its loads wait on shared memory rather than on a second
-// L2 round trip.
-__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, float2 *ld, float2 *out,
-                                            unsigned char *stage) {
+// Colour phase f of the FP32 correction sweep: warp w takes slices w, w + nwarps, ... (a
+// colour of a 200k-vertex patch has 43-50 slices for 32 warps). Staging a warp's second slice
+// in shared memory by asynchronous copies issued before its first measured slower (20.5
+// against 19.5 us per sweep), as did loading two slices at once at 768 threads (28.6 against
+// 27.1 us before the boundary-phase change).
+__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, float2 *ld, float2 *out) {
   const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const float omega = (float)a.omega;
   float mx = 0.0f;
   const int base = ps.hps[0];
-  const int s_end = ps.hps[f + 1];
-  const int s0 = ps.hps[f] + wid, s1 = s0 + nwarps;
-  unsigned char *st = stage + (size_t)wid * kStageBytes;
-  bool staged = false;
-  if (stage && s1 < s_end) {
-    const int w1 = ps.w[s1 - base];
-    if (w1 <= kStageMaxW) {
-      stage_slice32(a, ps, s1, w1, st, lane);
-      staged = true;
-    }
-  }
-  auto from_global = [&](int s) {
+  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
     const int w = ps.w[s - base];
     const int64_t e0 = ps.e0[s - base] + lane;
     const int slot = s * kSlice + lane;
     slice32(a, ps, w, a.hcol + e0, a.hcuv32 + e0, a.hrow_l[slot], a.hrow_g[slot], a.hs3_32[slot], a.hsd32[slot], ld,
             out, omega, mx);
-  };
-  if (s0 < s_end) from_global(s0);
-  if (s1 < s_end) {
-    if (staged) {
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
-      __syncwarp();
-      const int w = ps.w[s1 - base];
-      const uint16_t *pc = reinterpret_cast<const uint16_t *>(st) + lane;
-      const float2 *pcu = reinterpret_cast<const float2 *>(st + w * kSlice * 2) + lane;
-      const unsigned char *rec = st + w * kSlice * 10;
-      slice32(a, ps, w, pc, pcu, reinterpret_cast<const int *>(rec)[lane], reinterpret_cast<const int *>(rec + 128)[lane],
-              reinterpret_cast<const float *>(rec + 256)[lane], reinterpret_cast<const float4 *>(rec + 384)[lane], ld,
-              out, omega, mx);
-    } else {
-      from_global(s1);
-    }
   }
-  for (int s = s1 + nwarps; s < s_end; s += nwarps) from_global(s);
   return abs_bits((double)mx);
 }
 
@@ -1358,7 +1285,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         for (int f = 0; f < 5; ++f) {
           if (ps.hps[f + 1] == ps.hps[f]) continue;
           unsigned long long m;
-          if constexpr (kM) m = halo_colour32(a, ps, f, hld, out, a.stage_off ? ufe_local_rows + a.stage_off : nullptr);
+          if constexpr (kM) m = halo_colour32(a, ps, f, hld, out);
           else m = halo_colour64<kMode == kExact64>(a, ps, f, hld, out);
           mx = m > mx ? m : mx;
           __syncthreads();
@@ -2671,13 +2598,6 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     bool local = halo || (mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0'));
     const void *fn = persistent_kernel(mode, halo);
     w->halo_used = halo;
-    // mixed halo sweeps: one staging area per warp after the working copy (UFE_SSA_STAGE=0: none)
-    const char *senv = std::getenv("UFE_SSA_STAGE");
-    const size_t stage_off = (bytes + 15) / 16 * 16;
-    const bool stage = halo && mode == kMixed && !(senv && senv[0] == '0') &&
-                       stage_off + (size_t)(kHaloBlock / 32) * kStageBytes <= 200 * 1024;
-    a.stage_off = stage ? (int)stage_off : 0;
-    if (stage) bytes = stage_off + (size_t)(kHaloBlock / 32) * kStageBytes;
     if (local) {
       // Ask for a shared-memory carveout that holds the mirror (the rest stays L1), and keep
       // the plain loads if one CTA per SM would then no longer fit.
