@@ -78,6 +78,24 @@ def test_200k_mixed_matches_oracle(dome200k):
     assert np.all(ur > 0)
 
 
+@pytest.mark.parametrize("precision", [nat.UFE_FP64, nat.UFE_MIXED])
+def test_200k_phased_sweeps_match_oracle(dome200k, monkeypatch, precision):
+    """The phased sweeps (one grid-wide phase per colour; the path of the batched members),
+    selected for a single solve with UFE_SSA_HALO=0, against the same oracle result."""
+    m, ssa, (oout, ost), dm = dome200k
+    monkeypatch.setenv("UFE_SSA_HALO", "0")
+    rc, gout, gst = dm.solve_ssa(ssa, api.default_params(precision=precision, fp64_exact=0), check=False)
+    assert rc == oout["status"]
+    assert gst["picard_iterations"] == ost["picard_iterations"]
+    err = _errors(gout, oout)
+    if precision == nat.UFE_FP64:
+        assert gst["sweeps"] == ost["sweeps"]
+        assert max(err.values()) <= FP64_TOL, err
+    else:
+        assert gst["sweeps"][0] == ost["sweeps"][0]
+        assert max(err.values()) <= MIXED_TOL, err
+
+
 @pytest.fixture(scope="module")
 def marine16k():
     """The marine setup (sloping bed with a Gaussian random field, floating shelf) on a 16k

@@ -112,7 +112,9 @@ struct SsaArgs {
   float4 *hsd32;           // halo sweeps, mixed: per slot (1/eu, 1/ev, defect x, y) in FP32;
                            // boundary slots: (c0 x, c0 y, 1 / count, 0), see halo_boundary
   double2 *hrcp, *hrhs;    // halo sweeps, fast FP64: per slot (1/eu, 1/ev) and (RHSx, RHSy)
+  float4 *bc0;             // mixed, per edge ordinal: (c0 x, c0 y, 1 / count, 0), see phase_boundary
   unsigned int *prog;      // per-CTA progress counters (stride 32 words)
+  int n_edge;              // edge ordinals (edge rows and corners)
   int nP;
   int nSlices;
   int ncm;
@@ -642,18 +644,16 @@ __device__ unsigned long long phase_sweep32(const SsaArgs &a, const PatchSmem &p
 // neighbour's new value is recomputed in place (same arithmetic, same result) so that the
 // corners need no second pass. SUM(vals) in the reference runs over nC_mem slots whose
 // unused entries are +0, hence the trailing "+ 0.0".
-template <bool kM>
+//
+// Mixed path: with u = u0 + d on every row, the mean of the neighbours' u minus the row's u0
+// is c0 + mean(d_j), c0 = mean(u0_j) - u0 (formed in FP64 by phase_defect whenever u0
+// changes, stored per edge ordinal in bc0 as (c0 x, c0 y, 1 / count)), so a sweep's boundary
+// phase is an FP32 sum of corrections and no FP64 division.
 __device__ __forceinline__ double2 edge_mean(const SsaArgs &a, int k) {
   const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
   double sx = 0.0, sy = 0.0;
   for (int q = b0; q < b1; ++q) {
-    const int j = a.bnd_nbr[q];
-    double2 u = a.UV[j];
-    if (kM) {
-      const float2 d = a.dUV[j];
-      u.x = u.x + (double)d.x;
-      u.y = u.y + (double)d.y;
-    }
+    const double2 u = a.UV[a.bnd_nbr[q]];
     sx = sx + u.x;
     sy = sy + u.y;
   }
@@ -662,39 +662,49 @@ __device__ __forceinline__ double2 edge_mean(const SsaArgs &a, int k) {
   return make_double2(sx / (double)nvals, sy / (double)nvals);
 }
 
+__device__ __forceinline__ float2 edge_correction(const SsaArgs &a, int k) {
+  const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
+  const float4 c = a.bc0[k];
+  float sx = 0.0f, sy = 0.0f;
+  for (int q = b0; q < b1; ++q) {
+    const float2 d = a.dUV[a.bnd_nbr[q]];
+    sx = sx + d.x;
+    sy = sy + d.y;
+  }
+  return make_float2(fmaf(sx, c.z, c.x), fmaf(sy, c.z, c.y));
+}
+
 template <bool kM>
 __device__ void phase_boundary(const SsaArgs &a, const PatchSmem &ps, const LocalRows &lc) {
   for (int k = ps.edge0 + threadIdx.x; k < ps.edge1; k += blockDim.x) {
     const int p = a.edge_row[k];
     const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
-    double sx = 0.0, sy = 0.0;
-    for (int q = b0; q < b1; ++q) {
-      const int j = a.bnd_nbr[q];
-      double2 u;
-      if (j < 0) {
-        u = edge_mean<kM>(a, -j - 1);   // a corner's edge neighbour, recomputed
-      } else {
-        u = a.UV[j];
-        if (kM) {
-          const float2 d = a.dUV[j];
-          u.x = u.x + (double)d.x;
-          u.y = u.y + (double)d.y;
-        }
+    if constexpr (kM) {
+      const float4 c = a.bc0[k];
+      float sx = 0.0f, sy = 0.0f;
+      for (int q = b0; q < b1; ++q) {
+        const int j = a.bnd_nbr[q];
+        // a corner's edge neighbour: its new correction, recomputed
+        const float2 d = j < 0 ? edge_correction(a, -j - 1) : a.dUV[j];
+        sx = sx + d.x;
+        sy = sy + d.y;
       }
-      sx = sx + u.x;
-      sy = sy + u.y;
-    }
-    const int nvals = b1 - b0;
-    if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
-    const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
-    if (!kM) {
-      a.UV[p] = v;
-      if (lc.n) static_cast<double2 *>(lc.base)[p - lc.p0] = v;
-    } else {
-      const double2 u0 = a.UV[p];
-      const float2 dv = make_float2((float)(v.x - u0.x), (float)(v.y - u0.y));
+      const float2 dv = make_float2(fmaf(sx, c.z, c.x), fmaf(sy, c.z, c.y));
       a.dUV[p] = dv;
       if (lc.n) static_cast<float2 *>(lc.base)[p - lc.p0] = dv;
+    } else {
+      double sx = 0.0, sy = 0.0;
+      for (int q = b0; q < b1; ++q) {
+        const int j = a.bnd_nbr[q];
+        const double2 u = j < 0 ? edge_mean(a, -j - 1) : a.UV[j];   // a corner's edge neighbour, recomputed
+        sx = sx + u.x;
+        sy = sy + u.y;
+      }
+      const int nvals = b1 - b0;
+      if (nvals < a.ncm) { sx = sx + 0.0; sy = sy + 0.0; }
+      const double2 v = make_double2(sx / (double)nvals, sy / (double)nvals);
+      a.UV[p] = v;
+      if (lc.n) static_cast<double2 *>(lc.base)[p - lc.p0] = v;
     }
   }
 }
@@ -1016,6 +1026,24 @@ __device__ void phase_defect(const SsaArgs &a, const Team &t) {
     const double lhsx = fma(ec.x, ui.x, fma(s3, ui.y, su));
     const double lhsy = fma(ec.y, ui.y, fma(s3, ui.x, sv));
     a.r0[p] = make_float2((float)(b.x - lhsx), (float)(b.y - lhsy));
+  }
+  // the boundary offsets of the new u0 (phase_boundary): c0 = mean of the averaged
+  // neighbours' u0 minus the row's u0, in FP64; a corner's edge neighbour by its row
+  const int tid = t.rank() * blockDim.x + threadIdx.x;
+  const int nt = t.size() * blockDim.x;
+  for (int k = tid; k < a.n_edge; k += nt) {
+    const int b0 = a.bnd_ptr[k], b1 = a.bnd_ptr[k + 1];
+    double sx = 0.0, sy = 0.0;
+    for (int q = b0; q < b1; ++q) {
+      const int j = a.bnd_nbr[q];
+      const double2 u = a.UV[j < 0 ? a.edge_row[-j - 1] : j];
+      sx = sx + u.x;
+      sy = sy + u.y;
+    }
+    const double2 u0 = a.UV[a.edge_row[k]];
+    const int n = b1 - b0;
+    const double rn = n > 0 ? 1.0 / (double)n : 0.0;
+    a.bc0[k] = make_float4((float)(sx * rn - u0.x), (float)(sy * rn - u0.y), (float)rn, 0.0f);
   }
 }
 
@@ -2220,6 +2248,7 @@ struct SsaWork {
   float2 *dUVb = nullptr;        // halo sweeps: second correction buffer (mixed)
   float4 *hsd32 = nullptr;       // halo sweeps: per-slot row data (mixed)
   double2 *hrcp = nullptr, *hrhs = nullptr;   // halo sweeps: per-slot row data (fast FP64)
+  float4 *bc0 = nullptr;         // mixed: boundary offsets per edge ordinal
   uint8_t *skip = nullptr;
   double *rn_part = nullptr;
   unsigned int *prog = nullptr;
@@ -2241,7 +2270,7 @@ void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
                   w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh,
-                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs};
+                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs, w->bc0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -2276,6 +2305,7 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc) rc = cuda_status(cudaMalloc(&w->rcp, (size_t)m.nP * sizeof(double2)), "ssa rcp");
   if (!rc) rc = cuda_status(cudaMalloc(&w->rcp32, (size_t)m.nP * sizeof(float2)), "ssa rcp32");
   if (!rc) rc = cuda_status(cudaMalloc(&w->skip, (size_t)m.nP), "ssa skip");
+  if (!rc) rc = cuda_status(cudaMalloc(&w->bc0, ((size_t)m.n_edge_total + 1) * sizeof(float4)), "ssa bc0");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->UVb, (size_t)m.nP * sizeof(double2)), "ssa UVb");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->dUVb, (size_t)m.nP * sizeof(float2)), "ssa dUVb");
   const size_t nslots = (size_t)m.n_hslices * kSlice;
@@ -2483,6 +2513,7 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->hload_dev = m.hload_dev; a->hsync_ptr = m.hsync_ptr; a->hsync_list = m.hsync_list;
   a->UVb = w->UVb; a->dUVb = w->dUVb; a->hs3_32 = m.hs3_32; a->hs3 = m.hs3;
   a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs;
+  a->bc0 = w->bc0; a->n_edge = m.n_edge_total;
   a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
   a->Hi = fl.Hi; a->Hb = fl.Hb; a->SL = fl.SL; a->hx = fl.hx; a->hy = fl.hy; a->Af = fl.Af;
   a->beta = fl.beta; a->tau = fl.tau;
