@@ -65,6 +65,66 @@ void free_mesh(DevMesh &m) {
   m = DevMesh();
 }
 
+// Slots of one phase of the halo sweep program: the phase's rows (device rows) dealt into
+// slices of 32 lanes, densely (padding, -1, only after the last row). A slice's k-th gather
+// reads, in each lane, the working-copy element (8 bytes in the mixed sweeps) of the lane's
+// k-th neighbour; local index l lies in bank pair l mod 16, and the gather costs one
+// shared-memory wavefront per element in its busiest bank pair (2 at best for 32 lanes, about 4.3
+// in degree-sorted order on a 200k-vertex mesh). Rows are taken by degree, descending (stable):
+// each slice starts with the first row not yet placed, so its width and the number of slices are
+// those of plain degree order, and every next lane takes, among the next kWindow rows not yet
+// placed, the one that raises the slice's per-entry maximum bank load least (the earliest on a
+// tie). cols_of(p, cols) writes the local columns of p's entries and returns their number.
+template <class ColsOf>
+void bank_aware_slices(std::vector<int> &rows, ColsOf cols_of) {
+  constexpr int kWindow = 64;
+  const size_t n = rows.size();
+  std::vector<int> nc(n), cols(n * kMaxDeg);
+  for (size_t i = 0; i < n; ++i) nc[i] = cols_of(rows[i], &cols[i * kMaxDeg]);
+  std::vector<int> idx(n);
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return nc[x] > nc[y]; });
+  std::vector<char> used(n, 0);
+  std::vector<int> out;
+  out.reserve(n + kSlice);
+  size_t first = 0;
+  for (;;) {
+    while (first < n && used[idx[first]]) ++first;
+    if (first == n) break;
+    int cnt[kMaxDeg][16], mx[kMaxDeg];
+    std::memset(cnt, 0, sizeof cnt);
+    std::memset(mx, 0, sizeof mx);
+    auto take = [&](int i) {
+      used[i] = 1;
+      out.push_back(rows[i]);
+      for (int k = 0; k < nc[i]; ++k) {
+        int &c = cnt[k][cols[(size_t)i * kMaxDeg + k] & 15];
+        if (++c > mx[k]) mx[k] = c;
+      }
+    };
+    take(idx[first]);
+    for (int lane = 1; lane < kSlice; ++lane) {
+      int best = -1, best_cost = kMaxDeg + 1, seen = 0;
+      for (size_t q = first + 1; q < n && seen < kWindow; ++q) {
+        const int i = idx[q];
+        if (used[i]) continue;
+        ++seen;
+        int c = 0;
+        for (int k = 0; k < nc[i]; ++k) c += cnt[k][cols[(size_t)i * kMaxDeg + k] & 15] >= mx[k];
+        if (c < best_cost) {
+          best_cost = c;
+          best = i;
+          if (c == 0) break;
+        }
+      }
+      if (best < 0) break;
+      take(best);
+    }
+    while (out.size() % kSlice) out.push_back(-1);
+  }
+  rows.swap(out);
+}
+
 }  // namespace
 
 }  // namespace ufe
@@ -393,27 +453,22 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
       for (int p : halo) hreads[b].push_back(patch_of[orig_of_dev[p]]);
       hload_dev.insert(hload_dev.end(), halo.begin(), halo.end());
       hload_ptr.push_back((int)hload_dev.size());
-      // program: per phase, the own rows in device order (keeping the device slices of the
-      // colour groups, so per-row loads stay coalesced), then the halo rows by degree
+      // program: per phase, the phase's own and halo rows packed densely into slices of 32
+      // (bank_aware_slices: by degree, lanes chosen to spread the working-copy gathers over
+      // the shared-memory banks)
       const int first_slice = (int)hslice_e0.size();
       for (int f = 0; f < 7; ++f) {
         hp_slice.push_back((int)hslice_e0.size());
         std::vector<int> rows;   // device rows, -1 = padding slot
-        if (f < 5) {
-          const int g0 = patch_slice[(size_t)b * (kGroups + 1) + f] * kSlice;
-          const int g1 = patch_slice[(size_t)b * (kGroups + 1) + f + 1] * kSlice;
-          for (int p = g0; p < g1; ++p) rows.push_back(ph[p] == f ? p : -1);
-        } else {
-          for (int p = p0; p < p1; ++p)
-            if (ph[p] == f) rows.push_back(p);
-          while (rows.size() % kSlice) rows.push_back(-1);
-        }
-        std::vector<int> hrows;
+        for (int p = p0; p < p1; ++p)
+          if (ph[p] == f) rows.push_back(p);
         for (int p : R)
-          if ((p < p0 || p >= p1) && ph[p] == f) hrows.push_back(p);
-        std::stable_sort(hrows.begin(), hrows.end(), [&](int x, int y) { return d->nCAaAc[orig_of_dev[x]] > d->nCAaAc[orig_of_dev[y]]; });
-        rows.insert(rows.end(), hrows.begin(), hrows.end());
-        while (rows.size() % kSlice) rows.push_back(-1);
+          if ((p < p0 || p >= p1) && ph[p] == f) rows.push_back(p);
+        bank_aware_slices(rows, [&](int p, int *cols) {
+          reads_of(p, rd);
+          for (size_t k = 0; k < rd.size(); ++k) cols[k] = local_of(rd[k]);
+          return (int)rd.size();
+        });
         for (size_t s0 = 0; s0 < rows.size(); s0 += kSlice) {
           int w = 0;
           for (int l = 0; l < kSlice; ++l) {

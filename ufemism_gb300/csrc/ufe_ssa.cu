@@ -1122,6 +1122,32 @@ __device__ __forceinline__ void lag_arrive(SsaCtl *ctl, unsigned int G, unsigned
   }
 }
 
+// lag_arrive, then publish_progress(value), under one release: thread 0 folds the CTA's maximum
+// into the slot, and a single fence orders it, and every write of the CTA before the barrier,
+// before both the slot's count and the progress counter (a fence followed by relaxed writes is
+// a release of each of them).
+template <class Team>
+__device__ __forceinline__ void lag_arrive_publish(const SsaArgs &a, const Team &t, unsigned int G,
+                                                   unsigned long long mx_bits, unsigned int value) {
+  __shared__ unsigned long long s_w[32];
+  unsigned long long v = warp_max_u64(mx_bits);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) s_w[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    unsigned long long x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0ull;
+    x = warp_max_u64(x);
+    if (l == 0) {
+      const float r = __double2float_ru(__longlong_as_double((long long)x));
+      const unsigned long long key = ((unsigned long long)(G + 1u) << 32) | (unsigned long long)__float_as_uint(r);
+      atomicMax(&a.ctl->lag_res[G % kLagRing], key);
+      asm volatile("fence.acq_rel.gpu;" ::: "memory");
+      asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(&a.ctl->lag_cnt[G % kLagRing]), "r"(1u) : "memory");
+      asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(a.prog + 32 * t.rank()), "r"(value) : "memory");
+    }
+  }
+}
+
 // Sweep G's maximum |res| for the whole block. Bounded wait; false when it ran out, when the
 // team's error bit is set, or when the slot already holds a later sweep (cannot happen with
 // lag <= kMaxLag).
@@ -1327,9 +1353,8 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         UFE_TM(kTmBoundary);
         par ^= 1;
         if constexpr (kLag) {
-          lag_arrive(ctl, G, mx);
           ++phases;
-          publish_progress(a, t, phases);
+          lag_arrive_publish(a, t, G, mx, phases);
           UFE_TM(kTmArrive);
           synced = false;
           const bool refold_now = a.refold > 0 && sweeps % a.refold == 0;
