@@ -27,9 +27,9 @@
 // of the FP64 iteration; FP32 rounding is relative to |d|, not |u|. Every `refold` sweeps
 // d is folded into u0 and the defect recomputed in FP64. The viscosity uses FP32 arithmetic
 // on FP64 differences u_j - u_i. Convergence norms (RN, max residual) are FP64. The mixed
-// sweeps have no team barrier between sweeps: a sweep's maximum residual is read one sweep
-// later from a ring of per-sweep slots (lag_arrive / lag_residual), so a converged linear
-// solve ends one sweep after the sweep that met the tolerance.
+// sweeps have no team barrier between sweeps: a sweep is decided one sweep later from a ring
+// of per-sweep slots (lag_arrive / lag_decide), so a converged linear solve ends one sweep
+// after the sweep that met the tolerance.
 #include <cooperative_groups.h>
 
 #include <algorithm>
@@ -63,7 +63,7 @@ struct SsaCtl {
   double last_max_residual;
   int sweeps[64];
   // lagged convergence decisions of the mixed sweeps (ring of kLagRing sweeps)
-  unsigned int lag_cnt[8];          // CTAs counted in per slot, monotonic within a launch
+  unsigned long long lag_word[8];   // arrivals per slot, monotonic within a solve (lag_increment)
   unsigned long long lag_res[8];    // (sweep + 1) << 32 | FP32 bits of the sweep's max |res|, rounded up
 };
 
@@ -137,6 +137,7 @@ struct SsaArgs {
   int refold;
   int fp32_visc;
   int local_rows;          // keep the patch's own velocities (mixed: corrections) in shared memory
+  int halo_index_off;      // halo sweeps: byte offset of the halo slots' device rows in dynamic shared memory
   long long timeout_ns;
 };
 
@@ -229,6 +230,12 @@ __device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int *p) {
 
 __device__ __forceinline__ void red_release_add_u32(unsigned int *p, unsigned int v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
 }
 
 // A team: the CTAs of a cooperative launch that solve one problem together. GridTeam is the
@@ -477,6 +484,9 @@ struct PatchSmem {
   // device rows [p0, p0 + n_own) and the halo slots [n_own, n_own + nh) of the working copy
   int hps[8];
   int p0, n_own, nh, hl0;
+  // lagged decisions: each slot's arrival word as this CTA last read it (lag_decide)
+  unsigned long long lag_prev[8];
+  int lag_act[2];
 };
 
 // One colour of the FP64 sweep in the reference's expression order (parity mode).
@@ -969,9 +979,11 @@ __device__ __forceinline__ void halo_refresh(const SsaArgs &a, const PatchSmem &
 }
 
 // Halo slots of the working copy from the buffer the neighbours wrote in the last sweep.
+// The patch's halo slots' device rows are kept in shared memory after the working copy
+// (halo_index), which saves one dependent L2 load per sweep.
 template <class T>
-__device__ __forceinline__ void halo_load(const SsaArgs &a, const PatchSmem &ps, T *ld, const T *in) {
-  for (int i = threadIdx.x; i < ps.nh; i += blockDim.x) ld[ps.n_own + i] = in[a.hload_dev[ps.hl0 + i]];
+__device__ __forceinline__ void halo_load(const PatchSmem &ps, const int *hidx, T *ld, const T *in) {
+  for (int i = threadIdx.x; i < ps.nh; i += blockDim.x) ld[ps.n_own + i] = in[hidx[i]];
 }
 
 // Own rows of the working copy into a global buffer.
@@ -1100,103 +1112,144 @@ __device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &
 }
 
 // Lagged decisions (mixed sweeps). After its colour phases each CTA folds its maximum |res|
-// into the ring slot of sweep G (one atomicMax of a key that carries the sweep, so a slot needs
-// no reset) and counts itself in with a release; a CTA reads sweep G's maximum once the slot's
-// count says every CTA of the team is in. The residual travels as FP32 rounded up, so a
-// decision can only come later, never earlier, than the FP64 value would give.
-__device__ __forceinline__ void lag_arrive(SsaCtl *ctl, unsigned int G, unsigned long long mx_bits) {
+// into the ring slot of sweep G (one atomicMax of a key that carries the sweep, kept for the
+// report of the final residual) and, behind a release, adds its arrival to the slot's word:
+// 1 (the count, bits 0-15), plus 1 << 16 unless its residual is below the tolerance, 1 << 32 if
+// it is above 1e6 (divergence), 1 << 48 if it is NaN. The residual travels as FP32 rounded up,
+// so a decision can only come later, never earlier, than the FP64 value would give. A reader
+// takes the difference between the word and the value it read at the slot's previous use: once
+// the count there is the team's size, the three counts decide the sweep as the maximum would
+// (converged when none is at or above the tolerance; diverged when some are above 1e6; neither
+// when some are NaN) with a single load. Every CTA reads every sweep of a solve in order (the
+// sweeps left undecided at the end of a linear solve are drained), so that difference holds
+// exactly the sweep's arrivals; a count above the team's size means that the slot was refilled
+// before it was read (cannot happen with lag <= kMaxLag).
+__device__ __forceinline__ unsigned long long lag_increment(unsigned long long mx_bits, double tol, unsigned int G,
+                                                            unsigned long long *key) {
+  const float r = __double2float_ru(__longlong_as_double((long long)mx_bits));
+  *key = ((unsigned long long)(G + 1u) << 32) | (unsigned long long)__float_as_uint(r);
+  const double rd = (double)r;
+  unsigned long long inc = 1ull;
+  if (!(rd < tol)) inc += 1ull << 16;
+  if (rd > 1e6) inc += 1ull << 32;
+  if (rd != rd) inc += 1ull << 48;
+  return inc;
+}
+
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v) {
   __shared__ unsigned long long s_w[32];
-  unsigned long long v = warp_max_u64(mx_bits);
+  v = warp_max_u64(v);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (l == 0) s_w[w] = v;
   __syncthreads();
+  unsigned long long x = 0ull;
   if (w == 0) {
-    unsigned long long x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0ull;
+    x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0ull;
     x = warp_max_u64(x);
-    if (l == 0) {
-      const float r = __double2float_ru(__longlong_as_double((long long)x));
-      const unsigned long long key = ((unsigned long long)(G + 1u) << 32) | (unsigned long long)__float_as_uint(r);
-      atomicMax(&ctl->lag_res[G % kLagRing], key);
-      red_release_add_u32(&ctl->lag_cnt[G % kLagRing], 1u);   // orders the atomicMax before the count
-    }
+  }
+  return x;   // valid in thread 0
+}
+
+__device__ __forceinline__ void lag_arrive(const SsaArgs &a, unsigned int G, unsigned long long mx_bits) {
+  const unsigned long long x = block_max_u64(mx_bits);
+  if (threadIdx.x == 0) {
+    unsigned long long key;
+    const unsigned long long inc = lag_increment(x, a.tol, G, &key);
+    atomicMax(&a.ctl->lag_res[G % kLagRing], key);
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(&a.ctl->lag_word[G % kLagRing]), "l"(inc) : "memory");
   }
 }
 
-// lag_arrive, then publish_progress(value), under one release: thread 0 folds the CTA's maximum
-// into the slot, and a single fence orders it, and every write of the CTA before the barrier,
-// before both the slot's count and the progress counter (a fence followed by relaxed writes is
-// a release of each of them).
+// lag_arrive, then publish_progress(value), under one release: a single fence orders the
+// slot's maximum, and every write of the CTA before the barrier, before both the arrival and
+// the progress counter (a fence followed by relaxed writes is a release of each of them).
 template <class Team>
 __device__ __forceinline__ void lag_arrive_publish(const SsaArgs &a, const Team &t, unsigned int G,
                                                    unsigned long long mx_bits, unsigned int value) {
-  __shared__ unsigned long long s_w[32];
-  unsigned long long v = warp_max_u64(mx_bits);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) s_w[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    unsigned long long x = l < (int)(blockDim.x >> 5) ? s_w[l] : 0ull;
-    x = warp_max_u64(x);
-    if (l == 0) {
-      const float r = __double2float_ru(__longlong_as_double((long long)x));
-      const unsigned long long key = ((unsigned long long)(G + 1u) << 32) | (unsigned long long)__float_as_uint(r);
-      atomicMax(&a.ctl->lag_res[G % kLagRing], key);
-      asm volatile("fence.acq_rel.gpu;" ::: "memory");
-      asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(&a.ctl->lag_cnt[G % kLagRing]), "r"(1u) : "memory");
-      asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(a.prog + 32 * t.rank()), "r"(value) : "memory");
-    }
+  const unsigned long long x = block_max_u64(mx_bits);
+  if (threadIdx.x == 0) {
+    unsigned long long key;
+    const unsigned long long inc = lag_increment(x, a.tol, G, &key);
+    atomicMax(&a.ctl->lag_res[G % kLagRing], key);
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+    asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(&a.ctl->lag_word[G % kLagRing]), "l"(inc) : "memory");
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(a.prog + 32 * t.rank()), "r"(value) : "memory");
   }
 }
 
-// Sweep G's maximum |res| for the whole block. Bounded wait; false when it ran out, when the
-// team's error bit is set, or when the slot already holds a later sweep (cannot happen with
-// lag <= kMaxLag).
+// The decision on sweep G for the whole block: 1 converged, 2 diverged, 0 neither, -1 when a
+// bounded wait ran out, the team's error bit is set, or the slot was refilled early.
 template <class Team>
-__device__ __forceinline__ bool lag_residual(const SsaArgs &a, const Team &t, unsigned int G, double &res) {
-  __shared__ double s_res;
-  __shared__ int s_ok;
+__device__ __forceinline__ int lag_decide(const SsaArgs &a, const Team &t, PatchSmem &ps, unsigned int G) {
   if (threadIdx.x == 0) {
     const unsigned int slot = G % kLagRing;
-    const unsigned int target = (unsigned)t.size() * (G / kLagRing + 1u);
-    const unsigned int *cnt = &a.ctl->lag_cnt[slot];
-    unsigned int v = ld_acquire_u32(cnt);
-    int ok = 1;
-    if ((int)(v - target) < 0) {
+    const unsigned long long *wp = &a.ctl->lag_word[slot];
+    const unsigned long long n = (unsigned long long)t.size();
+    const unsigned long long prev = ps.lag_prev[slot];
+    unsigned long long d = ld_acquire_u64(wp) - prev;
+    int act = 0;
+    if ((d & 0xffffull) < n) {
       const unsigned long long t0 = globaltimer_ns();
       unsigned int ns = 16;
       for (;;) {
         __nanosleep(ns);
         if (ns < 64) ns <<= 1;
-        v = ld_acquire_u32(cnt);
-        if ((int)(v - target) >= 0) break;
-        if (*(volatile unsigned int *)t.bar() & kBarrierError) { ok = 0; break; }
+        d = ld_acquire_u64(wp) - prev;
+        if ((d & 0xffffull) >= n) break;
+        if (*(volatile unsigned int *)t.bar() & kBarrierError) { act = -1; break; }
         if ((long long)(globaltimer_ns() - t0) > a.timeout_ns) {
           atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
           atomicOr(t.bar(), kBarrierError);
-          ok = 0;
+          act = -1;
           break;
         }
       }
     }
-    if (ok) {
-      const unsigned long long key = *(volatile unsigned long long *)&a.ctl->lag_res[slot];
-      if ((unsigned int)(key >> 32) != G + 1u) {
-        atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
-        atomicOr(t.bar(), kBarrierError);
-        ok = 0;
-      }
-      s_res = (double)__uint_as_float((unsigned int)key);
+    if (act == 0 && (d & 0xffffull) != n) {
+      atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
+      atomicOr(t.bar(), kBarrierError);
+      act = -1;
     }
-    s_ok = ok;
+    if (act == 0) {
+      ps.lag_prev[slot] = prev + d;
+      const unsigned int nc = (unsigned int)(d >> 16) & 0xffffu, nd = (unsigned int)(d >> 32) & 0xffffu;
+      const unsigned int nn = (unsigned int)(d >> 48);
+      act = nn ? 0 : nc == 0 ? 1 : nd ? 2 : 0;
+    }
+    ps.lag_act[G & 1] = act;   // two cells: a fast thread 0 may write the next sweep's before all read this one
   }
   __syncthreads();
-  res = s_res;
-  return s_ok != 0;
+  return ps.lag_act[G & 1];
+}
+
+// The final maximum |res| of sweep G (the report), read by thread 0 after lag_decide took G.
+__device__ __forceinline__ double lag_residual_of(const SsaArgs &a, unsigned int G) {
+  const unsigned long long key = *(volatile unsigned long long *)&a.ctl->lag_res[G % kLagRing];
+  return (unsigned int)(key >> 32) == G + 1u ? (double)__uint_as_float((unsigned int)key) : -1.0;
+}
+
+// End of a linear solve with lagged decisions: the sweeps after the deciding one (`decided`)
+// are read without acting, so that every CTA has read every sweep of its slots; the leader
+// takes the deciding sweep's maximum |res| for the report.
+template <class Team>
+__device__ __forceinline__ bool lag_drain(const SsaArgs &a, const Team &t, PatchSmem &ps, unsigned int base,
+                                          int decided, int sweeps, bool leader, double &maxres) {
+  const int last = decided;
+  while (decided < sweeps) {
+    ++decided;
+    if (lag_decide(a, t, ps, base + (unsigned)(decided - 1)) < 0) {
+      if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu;
+      return false;
+    }
+  }
+  if (leader && last > 0) maxres = lag_residual_of(a, base + (unsigned)(last - 1));
+  return true;
 }
 
 // Patch b's slice table, edge range and synchronisation set into shared memory.
 template <class Args>
 __device__ __forceinline__ void load_patch(const Args &a, int b, PatchSmem &ps) {
+  if (threadIdx.x < 8) ps.lag_prev[threadIdx.x] = 0ull;
   if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
   if (threadIdx.x == 0) {
     ps.edge0 = a.patch_edge0[b];
@@ -1215,6 +1268,7 @@ __device__ __forceinline__ void load_patch(const Args &a, int b, PatchSmem &ps) 
 // Patch b's halo program (phase slice ranges and slice table), own rows, halo slots and the
 // patches of its start-of-sweep wait into shared memory.
 __device__ __forceinline__ void load_patch_halo(const SsaArgs &a, int b, PatchSmem &ps) {
+  if (threadIdx.x < 8) ps.lag_prev[threadIdx.x] = 0ull;
   if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
   if (threadIdx.x < 8) ps.hps[threadIdx.x] = a.hp_slice[b * 7 + threadIdx.x];
   if (threadIdx.x == 0) {
@@ -1255,6 +1309,11 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
   T *const hbuf0 = reinterpret_cast<T *>(kM ? (void *)a.dUV : (void *)a.UV);
   T *const hbuf1 = reinterpret_cast<T *>(kM ? (void *)a.dUVb : (void *)a.UVb);
   T *const hld = reinterpret_cast<T *>(ufe_local_rows);
+  int *const hidx = reinterpret_cast<int *>(ufe_local_rows + (size_t)a.halo_index_off);
+  if constexpr (kHalo) {
+    for (int i = threadIdx.x; i < ps.nh; i += blockDim.x) hidx[i] = a.hload_dev[ps.hl0 + i];
+    __syncthreads();
+  }
   // (Re)load the mirror from global memory: at the start and after the grid-wide phases
   // that rewrite every row (fold, reset). Halo sweeps: the own rows of the working copy, also
   // copied into the second buffer, which then holds every row that no sweep writes (Dirichlet
@@ -1331,7 +1390,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         const int slot = sweeps % 3;
         if (!kLag && leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
         if (!synced) wait_neighbours(a, ps, phases, t.bar());
-        halo_load(a, ps, hld, par ? hbuf1 : hbuf0);
+        halo_load(ps, hidx, hld, par ? hbuf1 : hbuf0);
         __syncthreads();
         UFE_TM(kTmWaitColour);
         T *const out = par ? hbuf0 : hbuf1;
@@ -1370,14 +1429,11 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
           int act = 0;             // 1: converged, 2: diverged
           while (decided < upto && act == 0) {
             ++decided;
-            double r;
-            if (!lag_residual(a, t, base + (unsigned)(decided - 1), r)) {
+            act = lag_decide(a, t, ps, base + (unsigned)(decided - 1));
+            if (act < 0) {
               if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu;
               return false;
             }
-            maxres = r;
-            if (r < a.tol) act = 1;
-            else if (r > 1e6) act = 2;
           }
           UFE_TM(kTmDecide);
           if (act == 1) {
@@ -1432,6 +1488,9 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
           UFE_TM(kTmOther);
         }
       }
+      if constexpr (kLag) {
+        if (!lag_drain(a, t, ps, base, decided, sweeps, leader, maxres)) return false;
+      }
       // the final own rows into the canonical buffer before the grid-wide phases read it
       const bool commit = par || (kLag && !synced);
       if (par) halo_store_own(ps, hld, hbuf0);
@@ -1463,7 +1522,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
           publish_progress(a, t, phases);
           UFE_TM(kTmColour);
         }
-        lag_arrive(ctl, G, mx);
+        lag_arrive(a, G, mx);
         UFE_TM(kTmArrive);
         wait_neighbours(a, ps, phases, t.bar());
         UFE_TM(kTmWaitBoundary);
@@ -1483,14 +1542,11 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         int act = 0;             // 1: converged, 2: diverged
         while (decided < upto && act == 0) {
           ++decided;
-          double r;
-          if (!lag_residual(a, t, base + (unsigned)(decided - 1), r)) {
+          act = lag_decide(a, t, ps, base + (unsigned)(decided - 1));
+          if (act < 0) {
             if (threadIdx.x == 0) a.prog[32 * t.rank()] = 0x7fffffffu;
             return false;
           }
-          maxres = r;
-          if (r < a.tol) act = 1;
-          else if (r > 1e6) act = 2;
         }
         UFE_TM(kTmDecide);
         if (act == 1) {
@@ -1513,6 +1569,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         }
         UFE_TM(kTmOther);
       }
+      if (!lag_drain(a, t, ps, base, decided, sweeps, leader, maxres)) return false;
       if (!synced) UFE_GRID_SYNC();
       UFE_TM(kTmGrid);
     } else
@@ -2650,6 +2707,8 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     const bool halo = m.has_halo && mode != kExact64 && (size_t)m.max_local * elem <= kLocalRowsMaxBytes &&
                       !(henv && henv[0] == '0');
     size_t bytes = halo ? (size_t)m.max_local * elem : (size_t)m.max_patch_slices * kSlice * elem;
+    a.halo_index_off = (int)bytes;
+    if (halo) bytes += (size_t)m.max_halo * sizeof(int);
     const char *env = std::getenv("UFE_SSA_LOCAL_ROWS");
     bool local = halo || (mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0'));
     const void *fn = persistent_kernel(mode, halo);
