@@ -111,6 +111,7 @@ struct DevMesh {
   // their entries as local columns and coefficients, in the reference's neighbour order.
   bool has_halo = false;
   int max_local = 0;            // largest own slots + halo rows of a patch
+  int max_halo = 0;             // largest number of halo rows of a patch
   int max_hslices = 0;          // largest number of program slices of a patch
   int max_hsync = 0;
   int n_hslices = 0;

@@ -450,6 +450,7 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
       }
       if (n_own + (int)halo.size() > 65535) { halo_ok = false; break; }
       m.max_local = std::max(m.max_local, n_own + (int)halo.size());
+      m.max_halo = std::max(m.max_halo, (int)halo.size());
       for (int p : halo) hreads[b].push_back(patch_of[orig_of_dev[p]]);
       hload_dev.insert(hload_dev.end(), halo.begin(), halo.end());
       hload_ptr.push_back((int)hload_dev.size());
