@@ -74,7 +74,7 @@ def mesh_counts(mesh):
     return dict(nV=nV, nA=nA, nnz_all=nnz_all, nnz_act=nnz_act, n_act=n_act, n_edge=n_edge, nb_bnd=nb_bnd)
 
 
-def algorithmic_bytes(c, st, mixed: bool, refold: int = 64):
+def algorithmic_bytes(c, st, mixed: bool, refold: int = 128):
     """Compulsory DRAM bytes of one persistent-kernel launch (each array touched once per
     phase; neighbour gathers of U,V counted once through the row's own U,V)."""
     if not mixed:
@@ -372,7 +372,7 @@ def profile_case(args):
     timers = hasattr(L, "ufe_debug_phase_cycles")
     if timers:
         import ctypes as ct
-        NT = 9
+        NT = 14   # 8 categories, the sweep count, the 5 colour phases of the halo sweeps
         buf = (ct.c_ulonglong * (NT + 1024 * NT))()
         L.ufe_debug_phase_cycles.restype = ct.c_int
         L.ufe_debug_phase_cycles(buf, NT + 1024 * NT, 1)
@@ -395,17 +395,20 @@ def profile_case(args):
             "cycles_per_cta_sweep": {k: float(v) / max(sweeps_cta, 1.0) for k, v in zip(names, cyc)}}
         # per CTA: the time it spends working (not waiting for other CTAs) per sweep
         per = np.array([buf[NT + i] for i in range(1024 * NT)], dtype=np.float64).reshape(1024, NT)
-        per = per[per[:, NT - 1] > 0]
+        per = per[per[:, 8] > 0]
         waits = per[:, 0] + per[:, 3] + per[:, 5] + per[:, 6]
-        busy = (per[:, :NT - 1].sum(axis=1) - waits) / per[:, NT - 1]
-        us = line["us_per_sweep"] / (per[:, :NT - 1].sum(axis=1) / per[:, NT - 1]).mean()
+        tot = per[:, :8].sum(axis=1)
+        busy = (tot - waits) / per[:, 8]
+        us = line["us_per_sweep"] / (tot / per[:, 8]).mean()
+        line["phase_timers"]["colour_phase_us"] = [float((per[:, 9 + f] / per[:, 8]).mean() * us) for f in range(5)]
+        line["phase_timers"]["colour_phase_us_max"] = [float((per[:, 9 + f] / per[:, 8]).max() * us) for f in range(5)]
         line["phase_timers"]["busy_us_per_sweep_per_cta"] = {
             "min": float(busy.min() * us), "mean": float(busy.mean() * us), "max": float(busy.max() * us),
             "slowest_ctas": [int(i) for i in np.argsort(-busy)[:8]],
-            "colour_us_by_cta_max": float((per[:, 1] / per[:, NT - 1]).max() * us),
-            "boundary_us_by_cta_max": float((per[:, 4] / per[:, NT - 1]).max() * us),
+            "colour_us_by_cta_max": float((per[:, 1] / per[:, 8]).max() * us),
+            "boundary_us_by_cta_max": float((per[:, 4] / per[:, 8]).max() * us),
             "all_busy_us": [round(float(b * us), 2) for b in busy],
-            "per_cta_us": {k: [round(float(v * us), 2) for v in per[:, i] / per[:, NT - 1]]
+            "per_cta_us": {k: [round(float(v * us), 2) for v in per[:, i] / per[:, 8]]
                            for i, k in enumerate(names)}}
     print(json.dumps(line))
     dm.close()

@@ -138,6 +138,7 @@ struct SsaArgs {
   int fp32_visc;
   int local_rows;          // keep the patch's own velocities (mixed: corrections) in shared memory
   int halo_index_off;      // halo sweeps: byte offset of the halo slots' device rows in dynamic shared memory
+  int stage_off, stage_bytes;   // halo sweeps, mixed: the resident program slices' area in dynamic shared memory
   long long timeout_ns;
 };
 
@@ -182,7 +183,8 @@ enum PhaseTimer : int {
   kTmGrid,             // team barriers inside the SOR loop
   kTmOther,            // viscosity, RN, coefficients, defect, fold, refolds
   kTmSweeps,           // (count) sweeps of this CTA
-  kTmCount
+  kTmColour0,          // halo sweeps: colour phases 1..5 one by one (also counted in kTmColour)
+  kTmCount = kTmColour0 + 5
 };
 #if UFE_PHASE_TIMERS
 __device__ unsigned long long g_phase_cycles[kTmCount];
@@ -190,15 +192,24 @@ constexpr int kTmMaxCta = 1024;
 __device__ unsigned long long g_phase_cycles_cta[kTmMaxCta * kTmCount];   // per CTA, single solves
 #define UFE_TM_DECL                                   \
   __shared__ unsigned long long s_tm[kTmCount];       \
-  __shared__ long long s_tm0;                         \
+  __shared__ long long s_tm0, s_tm1;                  \
   if (threadIdx.x < kTmCount) s_tm[threadIdx.x] = 0;  \
-  if (threadIdx.x == 0) s_tm0 = clock64();
+  if (threadIdx.x == 0) s_tm0 = s_tm1 = clock64();
 #define UFE_TM(cat)                                               \
   do {                                                            \
     if (threadIdx.x == 0) {                                       \
       const long long now_ = clock64();                           \
       s_tm[cat] += (unsigned long long)(now_ - s_tm0);            \
-      s_tm0 = now_;                                               \
+      s_tm0 = s_tm1 = now_;                                       \
+    }                                                             \
+  } while (0)
+// a sub-interval since the last stamp of either kind, without closing the current category
+#define UFE_TM_SUB(cat)                                           \
+  do {                                                            \
+    if (threadIdx.x == 0) {                                       \
+      const long long now_ = clock64();                           \
+      s_tm[cat] += (unsigned long long)(now_ - s_tm1);            \
+      s_tm1 = now_;                                               \
     }                                                             \
   } while (0)
 #define UFE_TM_COUNT(cat) do { if (threadIdx.x == 0) s_tm[cat] += 1; } while (0)
@@ -212,6 +223,7 @@ __device__ unsigned long long g_phase_cycles_cta[kTmMaxCta * kTmCount];   // per
 #else
 #define UFE_TM_DECL
 #define UFE_TM(cat) do { } while (0)
+#define UFE_TM_SUB(cat) do { } while (0)
 #define UFE_TM_COUNT(cat) do { } while (0)
 #define UFE_TM_FLUSH() do { } while (0)
 #endif
@@ -487,6 +499,9 @@ struct PatchSmem {
   // lagged decisions: each slot's arrival word as this CTA last read it (lag_decide)
   unsigned long long lag_prev[8];
   int lag_act[2];
+  // halo sweeps, mixed: offset (16-byte units) of each program slice's resident copy in the
+  // staging area, -1 = read from global memory (halo_stage)
+  short soff[kMaxPatchSlices];
 };
 
 // One colour of the FP64 sweep in the reference's expression order (parity mode).
@@ -735,8 +750,8 @@ __device__ __forceinline__ int halo_global(const SsaArgs &a, const PatchSmem &ps
 // One slice of a colour phase of the FP32 correction sweep (as phase_sweep32), its entries
 // read through pointers already offset by the lane (entry k of the lane at [32 k]).
 __device__ __forceinline__ void slice32(const SsaArgs &a, const PatchSmem &ps, int w, const uint16_t *pc,
-                                        const float2 *pcu, int l, int g, float s3, float4 sd, float2 *ld, float2 *out,
-                                        float omega, float &mx) {
+                                        const float2 *pcu, int l, float s3, float4 sd, const int *hidx, float2 *ld,
+                                        float2 *out, float omega, float &mx) {
   int j[kBatch];
   float2 c[kBatch];
 #pragma unroll
@@ -744,7 +759,8 @@ __device__ __forceinline__ void slice32(const SsaArgs &a, const PatchSmem &ps, i
     j[q] = q < w ? (int)pc[q * kSlice] : (int)kNoCol;
     c[q] = q < w ? pcu[q * kSlice] : make_float2(0.f, 0.f);
   }
-  if (l < 0 || (a.skip && a.skip[g])) return;   // padding slot, or a Dirichlet row
+  if (l < 0) return;   // padding slot
+  if (a.skip && a.skip[l < ps.n_own ? ps.p0 + l : hidx[l - ps.n_own]]) return;   // a Dirichlet row
   const float2 di = ld[l];
   float su = 0.0f, sv = 0.0f;
 #pragma unroll
@@ -768,29 +784,99 @@ __device__ __forceinline__ void slice32(const SsaArgs &a, const PatchSmem &ps, i
   const float2 dn = make_float2(fmaf(-omega, ru, di.x), fmaf(-omega, rv, di.y));
   ld[l] = dn;
   if (l < ps.n_own) {
-    out[g] = dn;
+    out[ps.p0 + l] = dn;
     mx = fmaxf(mx, fmaxf(fabsf(ru), fabsf(rv)));
   }
 }
 
 // Colour phase f of the FP32 correction sweep: warp w takes slices w, w + nwarps, ... (a
-// colour of a 200k-vertex patch has 43-50 slices for 32 warps). Staging a warp's second slice
-// in shared memory by asynchronous copies issued before its first measured slower (20.5
-// against 19.5 us per sweep), as did loading two slices at once at 768 threads (28.6 against
-// 27.1 us before the boundary-phase change).
-__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, float2 *ld, float2 *out) {
+// colour of a 200k-vertex patch has 42-50 slices for 32 warps). A round of 32 slices costs
+// about 0.5 us plus the time to bring its program data (about 100 KB) from L2 into the SM,
+// which is why the resident slices (halo_stage) are read from shared memory.
+__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, const unsigned char *stage,
+                                            const int *hidx, float2 *ld, float2 *out) {
   const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
   const float omega = (float)a.omega;
   float mx = 0.0f;
   const int base = ps.hps[0];
   for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
     const int w = ps.w[s - base];
-    const int64_t e0 = ps.e0[s - base] + lane;
-    const int slot = s * kSlice + lane;
-    slice32(a, ps, w, a.hcol + e0, a.hcuv32 + e0, a.hrow_l[slot], a.hrow_g[slot], a.hs3_32[slot], a.hsd32[slot], ld,
-            out, omega, mx);
+    const int so = ps.soff[s - base];
+    if (so >= 0) {
+      const unsigned char *b = stage + 16 * so;
+      const int *rl = reinterpret_cast<const int *>(b + w * kSlice * 10);
+      slice32(a, ps, w, reinterpret_cast<const uint16_t *>(b) + lane, reinterpret_cast<const float2 *>(b + w * kSlice * 2) + lane,
+              rl[lane], reinterpret_cast<const float *>(rl)[kSlice + lane], reinterpret_cast<const float4 *>(rl + 2 * kSlice)[lane],
+              hidx, ld, out, omega, mx);
+    } else {
+      const int64_t e0 = ps.e0[s - base] + lane;
+      const int slot = s * kSlice + lane;
+      slice32(a, ps, w, a.hcol + e0, a.hcuv32 + e0, a.hrow_l[slot], a.hs3_32[slot], a.hsd32[slot], hidx, ld, out, omega,
+              mx);
+    }
   }
   return abs_bits((double)mx);
+}
+
+// Resident program slices (mixed halo sweeps). The shared memory left after the working copy
+// and the halo indices (stage_bytes) holds, for the whole solve, copies of some of the patch's
+// colour-phase slices: the entries' local columns and coefficients, then per slot the local row,
+// 3 sNxy and the row data of halo_refresh (refreshed there with the global copy): w * 320 + 768
+// bytes for a slice of width w. Which: whole rounds of 32 slices, smallest first — the rounds after
+// the first of a colour with more than 32 slices, and whole colours of at most 32 slices — as many
+// as fit. Thread 0 plans, then the CTA copies the static parts.
+__device__ __forceinline__ int stage_slice_bytes(int w) { return w * kSlice * 10 + 2 * kSlice * 4 + kSlice * 16; }
+
+__device__ void halo_stage(const SsaArgs &a, PatchSmem &ps, unsigned char *stage) {
+  const int base = ps.hps[0];
+  for (int s = ps.hps[0] + (int)threadIdx.x; s < ps.hps[7]; s += blockDim.x) ps.soff[s - base] = -1;
+  __syncthreads();
+  constexpr int kMaxUnits = 40;
+  __shared__ int u0[kMaxUnits], u1[kMaxUnits], ub[kMaxUnits];
+  if (threadIdx.x == 0 && a.stage_bytes > 0) {
+    int nu = 0;
+    for (int f = 0; f < 5; ++f) {
+      const int s0 = ps.hps[f], s1 = ps.hps[f + 1];
+      for (int r = s1 - s0 <= kSlice ? s0 : s0 + kSlice; r < s1 && nu < kMaxUnits; r += kSlice) {
+        u0[nu] = r;
+        u1[nu] = r + kSlice < s1 ? r + kSlice : s1;
+        int b = 0;
+        for (int q = u0[nu]; q < u1[nu]; ++q) b += stage_slice_bytes(ps.w[q - base]);
+        ub[nu++] = b;
+      }
+    }
+    int used = 0;
+    for (;;) {
+      int best = -1;
+      for (int k = 0; k < nu; ++k)
+        if (ub[k] >= 0 && (best < 0 || ub[k] < ub[best])) best = k;
+      if (best < 0 || used + ub[best] > a.stage_bytes) break;
+      for (int q = u0[best]; q < u1[best]; ++q) {
+        ps.soff[q - base] = (short)(used / 16);
+        used += stage_slice_bytes(ps.w[q - base]);
+      }
+      ub[best] = -1;
+    }
+  }
+  __syncthreads();
+  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+  for (int s = ps.hps[0] + wid; s < ps.hps[5]; s += nwarps) {
+    const int so = ps.soff[s - base];
+    if (so < 0) continue;
+    unsigned char *b = stage + 16 * so;
+    const int w = ps.w[s - base];
+    const int64_t e0 = ps.e0[s - base];
+    uint16_t *pc = reinterpret_cast<uint16_t *>(b);
+    float2 *pcu = reinterpret_cast<float2 *>(b + w * kSlice * 2);
+    for (int k = lane; k < w * kSlice; k += kSlice) {
+      pc[k] = a.hcol[e0 + k];
+      pcu[k] = a.hcuv32[e0 + k];
+    }
+    int *rl = reinterpret_cast<int *>(b + w * kSlice * 10);
+    rl[lane] = a.hrow_l[s * kSlice + lane];
+    reinterpret_cast<float *>(rl)[kSlice + lane] = a.hs3_32[s * kSlice + lane];
+  }
+  __syncthreads();
 }
 
 // Colour phase f of the FP64 sweeps (as phase_sweep_exact and phase_sweep_fast).
@@ -943,13 +1029,19 @@ __device__ void halo_boundary(const SsaArgs &a, const PatchSmem &ps, int f, T *l
 // and the right-hand side), refreshed by each CTA for its own program slots once the
 // grid-wide phase that wrote them is complete.
 template <int kMode>
-__device__ __forceinline__ void halo_refresh(const SsaArgs &a, const PatchSmem &ps) {
+__device__ __forceinline__ void halo_refresh(const SsaArgs &a, const PatchSmem &ps, unsigned char *stage) {
   for (int k = 32 * ps.hps[0] + (int)threadIdx.x; k < 32 * ps.hps[7]; k += blockDim.x) {
     if (a.hrow_l[k] < 0) continue;
     const int g = a.hrow_g[k];
     if constexpr (kMode == kMixed) {
       const float2 r = a.rcp32[g], d = a.r0[g];
       a.hsd32[k] = make_float4(r.x, r.y, d.x, d.y);
+      if (k < 32 * ps.hps[5]) {
+        const int s = k / kSlice, so = ps.soff[s - ps.hps[0]];
+        if (so >= 0)
+          reinterpret_cast<float4 *>(stage + 16 * so + ps.w[s - ps.hps[0]] * kSlice * 10 + 2 * kSlice * 4)[k % kSlice] =
+              make_float4(r.x, r.y, d.x, d.y);
+      }
       if (k >= 32 * ps.hps[5]) {
         // boundary slots: c0 = mean of the averaged neighbours' u0 minus the row's u0 (FP64),
         // and 1 / (number averaged), for halo_boundary
@@ -1310,9 +1402,11 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
   T *const hbuf1 = reinterpret_cast<T *>(kM ? (void *)a.dUVb : (void *)a.UVb);
   T *const hld = reinterpret_cast<T *>(ufe_local_rows);
   int *const hidx = reinterpret_cast<int *>(ufe_local_rows + (size_t)a.halo_index_off);
+  unsigned char *const hstage = ufe_local_rows + (size_t)a.stage_off;
   if constexpr (kHalo) {
     for (int i = threadIdx.x; i < ps.nh; i += blockDim.x) hidx[i] = a.hload_dev[ps.hl0 + i];
     __syncthreads();
+    if constexpr (kM) halo_stage(a, ps, hstage);
   }
   // (Re)load the mirror from global memory: at the start and after the grid-wide phases
   // that rewrite every row (fold, reset). Halo sweeps: the own rows of the working copy, also
@@ -1381,7 +1475,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
       bool synced = true;
       int decided = 0;
       const unsigned int base = gsweep;
-      halo_refresh<kMode>(a, ps);
+      halo_refresh<kMode>(a, ps, hstage);
       UFE_TM(kTmOther);
       while (!lin_done && sweeps < a.max_inner) {
         ++sweeps;
@@ -1398,10 +1492,11 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         for (int f = 0; f < 5; ++f) {
           if (ps.hps[f + 1] == ps.hps[f]) continue;
           unsigned long long m;
-          if constexpr (kM) m = halo_colour32(a, ps, f, hld, out);
+          if constexpr (kM) m = halo_colour32(a, ps, f, hstage, hidx, hld, out);
           else m = halo_colour64<kMode == kExact64>(a, ps, f, hld, out);
           mx = m > mx ? m : mx;
           __syncthreads();
+          UFE_TM_SUB(kTmColour0 + f);
         }
         UFE_TM(kTmColour);
         for (int f = 5; f < 7; ++f) {
@@ -1454,7 +1549,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
             reload();
             phase_defect(a, t);
             UFE_GRID_SYNC();
-            halo_refresh<kMode>(a, ps);
+            halo_refresh<kMode>(a, ps, hstage);
           }
           UFE_TM(kTmOther);
         } else {
@@ -1483,7 +1578,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
             reload();
             phase_defect(a, t);
             UFE_GRID_SYNC();
-            halo_refresh<kMode>(a, ps);
+            halo_refresh<kMode>(a, ps, hstage);
           }
           UFE_TM(kTmOther);
         }
@@ -2611,7 +2706,9 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->max_inner = p->SSA_max_inner_loops; a->max_outer = p->SSA_max_outer_loops;
   a->sliding_law = p->sliding_law; a->has_beta = w->has_beta;
   w->sliding_law = p->sliding_law;
-  a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 64;   // 64: 26.2 against 27.4 us per sweep at 32 (200k dome)
+  // 128 on the 200k dome: 226.0 ms per solve against 234.2 at 64 and 221.7 at 256, with the same
+  // error against the FP64 solve (1.17e-7) and the same sweep count within one
+  a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 128;
   a->fp32_visc = p->mixed_fp32_viscosity != 0;
   a->timeout_ns = wait_timeout_ns();
   return rc;
@@ -2709,6 +2806,8 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
     size_t bytes = halo ? (size_t)m.max_local * elem : (size_t)m.max_patch_slices * kSlice * elem;
     a.halo_index_off = (int)bytes;
     if (halo) bytes += (size_t)m.max_halo * sizeof(int);
+    a.stage_off = (int)((bytes + 15) / 16 * 16);
+    a.stage_bytes = 0;
     const char *env = std::getenv("UFE_SSA_LOCAL_ROWS");
     bool local = halo || (mode == kMixed && bytes <= kLocalRowsMaxBytes && !(env && env[0] == '0'));
     const void *fn = persistent_kernel(mode, halo);
@@ -2720,6 +2819,14 @@ extern "C" int ufe_ssa_run(ufe_mesh_h h, const ufe_params *p, ufe_ssa_stats *sta
       int smem_sm = 0, per_sm = 0;
       rc = cuda_status(cudaFuncGetAttributes(&fa, fn), "function attributes");
       if (!rc) rc = cuda_status(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device), "smem per SM");
+      if (!rc && halo && mode == kMixed) {
+        // the resident program slices take what one CTA per SM leaves of the shared memory
+        int optin = 0;
+        rc = cuda_status(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device), "smem opt-in");
+        const long long room = (long long)optin - (long long)fa.sharedSizeBytes - (long long)a.stage_off - 1024;
+        a.stage_bytes = room > 0 ? (int)(room / 16 * 16) : 0;
+        bytes = (size_t)a.stage_off + (size_t)a.stage_bytes;
+      }
       if (!rc) rc = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes), "smem attribute");
       const int pct = smem_sm > 0 ? (int)std::min<size_t>(100, (100 * (bytes + fa.sharedSizeBytes + 2048) + smem_sm - 1) / smem_sm) : 100;
       if (!rc) rc = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct), "carveout");
