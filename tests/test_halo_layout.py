@@ -115,6 +115,17 @@ def test_halo_program_indices_in_bounds(layout):
         own = rl[rl >= 0] < n_own
         assert np.all((g[own] >= ps[b, 0] * 32) & (g[own] < ps[b, 6] * 32))
         assert np.all((g[~own] < ps[b, 0] * 32) | (g[~own] >= ps[b, 6] * 32))
+    # colour 1's rows that a sweep runs before its halo load: own rows reading own rows only
+    hs = lay["hp_split"]
+    assert hs.size == n_patch
+    for b in range(n_patch):
+        n_own = int(ps[b, 6] - ps[b, 0]) * 32
+        assert hp[7 * b] <= hs[b] <= hp[7 * b + 1]
+        for s in range(int(hp[7 * b]), int(hs[b])):
+            rl = lay["hrow_l"][32 * s:32 * s + 32]
+            assert np.all(rl < n_own)
+            cols = lay["hcol"][e0[s]:e0[s] + 32 * int(w[s])]
+            assert np.all((cols == NO_COL) | (cols < n_own))
     sp, sl = lay["hsync_ptr"], lay["hsync_list"]
     assert sp.size == n_patch + 1 and np.all(sl < n_patch)
     for b in range(n_patch):     # symmetric: a patch waits for every patch it reads and reads it back
@@ -188,10 +199,12 @@ def test_halo_sweeps_equal_the_sequential_sweep(layout):
             r = orig[p]
             U[p] = _mean([U[dev[CA[r, c]]] for c in range(nCA[r])])
 
-    # the halo program, patches as if concurrent: halo slots from buf[par], own rows to buf[par ^ 1]
+    # the halo program, patches as if concurrent: halo slots from buf[par], own rows to buf[par ^ 1];
+    # colour 1's halo-free rows before the halo load, as the kernel runs them
     ps = lay["patch_slice"].reshape(n_patch, 7)
     hp, e0, w = lay["hp_slice"], lay["hslice_e0"], lay["hslice_w"]
     hl, hd = lay["hload_ptr"], lay["hload_dev"]
+    split = lay["hp_split"]
     rowl, rowg, hcol, hcuv = lay["hrow_l"], lay["hrow_g"], lay["hcol"], lay["hcuv"]
     buf = [U0.copy(), U0.copy()]
     local = []
@@ -203,9 +216,14 @@ def test_halo_sweeps_equal_the_sequential_sweep(layout):
         for b in range(n_patch):
             ld = local[b]
             p0, n_own = ps[b, 0] * 32, (ps[b, 6] - ps[b, 0]) * 32
-            ld[n_own:] = buf[par][hd[hl[b]:hl[b + 1]]]
-            for f in range(7):
-                for s in range(hp[7 * b + f], hp[7 * b + f + 1]):
+            ld[n_own:] = np.nan   # halo slots not yet loaded: a halo-free row must not read them
+            order = [(0, hp[7 * b], split[b]), ("load", 0, 0), (0, split[b], hp[7 * b + 1])]
+            order += [(f, hp[7 * b + f], hp[7 * b + f + 1]) for f in range(1, 7)]
+            for f, s_begin, s_end in order:
+                if f == "load":
+                    ld[n_own:] = buf[par][hd[hl[b]:hl[b + 1]]]
+                    continue
+                for s in range(s_begin, s_end):
                     for lane in range(32):
                         l, g = rowl[32 * s + lane], rowg[32 * s + lane]
                         if l < 0 or (f < 5 and skip[g]):

@@ -117,6 +117,7 @@ struct DevMesh {
   int n_hslices = 0;
   int64_t n_hE = 0;
   int *hp_slice = nullptr;      // [n_patch * 7 + 1] first program slice of phases 0..6 of each patch, then the end
+  int *hp_split = nullptr;      // [n_patch] first slice of phase 0's rows that read halo slots (the others come first)
   int *hslice_e0 = nullptr;     // [n_hslices] first entry of a program slice
   uint8_t *hslice_w = nullptr;  // [n_hslices] entries per slot
   int *hrow_l = nullptr;        // [n_hslices * 32] local row, -1 = padding

@@ -57,7 +57,7 @@ void free_mesh(DevMesh &m) {
   void *ptrs[] = {m.orig_of_dev, m.dev_of_orig, m.deg, m.slice_ptr, m.col, m.cuv, m.nxy,
                   m.cuv32, m.nxy32, m.h_nxy, m.h_cuv, m.sNxy, m.s3Nxy, m.h_nxy32, m.s3Nxy32, m.bnd_ptr,
                   m.bnd_nbr, m.V, m.Aci12, m.iAci, m.nC, m.patch_slice, m.patch_edge0, m.edge_row,
-                  m.sync_ptr, m.sync_list, m.slice_e0, m.slice_w, m.slice_g, m.hp_slice, m.hslice_e0,
+                  m.sync_ptr, m.sync_list, m.slice_e0, m.slice_w, m.slice_g, m.hp_slice, m.hp_split, m.hslice_e0,
                   m.hslice_w, m.hrow_l, m.hrow_g, m.hcol, m.hcuv32, m.hcuv, m.hload_ptr, m.hload_dev,
                   m.hsync_ptr, m.hsync_list, m.hs3_32, m.hs3};
   for (void *p : ptrs)
@@ -400,7 +400,7 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
   // CAaAc neighbours (edge rows: the non-edge ones). A patch must also update every row of an
   // earlier phase that one of its updates reads (transitively): such a row is current only
   // after its own update in this sweep. Everything else it reads is a start-of-sweep value.
-  std::vector<int> hp_slice, hslice_e0, hrow_l, hrow_g, hload_ptr(1, 0), hload_dev, hsync_ptr(1, 0), hsync_list;
+  std::vector<int> hp_slice, hp_split, hslice_e0, hrow_l, hrow_g, hload_ptr(1, 0), hload_dev, hsync_ptr(1, 0), hsync_list;
   std::vector<uint8_t> hslice_w;
   std::vector<uint16_t> hcol;
   std::vector<float2> hcuv32;
@@ -465,11 +465,32 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
           if (ph[p] == f) rows.push_back(p);
         for (int p : R)
           if ((p < p0 || p >= p1) && ph[p] == f) rows.push_back(p);
-        bank_aware_slices(rows, [&](int p, int *cols) {
+        auto cols_of = [&](int p, int *cols) {
           reads_of(p, rd);
           for (size_t k = 0; k < rd.size(); ++k) cols[k] = local_of(rd[k]);
           return (int)rd.size();
-        });
+        };
+        if (f == 0) {
+          // colour 1's own rows that read no halo slot come first: a sweep runs them before it
+          // waits for the neighbouring patches
+          std::vector<int> early, late;
+          for (int p : rows) {
+            bool own_only = p >= p0 && p < p1;
+            if (own_only) {
+              reads_of(p, rd);
+              for (int j : rd)
+                if (local_of(j) >= n_own) { own_only = false; break; }
+            }
+            (own_only ? early : late).push_back(p);
+          }
+          bank_aware_slices(early, cols_of);
+          bank_aware_slices(late, cols_of);
+          hp_split.push_back((int)hslice_e0.size() + (int)(early.size() / kSlice));
+          rows = early;
+          rows.insert(rows.end(), late.begin(), late.end());
+        } else {
+          bank_aware_slices(rows, cols_of);
+        }
         for (size_t s0 = 0; s0 < rows.size(); s0 += kSlice) {
           int w = 0;
           for (int l = 0; l < kSlice; ++l) {
@@ -559,7 +580,7 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
     f.put("orig_of_dev", orig_of_dev); f.put("dev_of_orig", dev_of_orig); f.put("deg", deg);
     f.put("patch_slice", patch_slice); f.put("slice_ptr", slice_ptr); f.put("slice_w", slice_w); f.put("col", col);
     f.put("cuv", cuv); f.put("cuv32", cuv32); f.put("sync_ptr", sync_ptr); f.put("sync_list", sync_list);
-    f.put("hp_slice", hp_slice); f.put("hslice_e0", hslice_e0); f.put("hslice_w", hslice_w);
+    f.put("hp_slice", hp_slice); f.put("hp_split", hp_split); f.put("hslice_e0", hslice_e0); f.put("hslice_w", hslice_w);
     f.put("hrow_l", hrow_l); f.put("hrow_g", hrow_g); f.put("hcol", hcol); f.put("hcuv", hcuv);
     f.put("hcuv32", hcuv32); f.put("hload_ptr", hload_ptr); f.put("hload_dev", hload_dev);
     f.put("hsync_ptr", hsync_ptr); f.put("hsync_list", hsync_list);
@@ -603,6 +624,7 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
   if (!rc) rc = upload(&m.slice_g, slice_g, S, "slice_g");
   if (!rc && m.has_halo) {
     rc = upload(&m.hp_slice, hp_slice, S, "hp_slice");
+    if (!rc) rc = upload(&m.hp_split, hp_split, S, "hp_split");
     if (!rc) rc = upload(&m.hslice_e0, hslice_e0, S, "hslice_e0");
     if (!rc) rc = upload(&m.hslice_w, hslice_w, S, "hslice_w");
     if (!rc) rc = upload(&m.hrow_l, hrow_l, S, "hrow_l");

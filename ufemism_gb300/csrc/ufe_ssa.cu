@@ -101,6 +101,7 @@ struct SsaArgs {
   const int *sync_list;
   // halo sweep program (DevMesh, ufe_internal.h)
   const int *hp_slice, *hslice_e0;
+  const int *hp_split;     // first slice of phase 0's rows that read halo slots
   const uint8_t *hslice_w;
   const int *hrow_l, *hrow_g;
   const uint16_t *hcol;
@@ -123,8 +124,8 @@ struct SsaArgs {
   const uint8_t *skip;    // Dirichlet rows (grounding-line Ac rows under the GL-flux option), may be null
   double2 *UV;            // FP64 velocities (u0 in the mixed path)
   float2 *dUV;            // mixed: correction d
-  double2 *UVb;           // halo sweeps, FP64 modes: the second velocity buffer
-  float2 *dUVb;           // halo sweeps, mixed: the second correction buffer
+  double2 *UVb, *UVc;     // halo sweeps, FP64 modes: the second and third velocity buffers
+  float2 *dUVb, *dUVc;    // halo sweeps, mixed: the second and third correction buffers
   float2 *r0;             // mixed: defect
   float2 *rcp32;          // mixed: FP32 reciprocals of (eu, ev)
   double *eta, *Na, *Nb, *S;
@@ -495,10 +496,13 @@ struct PatchSmem {
   // halo sweeps: program slices of the 7 phases (e0, w hold the program's slices), the own
   // device rows [p0, p0 + n_own) and the halo slots [n_own, n_own + nh) of the working copy
   int hps[8];
+  int hsplit;   // phase 0: slices [hps[0], hsplit) read no halo slot
   int p0, n_own, nh, hl0;
   // lagged decisions: each slot's arrival word as this CTA last read it (lag_decide)
   unsigned long long lag_prev[8];
   int lag_act[2];
+  unsigned long long lag_pre;   // the arrival word of sweep lag_pre_g, read ahead by lag_arrive_publish
+  unsigned int lag_pre_g;
   // halo sweeps, mixed: offset (16-byte units) of each program slice's resident copy in the
   // staging area, -1 = read from global memory (halo_stage)
   short soff[kMaxPatchSlices];
@@ -542,6 +546,10 @@ __device__ unsigned long long phase_sweep_exact(const SsaArgs &a, const PatchSme
 }
 
 constexpr int kBatch = 8;   // neighbour entries loaded in one batch (rows of higher degree load the rest)
+// halo sweeps: warps that wait for the neighbouring patches and load the halo slots while the
+// others run colour 1's halo-free rows (halo_fetch), and the loads each thread issues together
+constexpr int kFetchWarps = 4;
+constexpr int kFetchBatch = 4;
 
 // One colour of the fast FP64 sweep: res = U + ((sum + 3 sNxy V) - RHS) / eu with the
 // reciprocal of eu formed once per Picard iteration, products accumulated with FMA.
@@ -793,13 +801,13 @@ __device__ __forceinline__ void slice32(const SsaArgs &a, const PatchSmem &ps, i
 // colour of a 200k-vertex patch has 42-50 slices for 32 warps). A round of 32 slices costs
 // about 0.5 us plus the time to bring its program data (about 100 KB) from L2 into the SM,
 // which is why the resident slices (halo_stage) are read from shared memory.
-__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int f, const unsigned char *stage,
-                                            const int *hidx, float2 *ld, float2 *out) {
-  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+__device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &ps, int s_begin, int s_end, int nwarps,
+                                            const unsigned char *stage, const int *hidx, float2 *ld, float2 *out) {
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const float omega = (float)a.omega;
   float mx = 0.0f;
   const int base = ps.hps[0];
-  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
+  for (int s = s_begin + wid; s < s_end; s += nwarps) {
     const int w = ps.w[s - base];
     const int so = ps.soff[s - base];
     if (so >= 0) {
@@ -822,9 +830,11 @@ __device__ unsigned long long halo_colour32(const SsaArgs &a, const PatchSmem &p
 // and the halo indices (stage_bytes) holds, for the whole solve, copies of some of the patch's
 // colour-phase slices: the entries' local columns and coefficients, then per slot the local row,
 // 3 sNxy and the row data of halo_refresh (refreshed there with the global copy): w * 320 + 768
-// bytes for a slice of width w. Which: whole rounds of 32 slices, smallest first — the rounds after
-// the first of a colour with more than 32 slices, and whole colours of at most 32 slices — as many
-// as fit. Thread 0 plans, then the CTA copies the static parts.
+// bytes for a slice of width w. Which: whole rounds (a slice per warp: 32 slices, 28 for colour
+// 1's halo-free rows, which four warps leave to the halo fetch), smallest first — the rounds after
+// the first of a colour, and whole colours of at most one round (colour 1 counting as two: its
+// halo-free rows and the others) — as many as fit. Thread 0 plans, then the CTA copies the static
+// parts.
 __device__ __forceinline__ int stage_slice_bytes(int w) { return w * kSlice * 10 + 2 * kSlice * 4 + kSlice * 16; }
 
 __device__ void halo_stage(const SsaArgs &a, PatchSmem &ps, unsigned char *stage) {
@@ -835,11 +845,13 @@ __device__ void halo_stage(const SsaArgs &a, PatchSmem &ps, unsigned char *stage
   __shared__ int u0[kMaxUnits], u1[kMaxUnits], ub[kMaxUnits];
   if (threadIdx.x == 0 && a.stage_bytes > 0) {
     int nu = 0;
-    for (int f = 0; f < 5; ++f) {
-      const int s0 = ps.hps[f], s1 = ps.hps[f + 1];
-      for (int r = s1 - s0 <= kSlice ? s0 : s0 + kSlice; r < s1 && nu < kMaxUnits; r += kSlice) {
+    for (int f = -1; f < 5; ++f) {   // -1: colour 1's halo-free rows, 0: its other rows
+      const int s0 = f < 0 ? ps.hps[0] : f == 0 ? ps.hsplit : ps.hps[f];
+      const int s1 = f < 0 ? ps.hsplit : ps.hps[f + 1];
+      const int rs = (int)(blockDim.x >> 5) - (f < 0 ? kFetchWarps : 0);   // slices per round
+      for (int r = s1 - s0 <= rs ? s0 : s0 + rs; r < s1 && nu < kMaxUnits; r += rs) {
         u0[nu] = r;
-        u1[nu] = r + kSlice < s1 ? r + kSlice : s1;
+        u1[nu] = r + rs < s1 ? r + rs : s1;
         int b = 0;
         for (int q = u0[nu]; q < u1[nu]; ++q) b += stage_slice_bytes(ps.w[q - base]);
         ub[nu++] = b;
@@ -881,12 +893,13 @@ __device__ void halo_stage(const SsaArgs &a, PatchSmem &ps, unsigned char *stage
 
 // Colour phase f of the FP64 sweeps (as phase_sweep_exact and phase_sweep_fast).
 template <bool kExact>
-__device__ unsigned long long halo_colour64(const SsaArgs &a, const PatchSmem &ps, int f, double2 *ld, double2 *out) {
-  const int wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+__device__ unsigned long long halo_colour64(const SsaArgs &a, const PatchSmem &ps, int s_begin, int s_end, int nwarps,
+                                            double2 *ld, double2 *out) {
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double omega = a.omega;
   unsigned long long mx = 0ull;
   const int base = ps.hps[0];
-  for (int s = ps.hps[f] + wid; s < ps.hps[f + 1]; s += nwarps) {
+  for (int s = s_begin + wid; s < s_end; s += nwarps) {
     const int w = ps.w[s - base];
     const int64_t e0 = ps.e0[s - base] + lane;
     const int slot = s * kSlice + lane;
@@ -1203,6 +1216,53 @@ __device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &
   __syncthreads();
 }
 
+// wait_neighbours and halo_load by the last kFetchWarps warps (the others meanwhile run the
+// rows that read no halo slot); the caller's CTA barrier then orders the halo slots before their
+// readers. The loads of a thread are issued together (up to kFetchBatch in flight).
+template <class T>
+__device__ __forceinline__ void halo_fetch(const SsaArgs &a, const PatchSmem &ps, unsigned int target,
+                                           unsigned int *team_bar, bool wait, const int *hidx, T *ld, const T *in) {
+  const int ft = (int)threadIdx.x - (int)(blockDim.x - kFetchWarps * kSlice);   // 0 .. 127
+  if (wait) {
+    for (int i = ft; i < ps.nsync; i += kFetchWarps * kSlice) {
+      const unsigned int *q = a.prog + 32 * ps.sync[i];
+      unsigned int v = ld_acquire_u32(q);
+      if ((int)(v - target) < 0) {
+        const unsigned long long t0 = globaltimer_ns();
+        unsigned int ns = 16;
+        for (;;) {
+          __nanosleep(ns);
+          if (ns < 64) ns <<= 1;
+          v = ld_acquire_u32(q);
+          if ((int)(v - target) >= 0) break;
+          if (*(volatile unsigned int *)team_bar & kBarrierError) break;   // another CTA failed
+          if ((long long)(globaltimer_ns() - t0) > a.timeout_ns) {
+            atomicCAS(&a.ctl->err, 0, (int)UFE_TIMEOUT);
+            atomicOr(team_bar, kBarrierError);
+            break;
+          }
+        }
+      }
+    }
+    // the fetch warps' barrier (id 1) orders every acquire before their halo loads
+    asm volatile("bar.sync 1, %0;" ::"r"(kFetchWarps * kSlice) : "memory");
+  }
+  constexpr int kStride = kFetchWarps * kSlice;
+  for (int i0 = ft; i0 < ps.nh; i0 += kStride * kFetchBatch) {
+    T v[kFetchBatch];
+#pragma unroll
+    for (int k = 0; k < kFetchBatch; ++k) {
+      const int i = i0 + k * kStride;
+      if (i < ps.nh) v[k] = in[hidx[i]];
+    }
+#pragma unroll
+    for (int k = 0; k < kFetchBatch; ++k) {
+      const int i = i0 + k * kStride;
+      if (i < ps.nh) ld[ps.n_own + i] = v[k];
+    }
+  }
+}
+
 // Lagged decisions (mixed sweeps). After its colour phases each CTA folds its maximum |res|
 // into the ring slot of sweep G (one atomicMax of a key that carries the sweep, kept for the
 // report of the final residual) and, behind a release, adds its arrival to the slot's word:
@@ -1215,7 +1275,9 @@ __device__ __forceinline__ void wait_neighbours(const Args &a, const PatchSmem &
 // when some are NaN) with a single load. Every CTA reads every sweep of a solve in order (the
 // sweeps left undecided at the end of a linear solve are drained), so that difference holds
 // exactly the sweep's arrivals; a count above the team's size means that the slot was refilled
-// before it was read (cannot happen with lag <= kMaxLag).
+// before it was read (cannot happen with lag <= kMaxLag). The halo sweeps' arrival reads the
+// previous sweep's word ahead, its load overlapping the arrival's fence, and the decision uses
+// that value when it already holds the whole sweep.
 __device__ __forceinline__ unsigned long long lag_increment(unsigned long long mx_bits, double tol, unsigned int G,
                                                             unsigned long long *key) {
   const float r = __double2float_ru(__longlong_as_double((long long)mx_bits));
@@ -1256,10 +1318,16 @@ __device__ __forceinline__ void lag_arrive(const SsaArgs &a, unsigned int G, uns
 // slot's maximum, and every write of the CTA before the barrier, before both the arrival and
 // the progress counter (a fence followed by relaxed writes is a release of each of them).
 template <class Team>
-__device__ __forceinline__ void lag_arrive_publish(const SsaArgs &a, const Team &t, unsigned int G,
+__device__ __forceinline__ void lag_arrive_publish(const SsaArgs &a, const Team &t, PatchSmem &ps, unsigned int G,
                                                    unsigned long long mx_bits, unsigned int value) {
+  // sweep G - 1's word, read ahead for lag_decide: its load overlaps the reduction and the fence
+  unsigned long long pre = 0ull;
+  if (threadIdx.x == 0 && G > 0u)
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(pre) : "l"(&a.ctl->lag_word[(G - 1u) % kLagRing]) : "memory");
   const unsigned long long x = block_max_u64(mx_bits);
   if (threadIdx.x == 0) {
+    ps.lag_pre = pre;
+    ps.lag_pre_g = G - 1u;
     unsigned long long key;
     const unsigned long long inc = lag_increment(x, a.tol, G, &key);
     atomicMax(&a.ctl->lag_res[G % kLagRing], key);
@@ -1278,7 +1346,13 @@ __device__ __forceinline__ int lag_decide(const SsaArgs &a, const Team &t, Patch
     const unsigned long long *wp = &a.ctl->lag_word[slot];
     const unsigned long long n = (unsigned long long)t.size();
     const unsigned long long prev = ps.lag_prev[slot];
-    unsigned long long d = ld_acquire_u64(wp) - prev;
+    unsigned long long d = 0ull;
+    bool have = false;   // the word read ahead holds the whole sweep
+    if (ps.lag_pre_g == G) {
+      d = ps.lag_pre - prev;
+      have = (d & 0xffffull) == n;
+    }
+    if (!have) d = ld_acquire_u64(wp) - prev;
     int act = 0;
     if ((d & 0xffffull) < n) {
       const unsigned long long t0 = globaltimer_ns();
@@ -1361,10 +1435,12 @@ __device__ __forceinline__ void load_patch(const Args &a, int b, PatchSmem &ps) 
 // patches of its start-of-sweep wait into shared memory.
 __device__ __forceinline__ void load_patch_halo(const SsaArgs &a, int b, PatchSmem &ps) {
   if (threadIdx.x < 8) ps.lag_prev[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) ps.lag_pre_g = 0xffffffffu;
   if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
   if (threadIdx.x < 8) ps.hps[threadIdx.x] = a.hp_slice[b * 7 + threadIdx.x];
   if (threadIdx.x == 0) {
     ps.nsync = a.hsync_ptr[b + 1] - a.hsync_ptr[b];
+    ps.hsplit = a.hp_split[b];
     ps.hl0 = a.hload_ptr[b];
     ps.nh = a.hload_ptr[b + 1] - a.hload_ptr[b];
   }
@@ -1400,6 +1476,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
                      (kMode != kExact64 && a.local_rows) ? (ps.ps[kGroups] - ps.ps[0]) * kSlice : 0};
   T *const hbuf0 = reinterpret_cast<T *>(kM ? (void *)a.dUV : (void *)a.UV);
   T *const hbuf1 = reinterpret_cast<T *>(kM ? (void *)a.dUVb : (void *)a.UVb);
+  T *const hbuf2 = reinterpret_cast<T *>(kM ? (void *)a.dUVc : (void *)a.UVc);
   T *const hld = reinterpret_cast<T *>(ufe_local_rows);
   int *const hidx = reinterpret_cast<int *>(ufe_local_rows + (size_t)a.halo_index_off);
   unsigned char *const hstage = ufe_local_rows + (size_t)a.stage_off;
@@ -1410,14 +1487,15 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
   }
   // (Re)load the mirror from global memory: at the start and after the grid-wide phases
   // that rewrite every row (fold, reset). Halo sweeps: the own rows of the working copy, also
-  // copied into the second buffer, which then holds every row that no sweep writes (Dirichlet
-  // rows) as well.
+  // copied into the other two buffers, which then hold every row that no sweep writes
+  // (Dirichlet rows) as well.
   auto reload = [&]() {
     if constexpr (kHalo) {
       for (int i = threadIdx.x; i < ps.n_own; i += blockDim.x) {
         const T v = hbuf0[ps.p0 + i];
         hld[i] = v;
         hbuf1[ps.p0 + i] = v;
+        hbuf2[ps.p0 + i] = v;
       }
       __syncthreads();
       return;
@@ -1465,13 +1543,17 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
     int did_reset = 0;
     double maxres = 0.0;
     if constexpr (kHalo) {
-      // Halo sweeps. A sweep waits once for the patches whose rows it reads (they finished
-      // the previous sweep, so the buffer `par` holds their rows) and for those that read its
-      // rows (they are done reading the buffer it is about to write), loads its halo slots,
-      // runs the seven phases on its working copy with CTA barriers only, and writes its own
-      // rows to buffer par ^ 1. Sync points commit the own rows to the canonical buffer.
+      // Halo sweeps. Every patch's rows of a sweep go to the next of three buffers (cur: the one
+      // holding the latest rows). A sweep first runs colour 1's own rows that read no halo slot
+      // (their inputs are own rows of the working copy; the buffer it writes was last read by
+      // the neighbouring patches two sweeps ago, before they completed the sweep this patch
+      // waited for at the start of the previous one), then waits once for the patches whose rows
+      // it reads and that read its rows (they finished the previous sweep, so buffer cur holds
+      // their rows), loads its halo slots, and runs the rest of the seven phases on its working
+      // copy with CTA barriers only. Sync points commit the own rows to the canonical buffer.
       constexpr bool kLag = kM && kMixedLag > 0;
-      int par = 0;
+      auto hb = [&](int i) { return i == 0 ? hbuf0 : i == 1 ? hbuf1 : hbuf2; };
+      int cur = 0;
       bool synced = true;
       int decided = 0;
       const unsigned int base = gsweep;
@@ -1483,17 +1565,29 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         const unsigned int G = gsweep++;
         const int slot = sweeps % 3;
         if (!kLag && leader) ctl->maxres[(sweeps + 1) % 3] = 0ull;
-        if (!synced) wait_neighbours(a, ps, phases, t.bar());
-        halo_load(ps, hidx, hld, par ? hbuf1 : hbuf0);
+        T *const out = hb(cur == 2 ? 0 : cur + 1);
+        auto colour = [&](int s_begin, int s_end, int nw) -> unsigned long long {
+          if constexpr (kM) return halo_colour32(a, ps, s_begin, s_end, nw, hstage, hidx, hld, out);
+          else return halo_colour64<kMode == kExact64>(a, ps, s_begin, s_end, nw, hld, out);
+        };
+        // the last kFetchWarps warps wait for the neighbouring patches and load the halo slots
+        // while the others run colour 1's halo-free rows
+        // (the FP64 modes, with a team barrier after every sweep, wait for nothing here and run
+        // colour 1 whole)
+        const int nwarps = blockDim.x >> 5;
+        unsigned long long mx = 0ull;
+        if constexpr (kLag) {
+          if ((int)(threadIdx.x >> 5) < nwarps - kFetchWarps) mx = colour(ps.hps[0], ps.hsplit, nwarps - kFetchWarps);
+          else halo_fetch(a, ps, phases, t.bar(), !synced, hidx, hld, hb(cur));
+        } else {
+          halo_load(ps, hidx, hld, hb(cur));
+        }
         __syncthreads();
         UFE_TM(kTmWaitColour);
-        T *const out = par ? hbuf0 : hbuf1;
-        unsigned long long mx = 0ull;
         for (int f = 0; f < 5; ++f) {
-          if (ps.hps[f + 1] == ps.hps[f]) continue;
-          unsigned long long m;
-          if constexpr (kM) m = halo_colour32(a, ps, f, hstage, hidx, hld, out);
-          else m = halo_colour64<kMode == kExact64>(a, ps, f, hld, out);
+          const int s_begin = f == 0 && kLag ? ps.hsplit : ps.hps[f];
+          if (ps.hps[f + 1] == s_begin) continue;
+          const unsigned long long m = colour(s_begin, ps.hps[f + 1], nwarps);
           mx = m > mx ? m : mx;
           __syncthreads();
           UFE_TM_SUB(kTmColour0 + f);
@@ -1505,17 +1599,17 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
           __syncthreads();
         }
         UFE_TM(kTmBoundary);
-        par ^= 1;
+        cur = cur == 2 ? 0 : cur + 1;
         if constexpr (kLag) {
           ++phases;
-          lag_arrive_publish(a, t, G, mx, phases);
+          lag_arrive_publish(a, t, ps, G, mx, phases);
           UFE_TM(kTmArrive);
           synced = false;
           const bool refold_now = a.refold > 0 && sweeps % a.refold == 0;
           const bool sync_point = sweeps == a.max_inner || refold_now;
           if (sync_point) {
-            if (par) halo_store_own(ps, hld, hbuf0);
-            par = 0;
+            if (cur) halo_store_own(ps, hld, hbuf0);
+            cur = 0;
             UFE_GRID_SYNC();
             synced = true;
             UFE_TM(kTmGrid);
@@ -1538,7 +1632,7 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
             phase_zero_velocity(a, t, kM);
             UFE_GRID_SYNC();
             reload();
-            par = 0;
+            cur = 0;
             did_reset = 1;
             lin_done = true;
           } else if (sweeps == a.max_inner) {
@@ -1564,14 +1658,14 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
             phase_zero_velocity(a, t, kM);
             UFE_GRID_SYNC();
             reload();
-            par = 0;
+            cur = 0;
             did_reset = 1;
             lin_done = true;
           } else if (sweeps == a.max_inner) {
             if (leader) ctl->not_converged += 1;
           } else if (kM && a.refold > 0 && sweeps % a.refold == 0) {
-            if (par) halo_store_own(ps, hld, hbuf0);
-            par = 0;
+            if (cur) halo_store_own(ps, hld, hbuf0);
+            cur = 0;
             UFE_GRID_SYNC();
             phase_fold(a, t);
             UFE_GRID_SYNC();
@@ -1587,8 +1681,8 @@ __device__ bool solve_member(const SsaArgs &a, Team &t) {
         if (!lag_drain(a, t, ps, base, decided, sweeps, leader, maxres)) return false;
       }
       // the final own rows into the canonical buffer before the grid-wide phases read it
-      const bool commit = par || (kLag && !synced);
-      if (par) halo_store_own(ps, hld, hbuf0);
+      const bool commit = cur || (kLag && !synced);
+      if (cur) halo_store_own(ps, hld, hbuf0);
       if (commit) UFE_GRID_SYNC();
       UFE_TM(kTmGrid);
     } else
@@ -2421,8 +2515,8 @@ struct SsaWork {
   double *f = nullptr;           // Hi, Hb, SL, hx, hy, Af, beta, tau, phi, eta, Na, Nb, S
   double2 *UV = nullptr, *rhs = nullptr, *euv = nullptr, *rcp = nullptr;
   float2 *dUV = nullptr, *r0 = nullptr, *rcp32 = nullptr;
-  double2 *UVb = nullptr;        // halo sweeps: second velocity buffer (FP64 modes)
-  float2 *dUVb = nullptr;        // halo sweeps: second correction buffer (mixed)
+  double2 *UVb = nullptr, *UVc = nullptr;   // halo sweeps: second and third velocity buffers (FP64 modes)
+  float2 *dUVb = nullptr, *dUVc = nullptr;  // halo sweeps: second and third correction buffers (mixed)
   float4 *hsd32 = nullptr;       // halo sweeps: per-slot row data (mixed)
   double2 *hrcp = nullptr, *hrhs = nullptr;   // halo sweeps: per-slot row data (fast FP64)
   float4 *bc0 = nullptr;         // mixed: boundary offsets per edge ordinal
@@ -2447,7 +2541,7 @@ void ssa_free(SsaWork *w) {
   if (!w) return;
   void *ptrs[] = {w->stage_in, w->stage_out, w->gl_int, w->gl_dbl, w->f, w->UV, w->rhs, w->euv,
                   w->rcp, w->dUV, w->r0, w->rcp32, w->skip, w->rn_part, w->prog, w->ctl, w->fh,
-                  w->UVb, w->dUVb, w->hsd32, w->hrcp, w->hrhs, w->bc0};
+                  w->UVb, w->dUVb, w->UVc, w->dUVc, w->hsd32, w->hrcp, w->hrhs, w->bc0};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (w->ctl_host) cudaFreeHost(w->ctl_host);
@@ -2485,6 +2579,8 @@ int ensure_work(ufe_mesh_h h) {
   if (!rc) rc = cuda_status(cudaMalloc(&w->bc0, ((size_t)m.n_edge_total + 1) * sizeof(float4)), "ssa bc0");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->UVb, (size_t)m.nP * sizeof(double2)), "ssa UVb");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->dUVb, (size_t)m.nP * sizeof(float2)), "ssa dUVb");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->UVc, (size_t)m.nP * sizeof(double2)), "ssa UVc");
+  if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->dUVc, (size_t)m.nP * sizeof(float2)), "ssa dUVc");
   const size_t nslots = (size_t)m.n_hslices * kSlice;
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hsd32, nslots * sizeof(float4)), "ssa hsd32");
   if (!rc && m.has_halo) rc = cuda_status(cudaMalloc(&w->hrcp, nslots * sizeof(double2)), "ssa hrcp");
@@ -2688,7 +2784,8 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->hp_slice = m.hp_slice; a->hslice_e0 = m.hslice_e0; a->hslice_w = m.hslice_w; a->hrow_l = m.hrow_l;
   a->hrow_g = m.hrow_g; a->hcol = m.hcol; a->hcuv32 = m.hcuv32; a->hcuv = m.hcuv; a->hload_ptr = m.hload_ptr;
   a->hload_dev = m.hload_dev; a->hsync_ptr = m.hsync_ptr; a->hsync_list = m.hsync_list;
-  a->UVb = w->UVb; a->dUVb = w->dUVb; a->hs3_32 = m.hs3_32; a->hs3 = m.hs3;
+  a->UVb = w->UVb; a->dUVb = w->dUVb; a->UVc = w->UVc; a->dUVc = w->dUVc; a->hs3_32 = m.hs3_32; a->hs3 = m.hs3;
+  a->hp_split = m.hp_split;
   a->hsd32 = w->hsd32; a->hrcp = w->hrcp; a->hrhs = w->hrhs;
   a->bc0 = w->bc0; a->n_edge = m.n_edge_total;
   a->prog = w->prog; a->nP = m.nP; a->nSlices = m.nSlices; a->ncm = m.ncm;
