@@ -1460,7 +1460,7 @@ __device__ __forceinline__ void load_patch_halo(const SsaArgs &a, int b, PatchSm
 // The whole solve_SSA of one problem, run by the CTAs of a team (each CTA owns one patch).
 // Returns false when a bounded wait failed; the error is recorded in the problem's control
 // block and the team's barrier counter. kHalo: the halo sweeps (one neighbour wait per
-// sweep, the patch's working copy in shared memory, velocities double-buffered by sweep).
+// sweep, the patch's working copy in shared memory, velocities in three buffers by sweep).
 template <int kMode, class Team, bool kHalo = false>
 __device__ bool solve_member(const SsaArgs &a, Team &t) {
   constexpr bool kM = kMode == kMixed;
