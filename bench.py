@@ -74,7 +74,7 @@ def mesh_counts(mesh):
     return dict(nV=nV, nA=nA, nnz_all=nnz_all, nnz_act=nnz_act, n_act=n_act, n_edge=n_edge, nb_bnd=nb_bnd)
 
 
-def algorithmic_bytes(c, st, mixed: bool, refold: int = 128):
+def algorithmic_bytes(c, st, mixed: bool, refold: int = 256):
     """Compulsory DRAM bytes of one persistent-kernel launch (each array touched once per
     phase; neighbour gathers of U,V counted once through the row's own U,V)."""
     if not mixed:

@@ -94,7 +94,7 @@ typedef struct ufe_params {
   int32_t nZ;
   const double *zeta;             /* (nZ) */
   int32_t precision;              /* UFE_FP64 or UFE_MIXED */
-  int32_t mixed_refold_sweeps;    /* mixed: FP64 defect recomputed every this many sweeps (0 = default 128) */
+  int32_t mixed_refold_sweeps;    /* mixed: FP64 defect recomputed every this many sweeps (0 = default 256) */
   int32_t fp64_exact;             /* FP64: 1 = the reference's expression order, separately rounded
                                      multiplies and adds and IEEE divisions (bit-level parity mode);
                                      0 = fused multiply-adds and a reciprocal of the centre

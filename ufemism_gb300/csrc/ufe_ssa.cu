@@ -2803,9 +2803,10 @@ int launch_prepare(ufe_mesh_h h, const ufe_params *p, cudaStream_t s, SsaArgs *a
   a->max_inner = p->SSA_max_inner_loops; a->max_outer = p->SSA_max_outer_loops;
   a->sliding_law = p->sliding_law; a->has_beta = w->has_beta;
   w->sliding_law = p->sliding_law;
-  // 128 on the 200k dome: 226.0 ms per solve against 234.2 at 64 and 221.7 at 256, with the same
-  // error against the FP64 solve (1.17e-7) and the same sweep count within one
-  a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 128;
+  // 256 on the 200k dome: 221.7 ms per solve against 226.0 at 128 and 234.2 at 64 (halo sweeps
+  // before the resident slices), with the same error against the FP64 solve (1.17e-7) and the
+  // same sweep count within one
+  a->refold = p->mixed_refold_sweeps > 0 ? p->mixed_refold_sweeps : 256;
   a->fp32_visc = p->mixed_fp32_viscosity != 0;
   a->timeout_ns = wait_timeout_ns();
   return rc;
