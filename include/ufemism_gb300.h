@@ -195,8 +195,7 @@ int ufe_sia_solve(ufe_mesh_h mesh, const ufe_params *params, const ufe_sia_in *i
  * is DEVICE memory of the mesh's device (the mesh's device must be current), nothing is
  * allocated, and the Ac intermediates the caller leaves NULL live in a fixed scratch array of
  * the library (at most UFE_SIA_NOALLOC_MAX_AC Ac edges; larger meshes return UFE_BAD_ARG).
- * Up to 64 devices. The first call on a device looks up the scratch address: make it before
- * any stream capture. The scratch is shared by every call on a device: calls that overlap in
+ * Up to 64 devices. The scratch is shared by every call on a device: calls that overlap in
  * time (several threads, or several meshes of the same device) race on it and must be
  * serialised by the caller. Synchronous like ufe_sia_solve. The results stay in the caller's
  * arrays only, not on the handle: the call drops the SIA velocities an earlier ufe_sia_solve
