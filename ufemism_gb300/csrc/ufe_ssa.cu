@@ -1416,6 +1416,7 @@ __device__ __forceinline__ bool lag_drain(const SsaArgs &a, const Team &t, Patch
 template <class Args>
 __device__ __forceinline__ void load_patch(const Args &a, int b, PatchSmem &ps) {
   if (threadIdx.x < 8) ps.lag_prev[threadIdx.x] = 0ull;
+  if (threadIdx.x == 0) ps.lag_pre_g = 0xffffffffu;   // nothing read ahead (lag_decide)
   if (threadIdx.x <= kGroups) ps.ps[threadIdx.x] = a.patch_slice[b * (kGroups + 1) + threadIdx.x];
   if (threadIdx.x == 0) {
     ps.edge0 = a.patch_edge0[b];
