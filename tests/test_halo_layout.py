@@ -27,7 +27,7 @@ NO_COL = 0xFFFF
 DT = {1: np.uint8, 2: np.uint16, 4: np.int32, 8: np.float64}
 
 
-def dump_layout(mesh, num_sms=152):
+def dump_layout(mesh, num_sms=152, n_patch=0):
     d, keep = api._mesh_desc(mesh)
     L = nat.load()
     fn = L.ufe_debug_dump_layout
@@ -36,7 +36,7 @@ def dump_layout(mesh, num_sms=152):
     fd, path = tempfile.mkstemp(suffix=".bin")
     os.close(fd)
     try:
-        rc = fn(ct.byref(d), num_sms, 0, path.encode())
+        rc = fn(ct.byref(d), num_sms, n_patch, path.encode())
         assert rc == nat.UFE_OK, nat.last_error()
         out = {}
         with open(path, "rb") as f:
@@ -64,11 +64,13 @@ def dump_layout(mesh, num_sms=152):
     return arr
 
 
-@pytest.fixture(scope="module", params=["tiny", "1k", "4k"])
+@pytest.fixture(scope="module", params=[("tiny", 0), ("1k", 0), ("4k", 0), ("1k", 3), ("4k", 7)])
 def layout(request):
-    base = base_mesh(request.param)
+    """Single-solve layouts (a patch per SM) and batched members' (a patch per CTA of a team)."""
+    name, n_patch = request.param
+    base = base_mesh(name)
     mesh = api.build_aaac(base)
-    return mesh, dump_layout(mesh)
+    return mesh, dump_layout(mesh, n_patch=n_patch)
 
 
 def phases_of(mesh, lay):

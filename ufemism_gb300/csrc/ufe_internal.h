@@ -101,8 +101,9 @@ struct DevMesh {
   int *iAci = nullptr;          // [nV * ncm] column-major Ac ids (0-based), for map_Ac_to_Aa
   int *nC = nullptr;            // [nV]
 
-  // Halo sweep program (single solves). One SOR sweep runs in seven phases: colours 1..5,
-  // then the edge rows, then the corners. A patch updates, besides its own rows, the halo
+  // Halo sweep program (single solves; batched members in the mixed mode). One SOR sweep runs
+  // in seven phases: colours 1..5, then the edge rows, then the corners. A patch updates,
+  // besides its own rows, the halo
   // rows whose updates its own rows read within the same sweep (the closure of "reads a row
   // of an earlier phase"), with the same arithmetic, so that a whole sweep needs the
   // neighbouring patches only once, at its start. Its working copy of the velocities

@@ -405,7 +405,7 @@ int mesh_create(const ufe_mesh_desc *d, int n_patch_request, ufe_mesh_h *out) {
   std::vector<uint16_t> hcol;
   std::vector<float2> hcuv32;
   std::vector<double2> hcuv;
-  bool halo_ok = n_patch_request == 0;
+  bool halo_ok = true;
   if (halo_ok) {
     std::vector<int8_t> ph(m.nP, -1);
     for (int p = 0; p < m.nP; ++p) {

@@ -1878,7 +1878,8 @@ struct BatchArgs {
   long long timeout_ns;
 };
 
-template <int kMode, int kBlock, int kPerSm>
+// kHalo (mixed only): the members run the halo sweeps (every member has the program).
+template <int kMode, int kBlock, int kPerSm, bool kHalo = false>
 __global__ void __launch_bounds__(kBlock, kPerSm) ssa_batched(const BatchArgs b) {
   __shared__ SsaArgs a;
   const int team = b.team_of_cta[blockIdx.x];
@@ -1896,7 +1897,7 @@ __global__ void __launch_bounds__(kBlock, kPerSm) ssa_batched(const BatchArgs b)
     const unsigned int m = *(volatile unsigned int *)&b.team_member[32 * team];
     if (m >= (unsigned)b.n_members) return;
     stage_args(a, b.members + m);
-    if (!solve_member<kMode>(a, t)) {
+    if (!solve_member<kMode, SubTeam, kHalo>(a, t)) {
       if (threadIdx.x == 0) atomicCAS(b.err, 0, (int)UFE_TIMEOUT);
       return;
     }
@@ -3148,6 +3149,11 @@ struct ufe_batch_s {
   int n = 0;                          // members
   int block = 0;                      // threads per CTA of the batched kernel
   bool use_graph = true;
+  // mixed members on the halo sweeps: every member has the program and the largest working copy
+  // (plus halo indices) fits the CTAs the plan keeps resident
+  bool halo_ok = false;
+  int halo_index_off = 0, halo_stage_off = 0;
+  size_t halo_smem = 0;
   ufe_batch_plan_out plan{};
   int n_teams = 0;
   std::vector<int32_t> team_of_member;
@@ -3191,8 +3197,17 @@ void batch_free(ufe_batch_s *b) {
   delete b;
 }
 
-// The batched kernel for a sweep mode and CTA shape (nullptr: not built).
-const void *batched_kernel(int mode, int block) {
+// The batched kernel for a sweep mode and CTA shape (nullptr: not built); halo: the mixed
+// members' halo sweeps.
+const void *batched_kernel(int mode, int block, bool halo = false) {
+  if (halo) {
+    switch (mode * 10000 + block) {
+      case kMixed * 10000 + 1024: return (const void *)ssa_batched<kMixed, 1024, 1, true>;
+      case kMixed * 10000 + 512: return (const void *)ssa_batched<kMixed, 512, 2, true>;
+      case kMixed * 10000 + 256: return (const void *)ssa_batched<kMixed, 256, 4, true>;
+      default: return nullptr;
+    }
+  }
   switch (mode * 10000 + block) {
     case kExact64 * 10000 + 1024: return (const void *)ssa_batched<kExact64, 1024, 1>;
     case kFast64 * 10000 + 1024: return (const void *)ssa_batched<kFast64, 1024, 1>;
@@ -3260,6 +3275,11 @@ int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
     bool solve = false;
     SsaArgs a;
     rc = launch_prepare(b->members[m], p, s, &a, &solve);
+    if (!rc && solve && mode == kMixed && b->halo_ok) {
+      a.halo_index_off = b->halo_index_off;
+      a.stage_off = b->halo_stage_off;
+      a.stage_bytes = 0;
+    }
     if (!rc && solve) {
       const int c = (int)(std::find(pl.class_team_ctas, pl.class_team_ctas + nc, b->team_of_member[m]) -
                           pl.class_team_ctas);
@@ -3278,7 +3298,7 @@ int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
       ti[team] = make_int4(cta, pl.class_team_ctas[c], c, 0);
       for (int r = 0; r < pl.class_team_ctas[c]; ++r) tc[cta++] = team;
     }
-  const void *fn = batched_kernel(mode, b->block);
+  const void *fn = batched_kernel(mode, b->block);   // (the halo variant below when it applies)
   if (!rc && n_active > 0) {
     unsigned int *queue = b->sched, *team_bar = queue + 32 * (size_t)kMaxClasses;
     unsigned int *team_member = team_bar + 32 * (size_t)b->n_teams;
@@ -3298,10 +3318,13 @@ int batch_enqueue(ufe_batch_s *b, const ufe_params *p, int mode) {
     ba.team_of_cta = tcd; ba.team_info = tid; ba.class_range = reinterpret_cast<const int2 *>(tid + b->n_teams);
     ba.queue = queue; ba.team_bar = team_bar; ba.team_member = team_member;
     ba.times = b->times_dev; ba.err = b->err_dev; ba.timeout_ns = wait_timeout_ns();
+    const bool halo = mode == kMixed && b->halo_ok;
+    if (halo) fn = batched_kernel(mode, b->block, true);
     if (!rc) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)pl.grid_ctas);
       cfg.blockDim = dim3((unsigned)b->block);
+      cfg.dynamicSmemBytes = halo ? b->halo_smem : 0;
       cfg.stream = s;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeCooperative;
@@ -3381,6 +3404,33 @@ extern "C" int ufe_batch_create(const ufe_mesh_desc *descs, int32_t n, const ufe
       set_error("ufe_batch_create: member " + std::to_string(k) + ": " + e);
     }
     if (!rc) b->cost[k] = member_work(rows[k], 1, 1024);
+  }
+  if (!rc) {
+    // Mixed members run the halo sweeps when every member has the program and the largest working
+    // copy with its halo indices leaves the plan's CTAs co-resident (else the phased sweeps).
+    int max_local = 0, max_halo = 0;
+    bool all = true;
+    for (ufe_mesh_h h : b->members) {
+      all = all && h->m.has_halo;
+      max_local = std::max(max_local, h->m.max_local);
+      max_halo = std::max(max_halo, h->m.max_halo);
+    }
+    const void *fn = batched_kernel(kMixed, block, true);
+    if (all && fn) {
+      const size_t idx_off = (size_t)max_local * sizeof(float2);
+      const size_t stage_off = (idx_off + (size_t)max_halo * sizeof(int) + 15) / 16 * 16;
+      int per_sm = 0;
+      int rc2 = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_off),
+                            "batch smem attribute");
+      if (!rc2) rc2 = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, stage_off), "occupancy");
+      if (!rc2 && per_sm * b->num_sms >= b->plan.grid_ctas) {
+        b->halo_ok = true;
+        b->halo_index_off = (int)idx_off;
+        b->halo_stage_off = (int)stage_off;
+        b->halo_smem = stage_off;
+      }
+      if (rc2) rc = rc2;
+    }
   }
   if (!rc) {
     b->n_teams = 0;
