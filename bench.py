@@ -800,7 +800,7 @@ def main():
                     help="dome: the 200k-vertex single solve; ensemble: the batched ensemble")
     ap.add_argument("--members", type=int, default=256)
     ap.add_argument("--autotune", action="store_true", help="ensemble: run the autotuner first")
-    ap.add_argument("--rows-per-cta", type=int, default=8192)
+    ap.add_argument("--rows-per-cta", type=int, default=16384)
     ap.add_argument("--block", type=int, default=1024)
     args = ap.parse_args()
     if args.impl == "reference":
