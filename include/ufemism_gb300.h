@@ -393,7 +393,10 @@ int ufe_ssa_vjp(ufe_mesh_h mesh, const ufe_params *params, const ufe_vjp_params 
  * each class gets CTAs in proportion to its estimated work. With use_graph the whole batch
  * (gathers, the persistent solve, scatters) is captured once per parameter set and upload
  * state and replayed as a CUDA graph. Members share one ufe_params; their inputs are
- * uploaded one by one (the arrays of ufe_ssa_upload). */
+ * uploaded one by one (the arrays of ufe_ssa_upload). In the mixed precision the members run
+ * the halo sweeps of the single solves when the largest member's working copy fits beside the
+ * CTAs the plan keeps resident (else the phased sweeps); either gives each member the result of
+ * its single solve. */
 typedef struct ufe_batch_s *ufe_batch_h;
 typedef struct ufe_batch_config {
   int32_t team_ctas;     /* > 0: every member solved by a team of this many CTAs */
