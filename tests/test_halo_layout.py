@@ -243,3 +243,25 @@ def test_halo_sweeps_equal_the_sequential_sweep(layout):
     got = buf[par]
     live = ph >= 0
     assert np.array_equal(got[live], U[live])
+
+
+def test_halo_gathers_spread_over_banks():
+    """The program's slots are dealt bank-aware: a slice's k-th gather from the working copy
+    (8-byte elements, local index l in bank pair l mod 16) costs one shared-memory wavefront per
+    element in its busiest bank pair. Degree-sorted order alone gives about 4.3 per gather on a
+    200k-vertex mesh; the assignment keeps it near 3 (2 at best for 32 distinct elements)."""
+    base = base_mesh("4k")
+    mesh = api.build_aaac(base)
+    lay = dump_layout(mesh)
+    hp, e0, w, hcol = lay["hp_slice"], lay["hslice_e0"], lay["hslice_w"], lay["hcol"]
+    loads, best = [], []
+    for s in range(int(hp[0]), int(hp[-1])):
+        for k in range(int(w[s])):
+            c = hcol[int(e0[s]) + 32 * k + np.arange(32)]
+            u = np.unique(c[c != NO_COL].astype(np.int64))
+            if u.size == 0:
+                continue
+            loads.append(np.bincount(u % 16, minlength=16).max())
+            best.append(-(-u.size // 16))
+    assert np.mean(loads) <= 3.2, np.mean(loads)
+    assert np.mean(loads) >= np.mean(best)
