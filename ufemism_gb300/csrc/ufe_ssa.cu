@@ -37,8 +37,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "ufe_internal.h"
@@ -3220,6 +3223,23 @@ const void *batched_kernel(int mode, int block, bool halo = false) {
   }
 }
 
+// Raises a batched kernel's dynamic shared-memory limit on a device to at least `bytes`, never
+// lowering it (batches alive at the same time share the kernel, and a captured batch replays with
+// the size it was captured with); false when the device cannot give that much.
+bool raise_dynamic_smem(const void *fn, int device, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &cur = limit[std::make_pair(device, fn)];
+  if (bytes <= cur) return true;
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  cur = bytes;
+  return true;
+}
+
 // Co-resident CTAs of the batched kernels of one CTA size (the smallest over the modes).
 int resident_ctas(int block, int num_sms, int *out) {
   int per_sm = 1 << 30;
@@ -3420,16 +3440,16 @@ extern "C" int ufe_batch_create(const ufe_mesh_desc *descs, int32_t n, const ufe
       const size_t idx_off = (size_t)max_local * sizeof(float2);
       const size_t stage_off = (idx_off + (size_t)max_halo * sizeof(int) + 15) / 16 * 16;
       int per_sm = 0;
-      int rc2 = cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)stage_off),
-                            "batch smem attribute");
-      if (!rc2) rc2 = cuda_status(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, stage_off), "occupancy");
-      if (!rc2 && per_sm * b->num_sms >= b->plan.grid_ctas) {
+      if (raise_dynamic_smem(fn, b->device, stage_off) &&
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, stage_off) == cudaSuccess &&
+          per_sm * b->num_sms >= b->plan.grid_ctas) {
         b->halo_ok = true;
         b->halo_index_off = (int)idx_off;
         b->halo_stage_off = (int)stage_off;
         b->halo_smem = stage_off;
+      } else {
+        cudaGetLastError();   // a working copy too large for the device: the phased sweeps
       }
-      if (rc2) rc = rc2;
     }
   }
   if (!rc) {
